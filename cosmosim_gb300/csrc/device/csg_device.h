@@ -1,0 +1,101 @@
+/*
+ * csg_device.h — the thin C-ABI between the C11 host layer and the CUDA
+ * kernels. Everything here is plain C: opaque handles, pointers and sizes.
+ *
+ * A csgd_t holds one simulation's device state on one CUDA stream:
+ *   - bodies as FP64 structure-of-arrays in the caller's index order
+ *     (x,y,z, vx,vy,vz, ax,ay,az, mass, type, density, pressure, u, h),
+ *   - the octree in depth-first (preorder) layout, built every substep from
+ *     63-bit octant keys (see dev_tree.cu),
+ *   - scratch for the key sort, the tree and the Body array-of-structs staging.
+ * All calls are asynchronous on the state's stream unless they say otherwise;
+ * csgd_sync() waits and reports the first error.
+ */
+#ifndef CSG_DEVICE_H
+#define CSG_DEVICE_H
+
+#include <stdint.h>
+#include "../../../include/cosmosim_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct csgd csgd_t;
+
+/* Error codes and precisions: CSG_OK, CSG_ERR_*, CSG_PREC_* (cosmosim_gb300.h). */
+
+typedef struct {
+    double G, softening, theta;
+    int precision; /* CSG_PREC_* */
+} csgd_force_params;
+
+csgd_t *csgd_create(void);
+void csgd_destroy(csgd_t *d);
+
+/* Uses the given cudaStream_t (NULL = the state's own stream). */
+void csgd_set_stream(csgd_t *d, void *stream);
+void *csgd_stream(csgd_t *d);
+
+/* Makes room for n bodies (grow-only). */
+int csgd_reserve(csgd_t *d, int n);
+int csgd_count(const csgd_t *d);
+
+/* Body array-of-structs <-> device SoA (host buffers may be pageable). */
+int csgd_upload_bodies(csgd_t *d, const Body *host, int n);
+int csgd_download_bodies(csgd_t *d, Body *host, int n);
+
+/* Tree build over the current positions/masses. With geometry != 0 it also
+   computes every cell's geometric centre (needed by SPH and pool export). */
+int csgd_build_tree(csgd_t *d, int geometry);
+
+/* Accelerations a = Barnes-Hut gravity (overwrites a; dead bodies get 0).
+   exact != 0 uses the reference's own FP64 operation sequence. */
+int csgd_gravity(csgd_t *d, const csgd_force_params *p);
+int csgd_gravity_ex(csgd_t *d, const csgd_force_params *p, int exact);
+
+/* SPH on the current tree (needs geometry). */
+int csgd_sph_density(csgd_t *d);
+int csgd_sph_forces(csgd_t *d);
+int csgd_sph_cooling(csgd_t *d, double dt);
+
+/* Leapfrog pieces: v += a*dt/2 and x += v*dt; and v += a*dt/2. */
+int csgd_kick_drift(csgd_t *d, double dt);
+int csgd_kick(csgd_t *d, double dt);
+
+/* One full KDK substep, all on the device (reference src/integrator.c:12-57). */
+int csgd_substep(csgd_t *d, double dt, const csgd_force_params *p, int sph);
+
+/* The tree as a reference-layout pool, in the reference's allocation order.
+   Blocks until done. pool must hold *pool_size_out <= capacity nodes. */
+int csgd_export_pool(csgd_t *d, OctreeNode *pool, int capacity, int *pool_size_out);
+
+/* Replaces the device tree by the caller's pool (nodes reachable from root;
+   n_nodes = highest reachable index + 1). */
+int csgd_import_pool(csgd_t *d, const OctreeNode *pool, int n_nodes, int root);
+
+/* Neighbour query on the current tree, reference semantics (first cap alive
+   bodies within radius in depth-first order). Blocks until done. */
+int csgd_find_neighbors(csgd_t *d, double cx, double cy, double cz, double radius, int *buf,
+                        int cap, int *count_out);
+
+/* Node count of the current tree (blocks). */
+int csgd_node_count(csgd_t *d, int *n_nodes);
+
+/* Interaction count summed over gravity walks since the last reset (only
+   while stats are enabled). */
+void csgd_enable_stats(csgd_t *d, int on);
+int csgd_reset_stats(csgd_t *d);
+int csgd_interactions(csgd_t *d, int64_t *total);
+
+/* Alive bodies (mass > 0 or NaN, as the reference's mass <= 0 test). Blocks. */
+int csgd_alive_count(csgd_t *d, int *count);
+
+/* Waits for the stream; returns CSG_OK or the first error (CUDA or device). */
+int csgd_sync(csgd_t *d);
+const char *csgd_error_string(int code);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

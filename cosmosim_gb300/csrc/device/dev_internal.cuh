@@ -1,0 +1,132 @@
+// dev_internal.cuh — device state and node layouts shared by the .cu files.
+//
+// Tree layout (all arrays indexed by node id; ids are depth-first preorder):
+//   a node's first child is id+1 and the node after its subtree is `next`, so
+//   a walk that either descends (id+1) or skips (next) visits cells in the
+//   reference's depth-first octant order 0..7 (src/octree.c:213-217) with no
+//   stack at all.
+//   NodeW64  — FP64 walk record: centre of mass, mass, opening size s^2, next, body
+//   NodeW32  — FP32 walk record: the same in FP32 (mass-weighted centre rounded)
+//   geo      — geometric centre and half size (SPH neighbour search, export)
+//   link     — parent, level, first sorted body, body count
+//   child    — 8 child ids per node in octant order (export, moments)
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "csg_device.h"
+
+#define CSG_WARP 32
+#define CSG_MAX_LEVEL 64  // reference src/octree.c:5 (MAX_DEPTH)
+#define CSG_KEY_LEVELS 21 // levels held by the 63-bit primary key
+#define CSG_DEAD_KEY 0xFFFFFFFFFFFFFFFFull
+
+struct __align__(16) NodeW64 {
+    double cx, cy, cz, m;
+    double s2;      // (2 * half_size)^2, the reference's s*s (src/octree.c:202-203)
+    int next;       // id after this subtree
+    int body;       // caller body index for a leaf, -1 for an internal cell
+};
+
+// FP32 walk record: the centre of mass is held as a float hi/lo pair so that
+// body-to-cell differences keep ~48 bits; everything after the difference is
+// FP32 (rsqrt, products, compensated sums).
+struct __align__(16) NodeW32 {
+    float cx, cy, cz, m;    // hi parts of the centre of mass, mass
+    float lx, ly, lz, s2;   // lo parts (centre - hi), s^2
+    int next;
+    int body;
+    float s;                // 2 * half_size
+    float pad;
+};
+
+struct __align__(16) NodeLink {
+    int parent;
+    int level;
+    int first;  // first sorted position of the cell's bodies
+    int count;  // number of bodies in the cell
+};
+
+// Per-build scalars kept on the device so that no step needs a host round trip.
+struct DevScalars {
+    unsigned long long omin[3], omax[3]; // order-preserving bbox encodings
+    double c0[3];                        // root centre
+    double hs0;                          // root half size
+    double key_scale;                    // 2^20 / hs0 (fast key path)
+    double key_tol;                      // fast-path guard, in key grid units
+    int fast_keys;                       // 1 when the fast key path is safe
+    int n_alive;
+    int n_nodes;
+    int deep;                            // positions that share a 63-bit key
+    int err;                             // first device error code (0 = none)
+    int n_gas;
+    unsigned long long interactions;     // walk statistics (when enabled)
+    unsigned long long key_slow;         // bodies that took the exact key path
+    int alive_count;                     // csgd_alive_count result
+};
+
+struct csgd {
+    cudaStream_t stream;
+    cudaStream_t own_stream;
+    int n;        // bodies in use
+    int cap;      // body capacity
+    int node_cap; // node capacity (8*cap + 64)
+    int stats;
+    int host_err; // first error seen on the host side (launch, allocation)
+
+    // bodies, caller index order
+    double *x, *y, *z, *vx, *vy, *vz, *ax, *ay, *az, *m;
+    double *rho, *P, *u, *h;
+    int *type;
+    Body *aos;        // Body staging for host I/O
+    OctreeNode *pool; // reference-layout staging for export/import
+
+    // keys and sort
+    unsigned long long *key, *key_alt;
+    int *perm, *perm_alt;
+    unsigned long long *ext; // 3 words per sorted position (deep cells only)
+    unsigned int *sort_hist;
+    int sort_hist_cap;
+
+    // per sorted position
+    signed char *lcp;  // lcp with the next position, in levels (-1 at the end)
+    int *cnt, *base;   // node counts and their exclusive scan (cap+1)
+    int *scan_tmp;
+    int scan_tmp_cap;
+    int *gas;          // gas bodies in key order (caller indices)
+
+    // nodes
+    NodeW64 *w64;
+    NodeW32 *w32;
+    NodeLink *link;
+    double4 *geo;
+    int *child;   // 8 per node
+    int *nchild;
+    int *ticket;
+    int2 *minidx; // two smallest caller indices below each cell (export order)
+    unsigned long long *ord_key, *ord_key_alt;
+    int *ord_id, *ord_id_alt, *rank;
+
+    DevScalars *sc;      // device
+    DevScalars *sc_host; // pinned mirror
+    int geometry_valid;
+    int imported; // the tree came from a caller pool (no sorted order)
+};
+
+// ---- helpers shared by the .cu files ----
+int csgd_check(csgd_t *d, cudaError_t e);
+void csgd_set_err(csgd_t *d, int code);
+int csgd_grid(long long n, int block);
+
+// ---- sort / scan utilities (dev_sort.cu) ----
+// Stable LSD radix sort of (key, value) over n items, on key bits [0, bits).
+// Result in (key, val); alt buffers are scratch of the same size.
+int csg_radix_sort(csgd_t *d, unsigned long long *key, int *val, unsigned long long *key_alt,
+                   int *val_alt, int n, int bits);
+// Exclusive scan of in[0..n) into out[0..n], out[n] = total. count_limit, when
+// non-NULL, is a device int: items at positions >= *count_limit count as 0.
+int csg_scan_exclusive(csgd_t *d, const int *in, int *out, int n, const int *count_limit);
+
+// ---- device error codes written to DevScalars::err ----
+__device__ __forceinline__ void dev_fail(DevScalars *sc, int code) { atomicCAS(&sc->err, 0, code); }

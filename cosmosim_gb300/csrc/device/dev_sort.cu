@@ -1,0 +1,243 @@
+// dev_sort.cu — exclusive scan and stable LSD radix sort used by the tree build.
+//
+// Radix sort: 8-bit digits, three kernels per digit (tile histogram, scan of
+// the digit-major histogram, stable scatter). Stability inside a tile comes
+// from giving each warp a contiguous slice of the tile and ranking equal
+// digits with __match_any_sync in input order; across tiles from the
+// digit-major exclusive scan. Stability matters: keys that tie keep caller
+// index order, which the tree build relies on (reference inserts bodies in
+// index order, src/octree.c:163-168).
+#include "dev_internal.cuh"
+
+namespace {
+
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+constexpr int SORT_THREADS = 256;
+constexpr int SORT_WARPS = SORT_THREADS / CSG_WARP;
+constexpr int SORT_ITEMS_PER_LANE = 16;
+constexpr int SORT_WARP_ITEMS = CSG_WARP * SORT_ITEMS_PER_LANE; // 512
+constexpr int SORT_TILE = SORT_WARPS * SORT_WARP_ITEMS;          // 4096
+constexpr int RADIX = 256;
+
+__device__ __forceinline__ int warp_incl_scan(int v)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o)
+            v += t;
+    }
+    return v;
+}
+
+// Exclusive scan of one 4096-item tile; writes the tile total to sums[block].
+__global__ void k_scan_tile(const int *__restrict__ in, int *__restrict__ out, int n,
+                            const int *__restrict__ limit, int *__restrict__ sums)
+{
+    __shared__ int warp_tot[SCAN_THREADS / 32];
+    const int lim = limit ? min(n, *limit) : n;
+    const long long base = (long long)blockIdx.x * SCAN_TILE + (long long)threadIdx.x * SCAN_ITEMS;
+    int v[SCAN_ITEMS];
+    int local = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        long long i = base + k;
+        v[k] = (i < lim) ? in[i] : 0;
+        local += v[k];
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int incl = warp_incl_scan(local);
+    if (lane == 31)
+        warp_tot[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        int t = warp_tot[lane];
+        int ti = warp_incl_scan(t);
+        warp_tot[lane] = ti - t;
+    }
+    __syncthreads();
+    int run = warp_tot[warp] + incl - local;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        long long i = base + k;
+        if (i < n)
+            out[i] = run;
+        run += v[k];
+    }
+    if (threadIdx.x == SCAN_THREADS - 1)
+        sums[blockIdx.x] = run;
+}
+
+__global__ void k_scan_add(int *__restrict__ out, int n, const int *__restrict__ offs)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        out[i] += offs[i / SCAN_TILE];
+}
+
+__global__ void k_scan_total(int *__restrict__ out, int n, const int *__restrict__ total)
+{
+    out[n] = *total;
+}
+
+// ---- radix sort kernels ----
+
+__global__ void k_radix_hist(const unsigned long long *__restrict__ key, int n, int shift,
+                             unsigned int *__restrict__ hist, int nblocks)
+{
+    __shared__ unsigned int h[RADIX];
+    for (int i = threadIdx.x; i < RADIX; i += blockDim.x)
+        h[i] = 0;
+    __syncthreads();
+    const long long t0 = (long long)blockIdx.x * SORT_TILE;
+    for (int k = threadIdx.x; k < SORT_TILE; k += blockDim.x) {
+        long long i = t0 + k;
+        if (i < n)
+            atomicAdd(&h[(unsigned)(key[i] >> shift) & (RADIX - 1)], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < RADIX; i += blockDim.x)
+        hist[(size_t)i * nblocks + blockIdx.x] = h[i];
+}
+
+__global__ void k_radix_scatter(const unsigned long long *__restrict__ key_in,
+                                const int *__restrict__ val_in,
+                                unsigned long long *__restrict__ key_out,
+                                int *__restrict__ val_out, int n, int shift,
+                                const int *__restrict__ offs, int nblocks)
+{
+    __shared__ int wcount[SORT_WARPS][RADIX];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < SORT_WARPS * RADIX; i += blockDim.x)
+        (&wcount[0][0])[i] = 0;
+    __syncthreads();
+    const long long w0 = (long long)blockIdx.x * SORT_TILE + (long long)warp * SORT_WARP_ITEMS;
+    const unsigned lt = (1u << lane) - 1u;
+    // pass 1: per-warp digit counts
+    for (int c = 0; c < SORT_ITEMS_PER_LANE; c++) {
+        long long i = w0 + c * CSG_WARP + lane;
+        int dg = (i < n) ? (int)((key_in[i] >> shift) & (RADIX - 1)) : RADIX;
+        unsigned peers = __match_any_sync(0xffffffffu, dg);
+        if (dg < RADIX && (peers & lt) == 0)
+            wcount[warp][dg] += __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // per digit: tile offset + counts of earlier warps
+    for (int dg = threadIdx.x; dg < RADIX; dg += blockDim.x) {
+        int run = offs[(size_t)dg * nblocks + blockIdx.x];
+        for (int w = 0; w < SORT_WARPS; w++) {
+            int c = wcount[w][dg];
+            wcount[w][dg] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    // pass 2: stable placement in input order
+    for (int c = 0; c < SORT_ITEMS_PER_LANE; c++) {
+        long long i = w0 + c * CSG_WARP + lane;
+        unsigned long long k = 0;
+        int v = 0;
+        int dg = RADIX;
+        if (i < n) {
+            k = key_in[i];
+            v = val_in[i];
+            dg = (int)((k >> shift) & (RADIX - 1));
+        }
+        unsigned peers = __match_any_sync(0xffffffffu, dg);
+        int pos = 0;
+        if (dg < RADIX) {
+            pos = wcount[warp][dg] + __popc(peers & lt);
+            key_out[pos] = k;
+            val_out[pos] = v;
+        }
+        __syncwarp();
+        if (dg < RADIX && (peers & lt) == 0)
+            wcount[warp][dg] += __popc(peers);
+        __syncwarp();
+    }
+}
+
+} // namespace
+
+int csg_scan_exclusive(csgd_t *d, const int *in, int *out, int n, const int *count_limit)
+{
+    if (n <= 0) {
+        cudaMemsetAsync(out, 0, sizeof(int), d->stream);
+        return csgd_check(d, cudaGetLastError());
+    }
+    // level sizes: n -> ceil(n/T) -> ... -> 1
+    int nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+    int *sums = d->scan_tmp;
+    int needed = 0;
+    for (int m = nb; m > 1; m = (m + SCAN_TILE - 1) / SCAN_TILE)
+        needed += 2 * m + 2;
+    needed += 2;
+    if (needed > d->scan_tmp_cap) {
+        csgd_set_err(d, CSG_ERR_NOMEM);
+        return CSG_ERR_NOMEM;
+    }
+    k_scan_tile<<<nb, SCAN_THREADS, 0, d->stream>>>(in, out, n, count_limit, sums);
+    if (nb > 1) {
+        // scan the block sums (exclusive, total at sums_out[nb]) and add back
+        int *sums_out = sums + nb + 1;
+        // temporarily shift the scratch window for the recursive level
+        int *saved = d->scan_tmp;
+        int saved_cap = d->scan_tmp_cap;
+        d->scan_tmp = sums_out + nb + 1;
+        d->scan_tmp_cap = saved_cap - 2 * (nb + 1);
+        int rc = csg_scan_exclusive(d, sums, sums_out, nb, nullptr);
+        d->scan_tmp = saved;
+        d->scan_tmp_cap = saved_cap;
+        if (rc)
+            return rc;
+        k_scan_add<<<csgd_grid(n, 256), 256, 0, d->stream>>>(out, n, sums_out);
+        k_scan_total<<<1, 1, 0, d->stream>>>(out, n, sums_out + nb);
+    } else {
+        k_scan_total<<<1, 1, 0, d->stream>>>(out, n, sums);
+    }
+    return csgd_check(d, cudaGetLastError());
+}
+
+int csg_radix_sort(csgd_t *d, unsigned long long *key, int *val, unsigned long long *key_alt,
+                   int *val_alt, int n, int bits)
+{
+    if (n <= 1)
+        return CSG_OK;
+    const int nblocks = (n + SORT_TILE - 1) / SORT_TILE;
+    const int hn = RADIX * nblocks;
+    if (2 * hn + 1 > d->sort_hist_cap) {
+        csgd_set_err(d, CSG_ERR_NOMEM);
+        return CSG_ERR_NOMEM;
+    }
+    unsigned int *hist = d->sort_hist;
+    int *offs = (int *)(d->sort_hist + hn);
+    unsigned long long *ki = key, *ko = key_alt;
+    int *vi = val, *vo = val_alt;
+    const int passes = (bits + 7) / 8;
+    for (int p = 0; p < passes; p++) {
+        const int shift = 8 * p;
+        k_radix_hist<<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, n, shift, hist, nblocks);
+        int rc = csg_scan_exclusive(d, (const int *)hist, offs, hn, nullptr);
+        if (rc)
+            return rc;
+        k_radix_scatter<<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, offs,
+                                                                  nblocks);
+        unsigned long long *tk = ki;
+        ki = ko;
+        ko = tk;
+        int *tv = vi;
+        vi = vo;
+        vo = tv;
+    }
+    if (ki != key) {
+        cudaMemcpyAsync(key, ki, sizeof(unsigned long long) * (size_t)n, cudaMemcpyDeviceToDevice,
+                        d->stream);
+        cudaMemcpyAsync(val, vi, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, d->stream);
+    }
+    return csgd_check(d, cudaGetLastError());
+}

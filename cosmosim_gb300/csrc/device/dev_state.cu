@@ -1,0 +1,490 @@
+// dev_state.cu — device state lifetime, Body I/O, leapfrog and cooling kernels.
+//
+// Compiled with -fmad=false: the leapfrog and cooling kernels then round every
+// operation exactly as the reference's C does (src/integrator.c:22-51,
+// src/sph.c:200-231), so given equal accelerations they agree bit for bit.
+#include "dev_internal.cuh"
+
+#include <stdlib.h>
+#include <string.h>
+
+namespace {
+
+constexpr double SPH_GAMMA = 5.0 / 3.0;
+
+__global__ void k_unpack(const Body *__restrict__ b, int n, double *x, double *y, double *z,
+                         double *vx, double *vy, double *vz, double *ax, double *ay, double *az,
+                         double *m, int *type, double *rho, double *P, double *u, double *h)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    const Body &q = b[i];
+    x[i] = q.x;
+    y[i] = q.y;
+    z[i] = q.z;
+    vx[i] = q.vx;
+    vy[i] = q.vy;
+    vz[i] = q.vz;
+    ax[i] = q.ax;
+    ay[i] = q.ay;
+    az[i] = q.az;
+    m[i] = q.mass;
+    type[i] = (int)q.type;
+    rho[i] = q.density;
+    P[i] = q.pressure;
+    u[i] = q.internal_energy;
+    h[i] = q.smoothing_h;
+}
+
+// Writes back the fields the hot path changes; mass, type and the quasar
+// fields keep the values that were uploaded.
+__global__ void k_pack(Body *__restrict__ b, int n, const double *x, const double *y,
+                       const double *z, const double *vx, const double *vy, const double *vz,
+                       const double *ax, const double *ay, const double *az, const double *rho,
+                       const double *P, const double *u, const double *h)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    Body &q = b[i];
+    q.x = x[i];
+    q.y = y[i];
+    q.z = z[i];
+    q.vx = vx[i];
+    q.vy = vy[i];
+    q.vz = vz[i];
+    q.ax = ax[i];
+    q.ay = ay[i];
+    q.az = az[i];
+    q.density = rho[i];
+    q.pressure = P[i];
+    q.internal_energy = u[i];
+    q.smoothing_h = h[i];
+}
+
+// Half kick and drift, src/integrator.c:22-31.
+__global__ void k_kick_drift(int n, double dt, const double *__restrict__ m, double *x, double *y,
+                             double *z, double *vx, double *vy, double *vz,
+                             const double *__restrict__ ax, const double *__restrict__ ay,
+                             const double *__restrict__ az)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || m[i] <= 0.0)
+        return;
+    double v0 = vx[i] + 0.5 * ax[i] * dt;
+    double v1 = vy[i] + 0.5 * ay[i] * dt;
+    double v2 = vz[i] + 0.5 * az[i] * dt;
+    vx[i] = v0;
+    vy[i] = v1;
+    vz[i] = v2;
+    x[i] = x[i] + v0 * dt;
+    y[i] = y[i] + v1 * dt;
+    z[i] = z[i] + v2 * dt;
+}
+
+// Half kick, src/integrator.c:45-51.
+__global__ void k_kick(int n, double dt, const double *__restrict__ m, double *vx, double *vy,
+                       double *vz, const double *__restrict__ ax, const double *__restrict__ ay,
+                       const double *__restrict__ az)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || m[i] <= 0.0)
+        return;
+    vx[i] = vx[i] + 0.5 * ax[i] * dt;
+    vy[i] = vy[i] + 0.5 * ay[i] * dt;
+    vz[i] = vz[i] + 0.5 * az[i] * dt;
+}
+
+// Implicit radiative cooling, src/sph.c:200-231.
+__global__ void k_cooling(int n, double dt, const double *__restrict__ m,
+                          const int *__restrict__ type, const double *__restrict__ rho, double *u,
+                          double *P)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || type[i] != BODY_GAS || m[i] <= 0.0)
+        return;
+    const double lambda0 = 0.05;
+    double ui = u[i];
+    double r = rho[i];
+    if (ui < 1e-15 || r < 1e-15)
+        return;
+    double un = ui / (1.0 + dt * lambda0 * r * 0.5 / sqrt(ui));
+    if (un < 0.01)
+        un = 0.01;
+    u[i] = un;
+    P[i] = (SPH_GAMMA - 1.0) * r * un;
+}
+
+__global__ void k_alive_count(int n, const double *__restrict__ m, DevScalars *sc)
+{
+    int c = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        c += (m[i] <= 0.0) ? 0 : 1;
+    c = __reduce_add_sync(0xffffffffu, c);
+    if ((threadIdx.x & 31) == 0 && c)
+        atomicAdd(&sc->alive_count, c);
+}
+
+template <typename T>
+cudaError_t dalloc(T **p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0)
+        count = 1;
+    return cudaMalloc((void **)p, sizeof(T) * count);
+}
+
+void free_bodies(csgd_t *d)
+{
+    void *ptrs[] = {d->x, d->y, d->z, d->vx, d->vy, d->vz, d->ax, d->ay, d->az, d->m,
+                    d->rho, d->P, d->u, d->h, d->type, d->aos, d->key, d->key_alt, d->perm,
+                    d->perm_alt, d->ext, d->sort_hist, d->lcp, d->cnt, d->base, d->scan_tmp,
+                    d->gas, d->w64, d->w32, d->link, d->geo, d->child, d->nchild, d->ticket,
+                    d->minidx, d->ord_key, d->ord_key_alt, d->ord_id, d->ord_id_alt, d->rank,
+                    d->pool};
+    for (void *p : ptrs)
+        if (p)
+            cudaFree(p);
+    d->x = d->y = d->z = d->vx = d->vy = d->vz = d->ax = d->ay = d->az = d->m = nullptr;
+    d->rho = d->P = d->u = d->h = nullptr;
+    d->type = nullptr;
+    d->aos = nullptr;
+    d->key = d->key_alt = nullptr;
+    d->perm = d->perm_alt = nullptr;
+    d->ext = nullptr;
+    d->sort_hist = nullptr;
+    d->lcp = nullptr;
+    d->cnt = d->base = d->scan_tmp = d->gas = nullptr;
+    d->w64 = nullptr;
+    d->w32 = nullptr;
+    d->link = nullptr;
+    d->geo = nullptr;
+    d->child = d->nchild = d->ticket = nullptr;
+    d->minidx = nullptr;
+    d->ord_key = d->ord_key_alt = nullptr;
+    d->ord_id = d->ord_id_alt = d->rank = nullptr;
+    d->pool = nullptr;
+    d->cap = 0;
+    d->node_cap = 0;
+}
+
+} // namespace
+
+// ---- shared helpers ----------------------------------------------------------
+
+int csgd_grid(long long n, int block)
+{
+    long long g = (n + block - 1) / block;
+    return (int)(g > 0 ? g : 1);
+}
+
+void csgd_set_err(csgd_t *d, int code)
+{
+    if (d->host_err == 0)
+        d->host_err = code;
+}
+
+int csgd_check(csgd_t *d, cudaError_t e)
+{
+    if (e == cudaSuccess)
+        return CSG_OK;
+    csgd_set_err(d, CSG_ERR_CUDA);
+    return CSG_ERR_CUDA;
+}
+
+extern "C" const char *csgd_error_string(int code)
+{
+    switch (code) {
+    case CSG_OK:
+        return "ok";
+    case CSG_ERR_CUDA:
+        return "CUDA runtime error";
+    case CSG_ERR_NOMEM:
+        return "out of memory";
+    case CSG_ERR_NODE_CAPACITY:
+        return "tree needs more than 8*n+64 nodes";
+    case CSG_ERR_BAD_ARG:
+        return "invalid argument";
+    case CSG_ERR_BAD_POOL:
+        return "octree pool is not a tree";
+    case CSG_ERR_WALK_LIMIT:
+        return "tree walk stopped on a malformed tree";
+    case CSG_ERR_NO_DEVICE:
+        return "no CUDA device";
+    case CSG_ERR_UNSUPPORTED:
+        return "needs a component that is not linked";
+    default:
+        return "unknown error";
+    }
+}
+
+// ---- lifetime ------------------------------------------------------------
+
+extern "C" csgd_t *csgd_create(void)
+{
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
+        return nullptr;
+    csgd_t *d = (csgd_t *)calloc(1, sizeof(csgd_t));
+    if (!d)
+        return nullptr;
+    if (cudaStreamCreateWithFlags(&d->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        free(d);
+        return nullptr;
+    }
+    d->stream = d->own_stream;
+    if (cudaMalloc((void **)&d->sc, sizeof(DevScalars)) != cudaSuccess ||
+        cudaMallocHost((void **)&d->sc_host, sizeof(DevScalars)) != cudaSuccess) {
+        if (d->sc)
+            cudaFree(d->sc);
+        cudaStreamDestroy(d->own_stream);
+        free(d);
+        return nullptr;
+    }
+    memset(d->sc_host, 0, sizeof(DevScalars));
+    cudaMemsetAsync(d->sc, 0, sizeof(DevScalars), d->stream);
+    return d;
+}
+
+extern "C" void csgd_destroy(csgd_t *d)
+{
+    if (!d)
+        return;
+    cudaStreamSynchronize(d->stream);
+    free_bodies(d);
+    if (d->sc)
+        cudaFree(d->sc);
+    if (d->sc_host)
+        cudaFreeHost(d->sc_host);
+    if (d->own_stream)
+        cudaStreamDestroy(d->own_stream);
+    free(d);
+}
+
+extern "C" void csgd_set_stream(csgd_t *d, void *stream)
+{
+    d->stream = stream ? (cudaStream_t)stream : d->own_stream;
+}
+
+extern "C" void *csgd_stream(csgd_t *d) { return (void *)d->stream; }
+
+extern "C" int csgd_count(const csgd_t *d) { return d->n; }
+
+extern "C" void csgd_enable_stats(csgd_t *d, int on) { d->stats = on; }
+
+extern "C" int csgd_reserve(csgd_t *d, int n)
+{
+    if (n < 0) {
+        csgd_set_err(d, CSG_ERR_BAD_ARG);
+        return CSG_ERR_BAD_ARG;
+    }
+    d->n = n;
+    if (n <= d->cap && d->cap > 0)
+        return CSG_OK;
+    cudaStreamSynchronize(d->stream);
+    free_bodies(d);
+    const size_t cap = (size_t)(n > 0 ? n : 1);
+    const size_t ncap = 8 * cap + 64; // the reference's pool contract
+    bool ok = true;
+    ok &= dalloc(&d->x, cap) == cudaSuccess;
+    ok &= dalloc(&d->y, cap) == cudaSuccess;
+    ok &= dalloc(&d->z, cap) == cudaSuccess;
+    ok &= dalloc(&d->vx, cap) == cudaSuccess;
+    ok &= dalloc(&d->vy, cap) == cudaSuccess;
+    ok &= dalloc(&d->vz, cap) == cudaSuccess;
+    ok &= dalloc(&d->ax, cap) == cudaSuccess;
+    ok &= dalloc(&d->ay, cap) == cudaSuccess;
+    ok &= dalloc(&d->az, cap) == cudaSuccess;
+    ok &= dalloc(&d->m, cap) == cudaSuccess;
+    ok &= dalloc(&d->rho, cap) == cudaSuccess;
+    ok &= dalloc(&d->P, cap) == cudaSuccess;
+    ok &= dalloc(&d->u, cap) == cudaSuccess;
+    ok &= dalloc(&d->h, cap) == cudaSuccess;
+    ok &= dalloc(&d->type, cap) == cudaSuccess;
+    ok &= dalloc(&d->aos, cap) == cudaSuccess;
+    ok &= dalloc(&d->key, ncap) == cudaSuccess; // the key buffers also sort cells at export
+    ok &= dalloc(&d->key_alt, ncap) == cudaSuccess;
+    ok &= dalloc(&d->perm, cap) == cudaSuccess;
+    ok &= dalloc(&d->perm_alt, cap) == cudaSuccess;
+    ok &= dalloc(&d->ext, 3 * cap) == cudaSuccess;
+    const size_t sort_items = ncap;
+    const size_t hist = 256 * ((sort_items + 4095) / 4096);
+    d->sort_hist_cap = (int)(2 * hist + 1);
+    ok &= dalloc(&d->sort_hist, (size_t)d->sort_hist_cap) == cudaSuccess;
+    ok &= dalloc(&d->lcp, cap) == cudaSuccess;
+    ok &= dalloc(&d->cnt, cap + 1) == cudaSuccess;
+    ok &= dalloc(&d->base, cap + 1) == cudaSuccess;
+    const size_t scan_len = (cap > hist ? cap : hist);
+    d->scan_tmp_cap = (int)(scan_len / 1024 + 4096);
+    ok &= dalloc(&d->scan_tmp, (size_t)d->scan_tmp_cap) == cudaSuccess;
+    ok &= dalloc(&d->gas, cap) == cudaSuccess;
+    ok &= dalloc(&d->w64, ncap) == cudaSuccess;
+    ok &= dalloc(&d->w32, ncap) == cudaSuccess;
+    ok &= dalloc(&d->link, ncap) == cudaSuccess;
+    ok &= dalloc(&d->geo, ncap) == cudaSuccess;
+    ok &= dalloc(&d->child, 8 * ncap) == cudaSuccess;
+    ok &= dalloc(&d->nchild, ncap) == cudaSuccess;
+    ok &= dalloc(&d->ticket, ncap) == cudaSuccess;
+    ok &= dalloc(&d->minidx, ncap) == cudaSuccess;
+    ok &= dalloc(&d->ord_key, ncap) == cudaSuccess;
+    ok &= dalloc(&d->ord_key_alt, ncap) == cudaSuccess;
+    ok &= dalloc(&d->ord_id, ncap) == cudaSuccess;
+    ok &= dalloc(&d->ord_id_alt, ncap) == cudaSuccess;
+    ok &= dalloc(&d->rank, ncap) == cudaSuccess;
+    ok &= dalloc(&d->pool, ncap) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        free_bodies(d);
+        d->n = 0;
+        csgd_set_err(d, CSG_ERR_NOMEM);
+        return CSG_ERR_NOMEM;
+    }
+    d->cap = (int)cap;
+    d->node_cap = (int)ncap;
+    d->n = n;
+    // the tree stays empty-but-valid until the first build
+    cudaMemsetAsync(d->sc, 0, sizeof(DevScalars), d->stream);
+    return csgd_check(d, cudaGetLastError());
+}
+
+// ---- host I/O --------------------------------------------------------------
+
+extern "C" int csgd_upload_bodies(csgd_t *d, const Body *host, int n)
+{
+    int rc = csgd_reserve(d, n);
+    if (rc)
+        return rc;
+    if (n == 0)
+        return CSG_OK;
+    cudaMemcpyAsync(d->aos, host, sizeof(Body) * (size_t)n, cudaMemcpyHostToDevice, d->stream);
+    k_unpack<<<csgd_grid(n, 256), 256, 0, d->stream>>>(d->aos, n, d->x, d->y, d->z, d->vx, d->vy,
+                                                        d->vz, d->ax, d->ay, d->az, d->m, d->type,
+                                                        d->rho, d->P, d->u, d->h);
+    d->geometry_valid = 0;
+    return csgd_check(d, cudaGetLastError());
+}
+
+extern "C" int csgd_download_bodies(csgd_t *d, Body *host, int n)
+{
+    if (n > d->n || n < 0) {
+        csgd_set_err(d, CSG_ERR_BAD_ARG);
+        return CSG_ERR_BAD_ARG;
+    }
+    if (n == 0)
+        return CSG_OK;
+    k_pack<<<csgd_grid(n, 256), 256, 0, d->stream>>>(d->aos, n, d->x, d->y, d->z, d->vx, d->vy,
+                                                      d->vz, d->ax, d->ay, d->az, d->rho, d->P,
+                                                      d->u, d->h);
+    cudaMemcpyAsync(host, d->aos, sizeof(Body) * (size_t)n, cudaMemcpyDeviceToHost, d->stream);
+    return csgd_check(d, cudaGetLastError());
+}
+
+// ---- leapfrog --------------------------------------------------------------
+
+extern "C" int csgd_kick_drift(csgd_t *d, double dt)
+{
+    if (d->n <= 0)
+        return CSG_OK;
+    k_kick_drift<<<csgd_grid(d->n, 256), 256, 0, d->stream>>>(d->n, dt, d->m, d->x, d->y, d->z,
+                                                               d->vx, d->vy, d->vz, d->ax, d->ay,
+                                                               d->az);
+    return csgd_check(d, cudaGetLastError());
+}
+
+extern "C" int csgd_kick(csgd_t *d, double dt)
+{
+    if (d->n <= 0)
+        return CSG_OK;
+    k_kick<<<csgd_grid(d->n, 256), 256, 0, d->stream>>>(d->n, dt, d->m, d->vx, d->vy, d->vz,
+                                                         d->ax, d->ay, d->az);
+    return csgd_check(d, cudaGetLastError());
+}
+
+extern "C" int csgd_sph_cooling(csgd_t *d, double dt)
+{
+    if (d->n <= 0)
+        return CSG_OK;
+    k_cooling<<<csgd_grid(d->n, 256), 256, 0, d->stream>>>(d->n, dt, d->m, d->type, d->rho, d->u,
+                                                            d->P);
+    return csgd_check(d, cudaGetLastError());
+}
+
+extern "C" int csgd_substep(csgd_t *d, double dt, const csgd_force_params *p, int sph)
+{
+    int rc = csgd_kick_drift(d, dt);
+    if (!rc)
+        rc = csgd_build_tree(d, sph);
+    if (!rc)
+        rc = csgd_gravity(d, p);
+    if (!rc && sph) {
+        rc = csgd_sph_density(d);
+        if (!rc)
+            rc = csgd_sph_forces(d);
+    }
+    if (!rc)
+        rc = csgd_kick(d, dt);
+    if (!rc && sph)
+        rc = csgd_sph_cooling(d, dt);
+    return rc;
+}
+
+// ---- synchronisation and queries ---------------------------------------
+
+extern "C" int csgd_sync(csgd_t *d)
+{
+    cudaError_t e = cudaMemcpyAsync(d->sc_host, d->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost,
+                                    d->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(d->stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        d->host_err = 0;
+        return CSG_ERR_CUDA;
+    }
+    int rc = d->host_err;
+    d->host_err = 0;
+    const int dev_err = d->sc_host->err;
+    if (dev_err) {
+        cudaMemsetAsync(&d->sc->err, 0, sizeof(int), d->stream);
+        cudaStreamSynchronize(d->stream);
+        if (!rc)
+            rc = dev_err;
+    }
+    return rc;
+}
+
+extern "C" int csgd_node_count(csgd_t *d, int *n_nodes)
+{
+    int rc = csgd_sync(d);
+    *n_nodes = d->sc_host->n_nodes;
+    return rc;
+}
+
+extern "C" int csgd_interactions(csgd_t *d, int64_t *total)
+{
+    int rc = csgd_sync(d);
+    *total = (int64_t)d->sc_host->interactions;
+    return rc;
+}
+
+extern "C" int csgd_reset_stats(csgd_t *d)
+{
+    cudaMemsetAsync(&d->sc->interactions, 0, sizeof(unsigned long long), d->stream);
+    return csgd_check(d, cudaGetLastError());
+}
+
+extern "C" int csgd_alive_count(csgd_t *d, int *count)
+{
+    cudaMemsetAsync(&d->sc->alive_count, 0, sizeof(int), d->stream);
+    if (d->n > 0) {
+        int g = csgd_grid(d->n, 256);
+        if (g > 152 * 8)
+            g = 152 * 8;
+        k_alive_count<<<g, 256, 0, d->stream>>>(d->n, d->m, d->sc);
+    }
+    int rc = csgd_sync(d);
+    *count = d->sc_host->alive_count;
+    return rc;
+}

@@ -1,0 +1,897 @@
+// dev_tree.cu — octree build from sorted octant keys, bottom-up moments,
+// reference-order pool export and caller-pool import.
+//
+// The reference inserts bodies one by one into a pointer octree
+// (src/octree.c:52-169). The cell structure that produces depends only on the
+// body positions: a cell holding two or more alive bodies is split into the
+// octants that hold bodies, down to depth 64 (src/octree.c:5, 71-79). This
+// file builds the same cells in parallel:
+//   1. bbox of the alive bodies -> root cube (src/octree.c:118-159);
+//   2. each body's octant digit per level, 3 bits (east | south<<1 |
+//      bottom<<2, src/octree.c:30-40), packed most-significant-first into a
+//      63-bit key for levels 0..20 — so ascending key order is the reference's
+//      depth-first child order;
+//   3. stable radix sort of (key, body index);
+//   4. bodies that share all 21 levels get the digits of levels 21..63 and
+//      are ordered by them (rare: closer than 2^-21 of the root cube);
+//   5. cells are maximal runs of sorted bodies with a common digit prefix; a
+//      run of >= 2 bodies at level L (< 64) is an internal cell, a body alone
+//      at its level is a leaf, a run of >= 2 at level 64 is one leaf whose
+//      body_index is its lowest body index (the reference's max-depth leaf);
+//   6. each sorted position a starts the internal cells of levels
+//      (lcp(a-1,a), lcp(a,a+1)] and possibly its leaf, so an exclusive scan of
+//      those counts numbers all cells in depth-first preorder.
+// Cell centres are recomputed with the reference's own arithmetic
+// (centre +/- 0.5*half_size per level, half_size*0.5), so split decisions and
+// geometry are identical to the reference's bit for bit.
+#include "dev_internal.cuh"
+
+#include <float.h>
+
+namespace {
+
+constexpr unsigned long long SIGN64 = 0x8000000000000000ull;
+constexpr int KEY_MASK21 = (1 << 21) - 1;
+
+__device__ __forceinline__ unsigned long long ord_enc(double v)
+{
+    unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    return (u & SIGN64) ? ~u : (u | SIGN64);
+}
+
+__device__ __forceinline__ double ord_dec(unsigned long long e)
+{
+    unsigned long long u = (e & SIGN64) ? (e & ~SIGN64) : ~e;
+    return __longlong_as_double((long long)u);
+}
+
+__device__ __forceinline__ bool is_alive(double m) { return !(m <= 0.0); }
+
+// Spreads the low 21 bits of v to every third bit (bit k -> bit 3k).
+__device__ __forceinline__ unsigned long long spread3(unsigned long long v)
+{
+    v &= 0x1fffffull;
+    v = (v | (v << 32)) & 0x1f00000000ffffull;
+    v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+
+// One level of the reference descent: octant code, then the child cube
+// (src/octree.c:30-50 and :87-90, :105-108).
+__device__ __forceinline__ int descend_one(double px, double py, double pz, double &cx,
+                                           double &cy, double &cz, double &hs)
+{
+    int q = (px >= cx ? 1 : 0) | (py < cy ? 2 : 0) | (pz < cz ? 4 : 0);
+    double ox = (q & 1) ? 0.5 : -0.5;
+    double oy = (q & 2) ? -0.5 : 0.5;
+    double oz = (q & 4) ? -0.5 : 0.5;
+    cx = cx + ox * hs;
+    cy = cy + oy * hs;
+    cz = cz + oz * hs;
+    hs = hs * 0.5;
+    return q;
+}
+
+// Digits of levels [l0, l0+nl) packed most-significant-first, after descending
+// l0 levels; also returns the cube reached.
+__device__ unsigned long long exact_digits(double px, double py, double pz, const DevScalars *sc,
+                                           int l0, int nl)
+{
+    double cx = sc->c0[0], cy = sc->c0[1], cz = sc->c0[2], hs = sc->hs0;
+    for (int l = 0; l < l0; l++)
+        descend_one(px, py, pz, cx, cy, cz, hs);
+    unsigned long long k = 0;
+    for (int l = 0; l < nl; l++)
+        k = (k << 3) | (unsigned long long)descend_one(px, py, pz, cx, cy, cz, hs);
+    return k;
+}
+
+__device__ __forceinline__ int clz_levels(unsigned long long x) { return (__clzll(x) - 1) / 3; }
+
+// Number of leading levels two sorted positions share (0..64).
+__device__ __forceinline__ int lcp_pos(const unsigned long long *__restrict__ key,
+                                       const unsigned long long *__restrict__ ext, int a, int b)
+{
+    unsigned long long ka = key[a], kb = key[b];
+    if (ka != kb)
+        return clz_levels(ka ^ kb);
+    const unsigned long long *ea = ext + 3 * (size_t)a, *eb = ext + 3 * (size_t)b;
+    if (ea[0] != eb[0])
+        return 21 + clz_levels(ea[0] ^ eb[0]);
+    if (ea[1] != eb[1])
+        return 42 + clz_levels(ea[1] ^ eb[1]);
+    return (ea[2] != eb[2]) ? 63 : 64;
+}
+
+// Digit of level l (0..63) of sorted position p.
+__device__ __forceinline__ int digit_at(const unsigned long long *__restrict__ key,
+                                        const unsigned long long *__restrict__ ext, int p, int l)
+{
+    if (l < 21)
+        return (int)((key[p] >> (3 * (20 - l))) & 7ull);
+    if (l < 42)
+        return (int)((ext[3 * (size_t)p] >> (3 * (41 - l))) & 7ull);
+    if (l < 63)
+        return (int)((ext[3 * (size_t)p + 1] >> (3 * (62 - l))) & 7ull);
+    return (int)(ext[3 * (size_t)p + 2] & 7ull);
+}
+
+// ---- 1. bbox -----------------------------------------------------------
+
+__global__ void k_reset(DevScalars *sc)
+{
+    for (int a = 0; a < 3; a++) {
+        sc->omin[a] = ~0ull;
+        sc->omax[a] = 0ull;
+    }
+    sc->n_alive = 0;
+    sc->deep = 0;
+    sc->n_gas = 0;
+    sc->key_slow = 0;
+}
+
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long t = __shfl_xor_sync(0xffffffffu, v, o);
+        v = t < v ? t : v;
+    }
+    return v;
+}
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long t = __shfl_xor_sync(0xffffffffu, v, o);
+        v = t > v ? t : v;
+    }
+    return v;
+}
+
+// Alive-body bbox (src/octree.c:118-139). NaN coordinates never win a
+// comparison in the reference, so they are left out here too.
+__global__ void k_bbox(const double *__restrict__ x, const double *__restrict__ y,
+                       const double *__restrict__ z, const double *__restrict__ m, int n,
+                       DevScalars *sc)
+{
+    unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
+    int cnt = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        if (!is_alive(m[i]))
+            continue;
+        cnt++;
+        double p[3] = {x[i], y[i], z[i]};
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            if (p[a] != p[a])
+                continue;
+            unsigned long long e = ord_enc(p[a]);
+            lo[a] = e < lo[a] ? e : lo[a];
+            hi[a] = e > hi[a] ? e : hi[a];
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        lo[a] = warp_min_u64(lo[a]);
+        hi[a] = warp_max_u64(hi[a]);
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0) {
+        for (int a = 0; a < 3; a++) {
+            if (lo[a] != ~0ull)
+                atomicMin(&sc->omin[a], lo[a]);
+            if (hi[a] != 0ull)
+                atomicMax(&sc->omax[a], hi[a]);
+        }
+        if (cnt)
+            atomicAdd(&sc->n_alive, cnt);
+    }
+}
+
+// Root cube, reference src/octree.c:141-159, plus the fast-key parameters.
+__global__ void k_root(DevScalars *sc)
+{
+    if (sc->n_alive == 0) {
+        sc->c0[0] = sc->c0[1] = sc->c0[2] = 0.0;
+        sc->hs0 = 1.0;
+        sc->fast_keys = 0;
+        sc->key_scale = 0.0;
+        sc->key_tol = 1.0;
+        return;
+    }
+    double lo[3], hi[3];
+    for (int a = 0; a < 3; a++) {
+        lo[a] = (sc->omin[a] == ~0ull) ? DBL_MAX : ord_dec(sc->omin[a]);
+        hi[a] = (sc->omax[a] == 0ull) ? -DBL_MAX : ord_dec(sc->omax[a]);
+        sc->c0[a] = (lo[a] + hi[a]) * 0.5;
+    }
+    double ext = hi[0] - lo[0];
+    if (hi[1] - lo[1] > ext)
+        ext = hi[1] - lo[1];
+    if (hi[2] - lo[2] > ext)
+        ext = hi[2] - lo[2];
+    double hs = ext * 0.5;
+    hs = hs * 1.01;
+    if (hs < 1e-10)
+        hs = 1.0;
+    sc->hs0 = hs;
+    // Fast keys: t = (p - c0) * 2^20/hs + 2^20 lies within R*2^-31 grid units
+    // of the exact descent, R = 1 + max|c0|/hs; bodies within the guard of
+    // a split point take the exact descent.
+    double r = fmax(fabs(sc->c0[0]), fmax(fabs(sc->c0[1]), fabs(sc->c0[2]))) / hs + 1.0;
+    double tol = 64.0 * r * 0x1p-32;
+    bool finite = isfinite(sc->c0[0]) && isfinite(sc->c0[1]) && isfinite(sc->c0[2]) &&
+                  isfinite(hs) && hs > 0.0;
+    sc->key_tol = tol;
+    sc->fast_keys = (finite && tol < 0.25) ? 1 : 0;
+    sc->key_scale = finite ? 1048576.0 / hs : 0.0;
+}
+
+// ---- 2. keys -----------------------------------------------------------
+
+__device__ __forceinline__ bool fast_coord(double p, double c, double scale, double tol, int &i)
+{
+    double t = (p - c) * scale + 1048576.0;
+    if (!(t >= tol && t <= 2097152.0 - tol))
+        return false;
+    double f = floor(t);
+    if (t - f < tol || (f + 1.0) - t < tol)
+        return false;
+    i = (int)f;
+    return true;
+}
+
+__global__ void k_keys(const double *__restrict__ x, const double *__restrict__ y,
+                       const double *__restrict__ z, const double *__restrict__ m, int n,
+                       DevScalars *sc, unsigned long long *__restrict__ key,
+                       int *__restrict__ perm)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+        return;
+    perm[i] = i;
+    if (!is_alive(m[i])) {
+        key[i] = CSG_DEAD_KEY;
+        return;
+    }
+    const double px = x[i], py = y[i], pz = z[i];
+    int ix, iy, iz;
+    if (sc->fast_keys && fast_coord(px, sc->c0[0], sc->key_scale, sc->key_tol, ix) &&
+        fast_coord(py, sc->c0[1], sc->key_scale, sc->key_tol, iy) &&
+        fast_coord(pz, sc->c0[2], sc->key_scale, sc->key_tol, iz)) {
+        // east = upper x half; south = lower y half; bottom = lower z half
+        unsigned long long sx = (unsigned long long)ix;
+        unsigned long long sy = (unsigned long long)(~iy & KEY_MASK21);
+        unsigned long long sz = (unsigned long long)(~iz & KEY_MASK21);
+        key[i] = spread3(sx) | (spread3(sy) << 1) | (spread3(sz) << 2);
+    } else {
+        key[i] = exact_digits(px, py, pz, sc, 0, 21);
+        atomicAdd(&sc->key_slow, 1ull);
+    }
+}
+
+// ---- 4. positions that share a 63-bit key ------------------------------
+
+__global__ void k_deep_mark(const double *__restrict__ x, const double *__restrict__ y,
+                            const double *__restrict__ z, DevScalars *sc,
+                            const unsigned long long *__restrict__ key,
+                            const int *__restrict__ perm, unsigned long long *__restrict__ ext)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int na = sc->n_alive;
+    if (p >= na)
+        return;
+    const unsigned long long k = key[p];
+    bool deep = (p > 0 && key[p - 1] == k) || (p + 1 < na && key[p + 1] == k);
+    if (!deep)
+        return;
+    const int b = perm[p];
+    ext[3 * (size_t)p + 0] = exact_digits(x[b], y[b], z[b], sc, 21, 21);
+    ext[3 * (size_t)p + 1] = exact_digits(x[b], y[b], z[b], sc, 42, 21);
+    ext[3 * (size_t)p + 2] = exact_digits(x[b], y[b], z[b], sc, 63, 1);
+    atomicAdd(&sc->deep, 1);
+}
+
+__device__ __forceinline__ bool ext_less(const unsigned long long *e, int a, int b)
+{
+    for (int w = 0; w < 3; w++) {
+        unsigned long long ea = e[3 * (size_t)a + w], eb = e[3 * (size_t)b + w];
+        if (ea != eb)
+            return ea < eb;
+    }
+    return false;
+}
+
+// Orders each run of equal 63-bit keys by its deeper digits; insertion sort is
+// stable, so equal full keys keep body index order.
+__global__ void k_deep_sort(DevScalars *sc, const unsigned long long *__restrict__ key,
+                            int *__restrict__ perm, unsigned long long *__restrict__ ext)
+{
+    if (sc->deep == 0)
+        return;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int na = sc->n_alive;
+    if (p >= na)
+        return;
+    const unsigned long long k = key[p];
+    if (!(p + 1 < na && key[p + 1] == k) || (p > 0 && key[p - 1] == k))
+        return; // not the start of a run
+    int e = p + 1;
+    while (e < na && key[e] == k)
+        e++;
+    for (int i = p + 1; i < e; i++) {
+        unsigned long long t0 = ext[3 * (size_t)i], t1 = ext[3 * (size_t)i + 1],
+                           t2 = ext[3 * (size_t)i + 2];
+        int tp = perm[i];
+        int j = i - 1;
+        while (j >= p) {
+            unsigned long long u0 = ext[3 * (size_t)j], u1 = ext[3 * (size_t)j + 1],
+                               u2 = ext[3 * (size_t)j + 2];
+            bool greater = (u0 != t0) ? (u0 > t0) : (u1 != t1) ? (u1 > t1) : (u2 > t2);
+            if (!greater)
+                break;
+            ext[3 * (size_t)(j + 1)] = u0;
+            ext[3 * (size_t)(j + 1) + 1] = u1;
+            ext[3 * (size_t)(j + 1) + 2] = u2;
+            perm[j + 1] = perm[j];
+            j--;
+        }
+        ext[3 * (size_t)(j + 1)] = t0;
+        ext[3 * (size_t)(j + 1) + 1] = t1;
+        ext[3 * (size_t)(j + 1) + 2] = t2;
+        perm[j + 1] = tp;
+    }
+}
+
+// ---- 5/6. cells ----------------------------------------------------------
+
+__global__ void k_count(DevScalars *sc, const unsigned long long *__restrict__ key,
+                        const unsigned long long *__restrict__ ext, signed char *__restrict__ lcp,
+                        int *__restrict__ cnt)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int na = sc->n_alive;
+    if (p >= na)
+        return;
+    int P = (p > 0) ? lcp_pos(key, ext, p - 1, p) : -1;
+    int Q = (p + 1 < na) ? lcp_pos(key, ext, p, p + 1) : -1;
+    lcp[p] = (signed char)Q;
+    int internal = min(Q, CSG_MAX_LEVEL - 1) - P;
+    cnt[p] = (internal > 0 ? internal : 0) + (P < CSG_MAX_LEVEL ? 1 : 0);
+}
+
+__device__ int search_hi(const unsigned long long *key, const unsigned long long *ext, int na,
+                         int p, int L)
+{
+    int q = p, step = 1;
+    while (true) {
+        int t = q + step;
+        if (t >= na || lcp_pos(key, ext, p, t) < L)
+            break;
+        q = t;
+        step <<= 1;
+    }
+    while (step > 1) {
+        step >>= 1;
+        int t = q + step;
+        if (t < na && lcp_pos(key, ext, p, t) >= L)
+            q = t;
+    }
+    return q;
+}
+
+__device__ int search_lo(const unsigned long long *key, const unsigned long long *ext, int p,
+                         int L)
+{
+    int q = p, step = 1;
+    while (true) {
+        int t = q - step;
+        if (t < 0 || lcp_pos(key, ext, t, p) < L)
+            break;
+        q = t;
+        step <<= 1;
+    }
+    while (step > 1) {
+        step >>= 1;
+        int t = q - step;
+        if (t >= 0 && lcp_pos(key, ext, t, p) >= L)
+            q = t;
+    }
+    return q;
+}
+
+__device__ __forceinline__ int parent_id(const unsigned long long *key,
+                                         const unsigned long long *ext,
+                                         const signed char *lcp, const int *base, int p, int P,
+                                         int L, int id)
+{
+    if (L == 0)
+        return -1;
+    if (L - 1 > P)
+        return id - 1; // the cell one level up starts at p as well
+    int a = search_lo(key, ext, p, L - 1);
+    int Pa = (a > 0) ? (int)lcp[a - 1] : -1;
+    return base[a] + (L - 1) - (Pa + 1);
+}
+
+__device__ __forceinline__ void write_cell(csgd_t dd, DevScalars *sc, int id, int parent, int L,
+                                           int first, int count, int next, int body)
+{
+    if (id >= dd.node_cap) {
+        dev_fail(sc, CSG_ERR_NODE_CAPACITY);
+        return;
+    }
+    double hs = ldexp(sc->hs0, -L);
+    double s = 2.0 * hs;
+    double s2 = s * s;
+    NodeW64 w;
+    w.cx = w.cy = w.cz = w.m = 0.0;
+    w.s2 = s2;
+    w.next = next;
+    w.body = body;
+    dd.w64[id] = w;
+    NodeW32 v;
+    v.cx = v.cy = v.cz = v.m = 0.0f;
+    v.lx = v.ly = v.lz = 0.0f;
+    v.next = next;
+    v.body = body;
+    v.s2 = (float)s2;
+    v.s = (float)s;
+    v.pad = 0.0f;
+    dd.w32[id] = v;
+    dd.link[id] = NodeLink{parent, L, first, count};
+    int4 *c = (int4 *)(dd.child + 8 * (size_t)id);
+    c[0] = make_int4(-1, -1, -1, -1);
+    c[1] = make_int4(-1, -1, -1, -1);
+    dd.nchild[id] = 0;
+    dd.ticket[id] = 0;
+}
+
+__global__ void k_nodes(csgd_t dd, DevScalars *sc, const unsigned long long *__restrict__ key,
+                        const unsigned long long *__restrict__ ext,
+                        const signed char *__restrict__ lcp, const int *__restrict__ base,
+                        const int *__restrict__ perm)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int na = sc->n_alive;
+    if (p == 0) {
+        int total = (na == 0) ? 1 : base[na];
+        sc->n_nodes = total;
+        if (total > dd.node_cap)
+            dev_fail(sc, CSG_ERR_NODE_CAPACITY);
+        if (na == 0) { // empty root, reference src/octree.c:141-144
+            write_cell(dd, sc, 0, -1, 0, 0, 0, 1, -1);
+            return;
+        }
+    }
+    if (p >= na)
+        return;
+    const int P = (p > 0) ? (int)lcp[p - 1] : -1;
+    const int Q = (int)lcp[p];
+    int id = base[p];
+    const int Lhi = min(Q, CSG_MAX_LEVEL - 1);
+    for (int L = P + 1; L <= Lhi; L++, id++) {
+        int hi = search_hi(key, ext, na, p, L);
+        int parent = parent_id(key, ext, lcp, base, p, P, L, id);
+        write_cell(dd, sc, id, parent, L, p, hi - p + 1, base[hi + 1], -1);
+    }
+    if (P < CSG_MAX_LEVEL) {
+        int L = max(P, Q) + 1;
+        int hi = (Q == CSG_MAX_LEVEL) ? search_hi(key, ext, na, p, CSG_MAX_LEVEL) : p;
+        int parent = parent_id(key, ext, lcp, base, p, P, L, id);
+        write_cell(dd, sc, id, parent, L, p, hi - p + 1, id + 1, perm[p]);
+    }
+}
+
+__global__ void k_link(csgd_t dd, DevScalars *sc, const unsigned long long *__restrict__ key,
+                       const unsigned long long *__restrict__ ext)
+{
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= min(sc->n_nodes, dd.node_cap))
+        return;
+    NodeLink l = dd.link[id];
+    if (l.parent < 0)
+        return;
+    int dg = digit_at(key, ext, l.first, l.level - 1);
+    dd.child[8 * (size_t)l.parent + dg] = id;
+    atomicAdd(&dd.nchild[l.parent], 1);
+}
+
+// Bottom-up moments: the last child to finish computes its parent, summing the
+// children in octant order so the result does not depend on scheduling.
+__global__ void k_moments(csgd_t dd, DevScalars *sc, const double *__restrict__ x,
+                          const double *__restrict__ y, const double *__restrict__ z,
+                          const double *__restrict__ m, const int *__restrict__ perm)
+{
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= min(sc->n_nodes, dd.node_cap))
+        return;
+    if (dd.w64[id].body < 0)
+        return;
+    NodeLink l = dd.link[id];
+    double M, sx, sy, sz;
+    int2 mi;
+    if (l.count == 1) {
+        int b = perm[l.first];
+        M = m[b];
+        sx = x[b];
+        sy = y[b];
+        sz = z[b];
+        mi = make_int2(b, INT_MAX);
+    } else { // bodies that coincide to depth 64 share one leaf
+        M = 0.0;
+        double ax = 0.0, ay = 0.0, az = 0.0;
+        for (int k = 0; k < l.count; k++) {
+            int b = perm[l.first + k];
+            M += m[b];
+            ax += m[b] * x[b];
+            ay += m[b] * y[b];
+            az += m[b] * z[b];
+        }
+        sx = ax / M;
+        sy = ay / M;
+        sz = az / M;
+        mi = make_int2(perm[l.first], perm[l.first + 1]);
+    }
+    int node = id;
+    while (true) {
+        NodeW64 w = dd.w64[node];
+        w.cx = sx;
+        w.cy = sy;
+        w.cz = sz;
+        w.m = M;
+        dd.w64[node] = w;
+        NodeW32 v = dd.w32[node];
+        v.cx = (float)sx;
+        v.cy = (float)sy;
+        v.cz = (float)sz;
+        v.lx = (float)(sx - (double)v.cx);
+        v.ly = (float)(sy - (double)v.cy);
+        v.lz = (float)(sz - (double)v.cz);
+        v.m = (float)M;
+        dd.w32[node] = v;
+        dd.minidx[node] = mi;
+        int parent = dd.link[node].parent;
+        if (parent < 0)
+            break;
+        __threadfence();
+        int t = atomicAdd(&dd.ticket[parent], 1);
+        if (t != __ldcg(&dd.nchild[parent]) - 1)
+            break;
+        __threadfence();
+        M = 0.0;
+        double ax = 0.0, ay = 0.0, az = 0.0;
+        int m1 = INT_MAX, m2 = INT_MAX;
+        for (int q = 0; q < 8; q++) {
+            int c = __ldcg(&dd.child[8 * (size_t)parent + q]);
+            if (c < 0)
+                continue;
+            double cm = __ldcg(&dd.w64[c].m);
+            M += cm;
+            ax += cm * __ldcg(&dd.w64[c].cx);
+            ay += cm * __ldcg(&dd.w64[c].cy);
+            az += cm * __ldcg(&dd.w64[c].cz);
+            int2 cmi = __ldcg(&dd.minidx[c]);
+            int cand[2] = {cmi.x, cmi.y};
+            for (int j = 0; j < 2; j++) {
+                int v2 = cand[j];
+                if (v2 < m1) {
+                    m2 = m1;
+                    m1 = v2;
+                } else if (v2 < m2) {
+                    m2 = v2;
+                }
+            }
+        }
+        sx = ax / M;
+        sy = ay / M;
+        sz = az / M;
+        mi = make_int2(m1, m2);
+        node = parent;
+    }
+}
+
+// Geometric cube of every cell, with the reference's arithmetic.
+__global__ void k_geometry(csgd_t dd, DevScalars *sc, const unsigned long long *__restrict__ key,
+                           const unsigned long long *__restrict__ ext)
+{
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= min(sc->n_nodes, dd.node_cap))
+        return;
+    NodeLink l = dd.link[id];
+    double cx = sc->c0[0], cy = sc->c0[1], cz = sc->c0[2], hs = sc->hs0;
+    for (int lev = 0; lev < l.level; lev++) {
+        int q = digit_at(key, ext, l.first, lev);
+        double ox = (q & 1) ? 0.5 : -0.5;
+        double oy = (q & 2) ? -0.5 : 0.5;
+        double oz = (q & 4) ? -0.5 : 0.5;
+        cx = cx + ox * hs;
+        cy = cy + oy * hs;
+        cz = cz + oz * hs;
+        hs = hs * 0.5;
+    }
+    dd.geo[id] = make_double4(cx, cy, cz, hs);
+}
+
+// ---- export in the reference's allocation order --------------------------
+//
+// The reference allocates a cell while inserting some body k (index order).
+// With S = the cell's bodies and T = its parent's, that k is max(min S,
+// second-smallest of T); cells allocated during one insertion come in
+// increasing depth, and at the one depth where two appear (the split that
+// finally separates the old body j from k) j's cell comes first. Sorting
+// cells by (k, depth, [min S == k]) therefore reproduces pool numbering.
+
+__global__ void k_order_keys(csgd_t dd, DevScalars *sc)
+{
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nn = min(sc->n_nodes, dd.node_cap);
+    if (id >= nn)
+        return;
+    NodeLink l = dd.link[id];
+    unsigned long long k;
+    if (l.parent < 0) {
+        k = 0ull;
+    } else {
+        int s0 = dd.minidx[id].x;
+        int t1 = dd.minidx[l.parent].y;
+        int kc = max(s0, t1);
+        k = ((unsigned long long)(kc + 1) << 8) | ((unsigned long long)l.level << 1) |
+            (s0 == kc ? 1ull : 0ull);
+    }
+    dd.ord_key[id] = k;
+    dd.ord_id[id] = id;
+}
+
+__global__ void k_rank(csgd_t dd, DevScalars *sc)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= min(sc->n_nodes, dd.node_cap))
+        return;
+    dd.rank[dd.ord_id[r]] = r;
+}
+
+__global__ void k_export(csgd_t dd, DevScalars *sc)
+{
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= min(sc->n_nodes, dd.node_cap))
+        return;
+    NodeW64 w = dd.w64[id];
+    double4 g = dd.geo[id];
+    OctreeNode o;
+    o.cx = w.cx;
+    o.cy = w.cy;
+    o.cz = w.cz;
+    o.total_mass = w.m;
+    o.center_x = g.x;
+    o.center_y = g.y;
+    o.center_z = g.z;
+    o.half_size = g.w;
+    o.body_index = w.body;
+    for (int q = 0; q < 8; q++) {
+        int c = dd.child[8 * (size_t)id + q];
+        o.children[q] = (c >= 0) ? dd.rank[c] : -1;
+    }
+    dd.pool[dd.rank[id]] = o;
+}
+
+// ---- import of a caller pool ---------------------------------------------
+// parent links, subtree sizes (bottom-up), preorder ids (walk up summing the
+// sizes of earlier siblings), then the walk/SPH records in preorder.
+
+constexpr int IMPORT_MAX_DEPTH = 4096;
+
+__global__ void k_imp_links(csgd_t dd, DevScalars *sc, int nn, int root, int *__restrict__ par,
+                            int *__restrict__ slot)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn)
+        return;
+    const OctreeNode &o = dd.pool[i];
+    int nc = 0;
+    for (int q = 0; q < 8; q++) {
+        int c = o.children[q];
+        if (c < 0)
+            continue;
+        if (c >= nn || c == root) {
+            dev_fail(sc, CSG_ERR_BAD_POOL);
+            continue;
+        }
+        if (atomicCAS(&par[c], -1, i) != -1) {
+            dev_fail(sc, CSG_ERR_BAD_POOL);
+            continue;
+        }
+        slot[c] = q;
+        nc++;
+    }
+    dd.nchild[i] = nc;
+    dd.ticket[i] = 0;
+}
+
+__global__ void k_imp_sizes(csgd_t dd, DevScalars *sc, int nn, const int *__restrict__ par,
+                            int *__restrict__ size)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn || dd.nchild[i] != 0)
+        return;
+    int node = i, s = 1, steps = 0;
+    while (true) {
+        size[node] = s;
+        int p = par[node];
+        if (p < 0)
+            break;
+        if (++steps > IMPORT_MAX_DEPTH) {
+            dev_fail(sc, CSG_ERR_BAD_POOL);
+            break;
+        }
+        __threadfence();
+        int t = atomicAdd(&dd.ticket[p], 1);
+        if (t != dd.nchild[p] - 1)
+            break;
+        __threadfence();
+        s = 1;
+        for (int q = 0; q < 8; q++) {
+            int c = dd.pool[p].children[q];
+            if (c >= 0)
+                s += __ldcg(&size[c]);
+        }
+        node = p;
+    }
+}
+
+__global__ void k_imp_write(csgd_t dd, DevScalars *sc, int nn, int root,
+                            const int *__restrict__ par, const int *__restrict__ slot,
+                            const int *__restrict__ size)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn)
+        return;
+    // preorder id = sum over the path of (1 + sizes of earlier siblings)
+    int id = 0, depth = 0, node = i;
+    while (node != root) {
+        int p = par[node];
+        if (p < 0)
+            return; // not reachable from root: not part of the tree
+        if (++depth > IMPORT_MAX_DEPTH) {
+            dev_fail(sc, CSG_ERR_BAD_POOL);
+            return;
+        }
+        int off = 1;
+        for (int q = 0; q < slot[node]; q++) {
+            int c = dd.pool[p].children[q];
+            if (c >= 0)
+                off += size[c];
+        }
+        id += off;
+        node = p;
+    }
+    if (i == root)
+        sc->n_nodes = size[root];
+    if (id >= dd.node_cap) {
+        dev_fail(sc, CSG_ERR_NODE_CAPACITY);
+        return;
+    }
+    const OctreeNode &o = dd.pool[i];
+    double s = 2.0 * o.half_size;
+    NodeW64 w;
+    w.cx = o.cx;
+    w.cy = o.cy;
+    w.cz = o.cz;
+    w.m = o.total_mass;
+    w.s2 = s * s;
+    w.next = id + size[i];
+    w.body = o.body_index >= 0 ? o.body_index : -1;
+    dd.w64[id] = w;
+    NodeW32 v;
+    v.cx = (float)o.cx;
+    v.cy = (float)o.cy;
+    v.cz = (float)o.cz;
+    v.lx = (float)(o.cx - (double)v.cx);
+    v.ly = (float)(o.cy - (double)v.cy);
+    v.lz = (float)(o.cz - (double)v.cz);
+    v.m = (float)o.total_mass;
+    v.next = w.next;
+    v.body = w.body;
+    v.s2 = (float)w.s2;
+    v.s = (float)s;
+    v.pad = 0.0f;
+    dd.w32[id] = v;
+    dd.geo[id] = make_double4(o.center_x, o.center_y, o.center_z, o.half_size);
+    dd.link[id] = NodeLink{-1, depth, -1, 0};
+}
+
+} // namespace
+
+// ---- host side -------------------------------------------------------------
+
+extern "C" int csgd_build_tree(csgd_t *d, int geometry)
+{
+    const int n = d->n;
+    cudaStream_t s = d->stream;
+    DevScalars *sc = d->sc;
+    const int B = 256;
+    k_reset<<<1, 1, 0, s>>>(sc);
+    int gb = min(csgd_grid(n, B), 152 * 8);
+    k_bbox<<<gb > 0 ? gb : 1, B, 0, s>>>(d->x, d->y, d->z, d->m, n, sc);
+    k_root<<<1, 1, 0, s>>>(sc);
+    if (n > 0)
+        k_keys<<<csgd_grid(n, B), B, 0, s>>>(d->x, d->y, d->z, d->m, n, sc, d->key, d->perm);
+    int rc = csg_radix_sort(d, d->key, d->perm, d->key_alt, d->perm_alt, n, 64);
+    if (rc)
+        return rc;
+    const int g = csgd_grid(n > 0 ? n : 1, B);
+    k_deep_mark<<<g, B, 0, s>>>(d->x, d->y, d->z, sc, d->key, d->perm, d->ext);
+    k_deep_sort<<<g, B, 0, s>>>(sc, d->key, d->perm, d->ext);
+    k_count<<<g, B, 0, s>>>(sc, d->key, d->ext, d->lcp, d->cnt);
+    rc = csg_scan_exclusive(d, d->cnt, d->base, n, &sc->n_alive);
+    if (rc)
+        return rc;
+    k_nodes<<<g, B, 0, s>>>(*d, sc, d->key, d->ext, d->lcp, d->base, d->perm);
+    const int gn = csgd_grid(d->node_cap, B);
+    // nodes beyond n_nodes exit at once; the grid covers the capacity
+    k_link<<<gn, B, 0, s>>>(*d, sc, d->key, d->ext);
+    k_moments<<<gn, B, 0, s>>>(*d, sc, d->x, d->y, d->z, d->m, d->perm);
+    d->geometry_valid = 0;
+    d->imported = 0;
+    if (geometry) {
+        k_geometry<<<gn, B, 0, s>>>(*d, sc, d->key, d->ext);
+        d->geometry_valid = 1;
+    }
+    return csgd_check(d, cudaGetLastError());
+}
+
+extern "C" int csgd_export_pool(csgd_t *d, OctreeNode *pool, int capacity, int *pool_size_out)
+{
+    cudaStream_t s = d->stream;
+    DevScalars *sc = d->sc;
+    const int B = 256;
+    if (!d->geometry_valid) {
+        const int gn = csgd_grid(d->node_cap, B);
+        k_geometry<<<gn, B, 0, s>>>(*d, sc, d->key, d->ext);
+        d->geometry_valid = 1;
+    }
+    int rc = csgd_node_count(d, pool_size_out);
+    if (rc)
+        return rc;
+    const int nn = *pool_size_out;
+    if (nn > capacity || nn > d->node_cap) {
+        csgd_set_err(d, CSG_ERR_NODE_CAPACITY);
+        return CSG_ERR_NODE_CAPACITY;
+    }
+    const int g = csgd_grid(nn, B);
+    k_order_keys<<<g, B, 0, s>>>(*d, sc);
+    rc = csg_radix_sort(d, d->ord_key, d->ord_id, d->ord_key_alt, d->ord_id_alt, nn, 40);
+    if (rc)
+        return rc;
+    k_rank<<<g, B, 0, s>>>(*d, sc);
+    k_export<<<g, B, 0, s>>>(*d, sc);
+    cudaMemcpyAsync(pool, d->pool, sizeof(OctreeNode) * (size_t)nn, cudaMemcpyDeviceToHost, s);
+    return csgd_sync(d);
+}
+
+extern "C" int csgd_import_pool(csgd_t *d, const OctreeNode *pool, int n_nodes, int root)
+{
+    if (n_nodes <= 0 || n_nodes > d->node_cap || root < 0 || root >= n_nodes) {
+        csgd_set_err(d, CSG_ERR_BAD_ARG);
+        return CSG_ERR_BAD_ARG;
+    }
+    cudaStream_t s = d->stream;
+    DevScalars *sc = d->sc;
+    const int B = 256;
+    // scratch: par, slot, size in the (unused here) sort/order buffers
+    int *par = d->ord_id, *slot = d->ord_id_alt, *size = d->rank;
+    cudaMemcpyAsync(d->pool, pool, sizeof(OctreeNode) * (size_t)n_nodes, cudaMemcpyHostToDevice,
+                    s);
+    cudaMemsetAsync(par, 0xff, sizeof(int) * (size_t)n_nodes, s);
+    const int g = csgd_grid(n_nodes, B);
+    k_imp_links<<<g, B, 0, s>>>(*d, sc, n_nodes, root, par, slot);
+    k_imp_sizes<<<g, B, 0, s>>>(*d, sc, n_nodes, par, size);
+    k_imp_write<<<g, B, 0, s>>>(*d, sc, n_nodes, root, par, slot, size);
+    d->geometry_valid = 1;
+    d->imported = 1;
+    return csgd_check(d, cudaGetLastError());
+}

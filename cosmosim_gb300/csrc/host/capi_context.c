@@ -1,0 +1,105 @@
+/*
+ * capi_context.c — per-thread device state, error channel and pool extent
+ * for the reference-compatible free functions.
+ */
+#include "capi_internal.h"
+
+#include <stdlib.h>
+#include <string.h>
+
+static _Thread_local csgd_t *tl_dev;
+static _Thread_local int tl_error;
+static _Thread_local int tl_precision = CSG_PREC_FP64;
+
+csgd_t *csg_thread_dev(void)
+{
+    if (!tl_dev) {
+        tl_dev = csgd_create();
+        if (!tl_dev)
+            tl_error = CSG_ERR_NO_DEVICE;
+    }
+    return tl_dev;
+}
+
+void csg_thread_set_error(int code) { tl_error = code; }
+
+int csg_thread_precision(void) { return tl_precision; }
+
+CSG_EXPORT int csg_last_error(void) { return tl_error; }
+
+CSG_EXPORT const char *csg_error_string(int code) { return csgd_error_string(code); }
+
+CSG_EXPORT void csg_set_precision(int precision)
+{
+    tl_precision = (precision == CSG_PREC_FP32_MIXED) ? CSG_PREC_FP32_MIXED : CSG_PREC_FP64;
+}
+
+int csg_pool_extent(const OctreeNode *pool, int root, int *n_nodes)
+{
+    /* The pool carries no size: walk it from the root, reading exactly the
+       cells the reference's own walk would read, and find the highest
+       reachable index. A cycle or a repeated child makes it not a tree. */
+    if (root < 0)
+        return CSG_ERR_BAD_POOL;
+    size_t cap = 1024;
+    int *stack = (int *)malloc(cap * sizeof(int));
+    size_t seen_cap = 0;
+    unsigned char *seen = NULL;
+    if (!stack)
+        return CSG_ERR_NOMEM;
+    size_t sp = 0;
+    int hi = root;
+    stack[sp++] = root;
+    int rc = CSG_OK;
+    long long visits = 0;
+    while (sp > 0) {
+        int c = stack[--sp];
+        if ((size_t)c >= seen_cap) {
+            size_t nc = seen_cap ? seen_cap : 4096;
+            while (nc <= (size_t)c)
+                nc *= 2;
+            unsigned char *ns = (unsigned char *)realloc(seen, nc);
+            if (!ns) {
+                rc = CSG_ERR_NOMEM;
+                break;
+            }
+            memset(ns + seen_cap, 0, nc - seen_cap);
+            seen = ns;
+            seen_cap = nc;
+        }
+        if (seen[c]) {
+            rc = CSG_ERR_BAD_POOL;
+            break;
+        }
+        seen[c] = 1;
+        if (c > hi)
+            hi = c;
+        if (++visits > 0x7ffffff0LL) {
+            rc = CSG_ERR_BAD_POOL;
+            break;
+        }
+        for (int q = 0; q < 8; q++) {
+            int ch = pool[c].children[q];
+            if (ch < 0)
+                continue;
+            if (sp == cap) {
+                size_t ncap = cap * 2;
+                int *ns = (int *)realloc(stack, ncap * sizeof(int));
+                if (!ns) {
+                    rc = CSG_ERR_NOMEM;
+                    break;
+                }
+                stack = ns;
+                cap = ncap;
+            }
+            stack[sp++] = ch;
+        }
+        if (rc)
+            break;
+    }
+    free(stack);
+    free(seen);
+    if (rc == CSG_OK)
+        *n_nodes = hi + 1;
+    return rc;
+}

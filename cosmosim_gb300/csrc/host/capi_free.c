@@ -1,0 +1,227 @@
+/*
+ * capi_free.c — the reference's free functions (octree.h, integrator.h,
+ * sph.h) over host arrays: upload, run on the device, copy results back.
+ *
+ * Semantics kept from the reference:
+ *   - the caller owns bodies and the pool; pool holds the built tree after
+ *     octree_build / integrator_* (root at index 0, reference numbering);
+ *   - octree_compute_forces / sph_* / octree_find_neighbors use the tree the
+ *     given pool holds (it is uploaded, whoever built it);
+ *   - void functions report failures through csg_last_error(), never abort.
+ * On failure the caller's arrays are left as they were.
+ */
+#include "capi_internal.h"
+
+#include <string.h>
+
+static csgd_force_params force_params(double G, double softening, double theta)
+{
+    csgd_force_params p;
+    p.G = G;
+    p.softening = softening;
+    p.theta = theta;
+    p.precision = csg_thread_precision();
+    return p;
+}
+
+/* Uploads bodies and the pool's tree. */
+static int load_pool(csgd_t *d, const OctreeNode *pool, int root, const Body *bodies, int n)
+{
+    int nn = 0;
+    int rc = csg_pool_extent(pool, root, &nn);
+    if (rc)
+        return rc;
+    rc = csgd_upload_bodies(d, bodies, n);
+    if (!rc)
+        rc = csgd_import_pool(d, pool, nn, root);
+    if (!rc)
+        rc = csgd_sync(d); /* a bad pool must be reported before any walk */
+    return rc;
+}
+
+/* Writes the device tree into the caller's pool (capacity 8n, the reference
+   contract; the root alone for n < 1). */
+static int store_pool(csgd_t *d, OctreeNode *pool, int *pool_size, int n)
+{
+    int ps = 0;
+    int cap = 8 * (n > 1 ? n : 1);
+    int rc = csgd_export_pool(d, pool, cap, &ps);
+    if (rc)
+        return rc;
+    if (pool_size)
+        *pool_size = ps;
+    return CSG_OK;
+}
+
+CSG_EXPORT void octree_build(OctreeNode *pool, int *pool_size, const Body *bodies, int n)
+{
+    csgd_t *d = csg_thread_dev();
+    if (!d)
+        return;
+    if (!pool || !pool_size || (n > 0 && !bodies) || n < 0) {
+        csg_thread_set_error(CSG_ERR_BAD_ARG);
+        return;
+    }
+    int rc = csgd_upload_bodies(d, bodies, n);
+    if (!rc)
+        rc = csgd_build_tree(d, 1);
+    if (!rc)
+        rc = store_pool(d, pool, pool_size, n);
+    csg_thread_set_error(rc);
+}
+
+static void compute_forces(const OctreeNode *pool, int root, Body *bodies, int n, double G,
+                           double softening, double theta, int exact)
+{
+    csgd_t *d = csg_thread_dev();
+    if (!d)
+        return;
+    if (!pool || (n > 0 && !bodies) || n < 0) {
+        csg_thread_set_error(CSG_ERR_BAD_ARG);
+        return;
+    }
+    if (n == 0) {
+        csg_thread_set_error(CSG_OK);
+        return;
+    }
+    int rc = load_pool(d, pool, root, bodies, n);
+    csgd_force_params p = force_params(G, softening, theta);
+    if (!rc)
+        rc = csgd_gravity_ex(d, &p, exact);
+    if (!rc)
+        rc = csgd_download_bodies(d, bodies, n);
+    if (!rc)
+        rc = csgd_sync(d);
+    csg_thread_set_error(rc);
+}
+
+CSG_EXPORT void octree_compute_forces(const OctreeNode *pool, int root, Body *bodies, int n,
+                                      double G, double softening, double theta)
+{
+    compute_forces(pool, root, bodies, n, G, softening, theta, 0);
+}
+
+CSG_EXPORT void csg_octree_compute_forces_exact(const OctreeNode *pool, int root, Body *bodies,
+                                                int n, double G, double softening, double theta)
+{
+    compute_forces(pool, root, bodies, n, G, softening, theta, 1);
+}
+
+CSG_EXPORT int octree_find_neighbors(const OctreeNode *pool, int root, const Body *bodies, int n,
+                                     double cx, double cy, double cz, double radius,
+                                     int *neighbor_buf, int buf_capacity)
+{
+    csgd_t *d = csg_thread_dev();
+    if (!d)
+        return 0;
+    if (!pool || n < 0 || (n > 0 && !bodies) || (buf_capacity > 0 && !neighbor_buf)) {
+        csg_thread_set_error(CSG_ERR_BAD_ARG);
+        return 0;
+    }
+    int count = 0;
+    int rc = load_pool(d, pool, root, bodies, n);
+    if (!rc)
+        rc = csgd_find_neighbors(d, cx, cy, cz, radius, neighbor_buf, buf_capacity, &count);
+    csg_thread_set_error(rc);
+    return rc ? 0 : count;
+}
+
+CSG_EXPORT void integrator_init_accelerations(Body *bodies, int n, double G, double softening,
+                                              double theta, OctreeNode *pool)
+{
+    csgd_t *d = csg_thread_dev();
+    if (!d)
+        return;
+    if (!pool || n < 0 || (n > 0 && !bodies)) {
+        csg_thread_set_error(CSG_ERR_BAD_ARG);
+        return;
+    }
+    csgd_force_params p = force_params(G, softening, theta);
+    int rc = csgd_upload_bodies(d, bodies, n);
+    if (!rc)
+        rc = csgd_build_tree(d, 1);
+    if (!rc)
+        rc = csgd_gravity(d, &p);
+    if (!rc)
+        rc = store_pool(d, pool, NULL, n); /* syncs */
+    if (!rc)
+        rc = csgd_download_bodies(d, bodies, n);
+    if (!rc)
+        rc = csgd_sync(d);
+    csg_thread_set_error(rc);
+}
+
+CSG_EXPORT void integrator_step(Body *bodies, int n, double dt, double G, double softening,
+                                double theta, OctreeNode *pool, int sph_enabled)
+{
+    csgd_t *d = csg_thread_dev();
+    if (!d)
+        return;
+    if (!pool || n < 0 || (n > 0 && !bodies)) {
+        csg_thread_set_error(CSG_ERR_BAD_ARG);
+        return;
+    }
+    csgd_force_params p = force_params(G, softening, theta);
+    int rc = csgd_upload_bodies(d, bodies, n);
+    if (!rc)
+        rc = csgd_substep(d, dt, &p, sph_enabled ? 1 : 0);
+    if (!rc)
+        rc = store_pool(d, pool, NULL, n);
+    if (!rc)
+        rc = csgd_download_bodies(d, bodies, n);
+    if (!rc)
+        rc = csgd_sync(d);
+    csg_thread_set_error(rc);
+}
+
+static void sph_pass(Body *bodies, int n, const OctreeNode *tree, int which)
+{
+    csgd_t *d = csg_thread_dev();
+    if (!d)
+        return;
+    if (!tree || n < 0 || (n > 0 && !bodies)) {
+        csg_thread_set_error(CSG_ERR_BAD_ARG);
+        return;
+    }
+    if (n == 0) {
+        csg_thread_set_error(CSG_OK);
+        return;
+    }
+    int rc = load_pool(d, tree, 0, bodies, n);
+    if (!rc)
+        rc = which == 0 ? csgd_sph_density(d) : csgd_sph_forces(d);
+    if (!rc)
+        rc = csgd_download_bodies(d, bodies, n);
+    if (!rc)
+        rc = csgd_sync(d);
+    csg_thread_set_error(rc);
+}
+
+CSG_EXPORT void sph_compute_density(Body *bodies, int n, const OctreeNode *tree)
+{
+    sph_pass(bodies, n, tree, 0);
+}
+
+CSG_EXPORT void sph_compute_forces(Body *bodies, int n, const OctreeNode *tree)
+{
+    sph_pass(bodies, n, tree, 1);
+}
+
+CSG_EXPORT void sph_apply_cooling(Body *bodies, int n, double dt)
+{
+    csgd_t *d = csg_thread_dev();
+    if (!d)
+        return;
+    if (n < 0 || (n > 0 && !bodies)) {
+        csg_thread_set_error(CSG_ERR_BAD_ARG);
+        return;
+    }
+    int rc = csgd_upload_bodies(d, bodies, n);
+    if (!rc)
+        rc = csgd_sph_cooling(d, dt);
+    if (!rc)
+        rc = csgd_download_bodies(d, bodies, n);
+    if (!rc)
+        rc = csgd_sync(d);
+    csg_thread_set_error(rc);
+}

@@ -1,0 +1,312 @@
+/*
+ * ics.c — seeded initial conditions.
+ *
+ * The reference draws its galaxies with a time-seeded xorshift64 generator
+ * (src/initial_conditions.c:8-38). Here the same published generator
+ * (Marsaglia xorshift, shifts 13/7/17; 53-bit uniforms; Box-Muller normals)
+ * is seeded explicitly so every run is reproducible.
+ *
+ * Two families:
+ *   csg_ref_spiral / csg_ref_merger: the reference's own galaxy recipe
+ *     (src/initial_conditions.c:40-144), used by cosmosim_create when the
+ *     application does not link the reference's generators;
+ *   csg_generate_ics kinds 0-4: the benchmark configurations (exponential
+ *     disks with the given scale lengths and masses, a Plummer bulge drawn by
+ *     the Aarseth-Henon-Wielen (1974) rejection method, a tilted merger).
+ */
+#include "capi_internal.h"
+
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#define CSG_PI 3.14159265358979323846
+
+typedef struct {
+    uint64_t s;
+} Rng;
+
+static void rng_seed(Rng *r, uint64_t seed) { r->s = seed ? seed : 1; }
+
+static uint64_t rng_next(Rng *r)
+{
+    uint64_t x = r->s;
+    x ^= x << 13;
+    x ^= x >> 7;
+    x ^= x << 17;
+    r->s = x;
+    return x;
+}
+
+static double rng_uniform(Rng *r) { return (double)(rng_next(r) >> 11) * (1.0 / 9007199254740992.0); }
+
+static double rng_normal(Rng *r)
+{
+    double u1 = rng_uniform(r);
+    double u2 = rng_uniform(r);
+    if (u1 < 1e-15)
+        u1 = 1e-15;
+    return sqrt(-2.0 * log(u1)) * cos(2.0 * CSG_PI * u2);
+}
+
+static void clear_body(Body *b)
+{
+    memset(b, 0, sizeof(*b));
+    b->type = BODY_STAR;
+}
+
+/* ---- the reference recipe (src/initial_conditions.c:40-144) -------------- */
+
+void csg_ref_spiral(Body *bodies, int n, double cx, double cy, double galaxy_mass,
+                    double disk_radius, double vx_bulk, double vy_bulk, uint64_t seed)
+{
+    Rng r;
+    rng_seed(&r, seed);
+    double rs = disk_radius / 4.0;
+    double zh = disk_radius * 0.02;
+    clear_body(&bodies[0]);
+    bodies[0].x = cx;
+    bodies[0].y = cy;
+    bodies[0].vx = vx_bulk;
+    bodies[0].vy = vy_bulk;
+    bodies[0].mass = galaxy_mass * 0.01;
+    for (int i = 1; i < n; i++) {
+        Body *b = &bodies[i];
+        clear_body(b);
+        double u = rng_uniform(&r);
+        if (u < 1e-15)
+            u = 1e-15;
+        double rad = -rs * log(1.0 - u * (1.0 - exp(-disk_radius / rs)));
+        double th0 = 2.0 * CSG_PI * rng_uniform(&r);
+        double arm = log(rad / rs + 0.1) / 0.27;
+        double th = th0 + 0.35 * exp(-rad / (disk_radius * 0.8)) * sin(2.0 * (th0 - arm));
+        b->x = cx + rad * cos(th);
+        b->y = cy + rad * sin(th);
+        b->z = rng_normal(&r) * zh;
+        b->mass = (rng_uniform(&r) < 0.01) ? 10.0 + rng_uniform(&r) * 90.0 : 1.0;
+        double menc = galaxy_mass * (1.0 - exp(-rad / rs) * (1.0 + rad / rs)) + bodies[0].mass;
+        if (rad < 1e-10)
+            rad = 1e-10;
+        double vc = sqrt(menc / rad);
+        double disp = 0.05 * vc;
+        double vt = vc + rng_normal(&r) * disp;
+        double vr = rng_normal(&r) * disp;
+        b->vx = vx_bulk - vt * sin(th) + vr * cos(th);
+        b->vy = vy_bulk + vt * cos(th) + vr * sin(th);
+        b->vz = rng_normal(&r) * disp * 0.1;
+    }
+}
+
+void csg_ref_merger(Body *bodies, int n, double separation, double approach_vel, uint64_t seed)
+{
+    int n1 = n / 2;
+    int n2 = n - n1;
+    double disk_radius = separation * 0.15;
+    double gm = (double)n1 * 2.0;
+    csg_ref_spiral(bodies, n1, -separation * 0.5, 0.0, gm, disk_radius, approach_vel,
+                   approach_vel * 0.3, seed);
+    csg_ref_spiral(bodies + n1, n2, separation * 0.5, 0.0, gm * 0.7, disk_radius * 0.8,
+                   -approach_vel, -approach_vel * 0.3, seed + 12345);
+}
+
+/* ---- benchmark configurations --------------------------------------------- */
+
+typedef struct {
+    double mass;       /* disk mass (excluding the central body) */
+    double rd;         /* scale length */
+    double zh;         /* vertical Gaussian scale */
+    double smbh;       /* central mass (0: none) */
+    double gas_frac;   /* inner fraction drawn as SPH gas */
+    double bulge_mass; /* Plummer bulge mass inside the disk (enclosed-mass term) */
+    double bulge_a;
+} DiskSpec;
+
+static double plummer_menc(double m, double a, double r)
+{
+    if (m <= 0.0)
+        return 0.0;
+    return m * r * r * r / pow(r * r + a * a, 1.5);
+}
+
+/* One exponential disk centred at the origin, in its own frame, following the
+   reference recipe (truncated radial draw to 4 scale lengths, two-arm spiral
+   perturbation, circular speed from the enclosed mass, 5% dispersion in the
+   plane and 0.5% vertically). Body 0 is the central mass when spec->smbh > 0.
+   Disk bodies share spec->mass equally. */
+static void disk(Body *out, int n, const DiskSpec *spec, Rng *r)
+{
+    int first = 0;
+    if (spec->smbh > 0.0 && n > 0) {
+        clear_body(&out[0]);
+        out[0].mass = spec->smbh;
+        out[0].type = BODY_SMBH;
+        first = 1;
+    }
+    int nd = n - first;
+    double mi = nd > 0 ? spec->mass / nd : 0.0;
+    double rmax = 4.0 * spec->rd;
+    double spacing = rmax / sqrt((double)(n > 0 ? n : 1));
+    for (int i = first; i < n; i++) {
+        Body *b = &out[i];
+        clear_body(b);
+        double u = rng_uniform(r);
+        if (u < 1e-15)
+            u = 1e-15;
+        double rad = -spec->rd * log(1.0 - u * (1.0 - exp(-rmax / spec->rd)));
+        double th0 = 2.0 * CSG_PI * rng_uniform(r);
+        double arm = log(rad / spec->rd + 0.1) / 0.27;
+        double th = th0 + 0.35 * exp(-rad / (rmax * 0.8)) * sin(2.0 * (th0 - arm));
+        b->x = rad * cos(th);
+        b->y = rad * sin(th);
+        b->z = rng_normal(r) * spec->zh;
+        b->mass = mi;
+        double x = rad / spec->rd;
+        double menc = spec->mass * (1.0 - exp(-x) * (1.0 + x)) + spec->smbh +
+                      plummer_menc(spec->bulge_mass, spec->bulge_a, rad);
+        if (rad < 1e-10)
+            rad = 1e-10;
+        double vc = sqrt(menc / rad);
+        double disp = 0.05 * vc;
+        double vt = vc + rng_normal(r) * disp;
+        double vr = rng_normal(r) * disp;
+        b->vx = -vt * sin(th) + vr * cos(th);
+        b->vy = vt * cos(th) + vr * sin(th);
+        b->vz = rng_normal(r) * disp * 0.1;
+        if (u < spec->gas_frac) { /* inner bodies are gas, src/initial_conditions.c:170-194 */
+            b->type = BODY_GAS;
+            double mg = spec->mass * (1.0 - exp(-x));
+            double vloc = sqrt(mg / rad);
+            b->internal_energy = 0.5 * vloc * vloc / (CSG_SPH_GAMMA - 1.0);
+            b->smoothing_h = spacing * 2.0;
+        }
+    }
+}
+
+/* Plummer sphere of mass m, scale a, truncated at 20a; velocities by the
+   Aarseth-Henon-Wielen rejection method. */
+static void plummer(Body *out, int n, double m, double a, Rng *r)
+{
+    double mi = n > 0 ? m / n : 0.0;
+    for (int i = 0; i < n; i++) {
+        Body *b = &out[i];
+        clear_body(b);
+        double rad;
+        do {
+            double u = rng_uniform(r);
+            if (u < 1e-12)
+                u = 1e-12;
+            rad = a / sqrt(pow(u, -2.0 / 3.0) - 1.0);
+        } while (!(rad < 20.0 * a));
+        double cz = 2.0 * rng_uniform(r) - 1.0;
+        double ph = 2.0 * CSG_PI * rng_uniform(r);
+        double sz = sqrt(1.0 - cz * cz);
+        b->x = rad * sz * cos(ph);
+        b->y = rad * sz * sin(ph);
+        b->z = rad * cz;
+        double q, g;
+        do {
+            q = rng_uniform(r);
+            g = 0.1 * rng_uniform(r);
+        } while (g > q * q * pow(1.0 - q * q, 3.5));
+        double ve = sqrt(2.0 * m / sqrt(rad * rad + a * a));
+        double v = q * ve;
+        double vz = 2.0 * rng_uniform(r) - 1.0;
+        double vph = 2.0 * CSG_PI * rng_uniform(r);
+        double vs = sqrt(1.0 - vz * vz);
+        b->vx = v * vs * cos(vph);
+        b->vy = v * vs * sin(vph);
+        b->vz = v * vz;
+        b->mass = mi;
+    }
+}
+
+static void shift(Body *b, int n, double x, double y, double z, double vx, double vy, double vz)
+{
+    for (int i = 0; i < n; i++) {
+        b[i].x += x;
+        b[i].y += y;
+        b[i].z += z;
+        b[i].vx += vx;
+        b[i].vy += vy;
+        b[i].vz += vz;
+    }
+}
+
+static void tilt_x(Body *b, int n, double deg)
+{
+    double t = deg * CSG_PI / 180.0, c = cos(t), s = sin(t);
+    for (int i = 0; i < n; i++) {
+        double y = b[i].y, z = b[i].z;
+        b[i].y = y * c - z * s;
+        b[i].z = y * s + z * c;
+        double vy = b[i].vy, vz = b[i].vz;
+        b[i].vy = vy * c - vz * s;
+        b[i].vz = vy * s + vz * c;
+    }
+}
+
+/* Two disks, mass ratio 1:1.2, the second tilted 50 deg about x; separation
+   30 scale lengths; nearly radial approach at 0.3 v_circ (tangential/radial
+   0.17, as the reference's merger comment gives); each with an SMBH of
+   0.005 x its disk mass. */
+static void merger(Body *out, int n, double gas_frac, Rng *r)
+{
+    int n1 = n / 2, n2 = n - n1;
+    DiskSpec g1 = {1.0, 1.0, 0.1, 0.005 * 1.0, gas_frac, 0.0, 0.0};
+    DiskSpec g2 = {1.2, 1.3, 0.13, 0.005 * 1.2, gas_frac, 0.0, 0.0};
+    disk(out, n1, &g1, r);
+    disk(out + n1, n2, &g2, r);
+    tilt_x(out + n1, n2, 50.0);
+    double m1 = g1.mass + g1.smbh, m2 = g2.mass + g2.smbh, mt = m1 + m2;
+    double sep = 30.0;
+    double vcirc = sqrt(mt / sep);
+    double vrel = 0.3 * vcirc;
+    double vrad = vrel / sqrt(1.0 + 0.17 * 0.17), vtan = 0.17 * vrad;
+    shift(out, n1, -sep * m2 / mt, 0.0, 0.0, vrad * m2 / mt, vtan * m2 / mt, 0.0);
+    shift(out + n1, n2, sep * m1 / mt, 0.0, 0.0, -vrad * m1 / mt, -vtan * m1 / mt, 0.0);
+}
+
+int csg_generate_ics_impl(int kind, int n, uint64_t seed, Body *out)
+{
+    if (n < 0 || (n > 0 && !out))
+        return -1;
+    Rng r;
+    rng_seed(&r, seed);
+    switch (kind) {
+    case 0: { /* single disk: R_d 1, z 0.1, mass 1, SMBH 0.01 */
+        DiskSpec s = {1.0, 1.0, 0.1, 0.01, 0.0, 0.0, 0.0};
+        disk(out, n, &s, &r);
+        break;
+    }
+    case 1:
+        merger(out, n, 0.10, &r);
+        break;
+    case 2: { /* Plummer bulge 30% (a 0.5) + disk 70%, equal masses, total 1 */
+        int nb = (int)(0.3 * (double)n);
+        int nd = n - nb;
+        double mb = (double)nb / (double)n, md = (double)nd / (double)n;
+        plummer(out, nb, mb, 0.5, &r);
+        DiskSpec s = {md, 1.0, 0.1, 0.0, 0.0, mb, 0.5};
+        disk(out + nb, nd, &s, &r);
+        break;
+    }
+    case 3: { /* ensemble member: R_d in [0.5, 2], SMBH fraction in [0.001, 0.02] */
+        double rd = 0.5 + 1.5 * rng_uniform(&r);
+        double f = 0.001 + 0.019 * rng_uniform(&r);
+        DiskSpec s = {1.0, rd, 0.1 * rd, f, 0.0, 0.0, 0.0};
+        disk(out, n, &s, &r);
+        break;
+    }
+    case 4:
+        merger(out, n, 0.0, &r);
+        break;
+    default:
+        return -1;
+    }
+    return n;
+}
+
+CSG_EXPORT int csg_generate_ics(int kind, int n, uint64_t seed, Body *out)
+{
+    return csg_generate_ics_impl(kind, n, seed, out);
+}

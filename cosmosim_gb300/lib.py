@@ -1,0 +1,279 @@
+"""ctypes binding of libcosmosim_gb300.so — the reference API over numpy arrays.
+
+The names and argument meanings follow cosmosim's C API (octree.h,
+integrator.h, sph.h, cosmosim_api.h); Body and OctreeNode arrays are numpy
+arrays of the ABI dtypes in ``cosmosim_gb300.abi``. There is no fallback: if
+the library is missing, loading raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .abi import BODY_DTYPE, NODE_DTYPE, CosmosimConfig, ptr
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcosmosim_gb300.so")
+
+PREC_FP64 = 0
+PREC_FP32_MIXED = 1
+
+_vp = ctypes.c_void_p
+_d = ctypes.c_double
+_i = ctypes.c_int
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+class CsgSimParams(ctypes.Structure):
+    _fields_ = [("G", _d), ("softening", _d), ("theta", _d), ("dt", _d),
+                ("substeps", _i), ("sph", _i), ("precision", _i)]
+
+
+class CudaError(RuntimeError):
+    pass
+
+
+_SIGS = {
+    "octree_build": ([_vp, _ip, _vp, _i], None),
+    "octree_compute_forces": ([_vp, _i, _vp, _i, _d, _d, _d], None),
+    "csg_octree_compute_forces_exact": ([_vp, _i, _vp, _i, _d, _d, _d], None),
+    "octree_find_neighbors": ([_vp, _i, _vp, _i, _d, _d, _d, _d, _vp, _i], _i),
+    "integrator_step": ([_vp, _i, _d, _d, _d, _d, _vp, _i], None),
+    "integrator_init_accelerations": ([_vp, _i, _d, _d, _d, _vp], None),
+    "sph_compute_density": ([_vp, _i, _vp], None),
+    "sph_compute_forces": ([_vp, _i, _vp], None),
+    "sph_apply_cooling": ([_vp, _i, _d], None),
+    "cosmosim_default_config": ([], CosmosimConfig),
+    "cosmosim_create": ([CosmosimConfig], _vp),
+    "cosmosim_create_ex": ([CosmosimConfig, _d, _d, _i], _vp),
+    "cosmosim_create_from_bodies": ([_vp, _i, ctypes.POINTER(CsgSimParams)], _vp),
+    "cosmosim_step": ([_vp], None),
+    "cosmosim_get_bodies": ([_vp], _vp),
+    "cosmosim_get_count": ([_vp], _i),
+    "cosmosim_get_active_count": ([_vp], _i),
+    "cosmosim_get_sim_time": ([_vp], _d),
+    "cosmosim_destroy": ([_vp], None),
+    "cosmosim_last_error": ([_vp], _i),
+    "cosmosim_substeps_async": ([_vp, _i], _i),
+    "cosmosim_sync": ([_vp], _i),
+    "cosmosim_set_stream": ([_vp, _vp], _i),
+    "cosmosim_copy_bodies": ([_vp, _vp, _i], _i),
+    "cosmosim_build_tree_async": ([_vp], _i),
+    "cosmosim_gravity_async": ([_vp], _i),
+    "cosmosim_enable_stats": ([_vp, _i], _i),
+    "cosmosim_interactions": ([_vp, ctypes.POINTER(ctypes.c_int64)], _i),
+    "cosmosim_node_count": ([_vp, _ip], _i),
+    "cosmosim_set_precision": ([_vp, _i], _i),
+    "csg_last_error": ([], _i),
+    "csg_error_string": ([_i], ctypes.c_char_p),
+    "csg_set_precision": ([_i], None),
+    "csg_generate_ics": ([_i, _i, ctypes.c_uint64, _vp], _i),
+}
+
+_lib = None
+
+
+def load(path=None):
+    """Loads (once) and returns the ctypes library; raises if it is missing."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise FileNotFoundError(
+            f"{p} not built: run `python -m cosmosim_gb300.build` (there is no CPU fallback)")
+    lib = ctypes.CDLL(p)
+    for name, (args, res) in _SIGS.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def exported_symbols():
+    return sorted(_SIGS)
+
+
+def _check(lib, what):
+    rc = lib.csg_last_error()
+    if rc:
+        raise CudaError(f"{what}: {lib.csg_error_string(rc).decode()} (code {rc})")
+
+
+def last_error():
+    return load().csg_last_error()
+
+
+def set_precision(p):
+    load().csg_set_precision(p)
+
+
+# ---- free functions (reference octree.h / integrator.h / sph.h) ----
+
+def octree_build(bodies, pool=None):
+    lib = load()
+    n = len(bodies)
+    if pool is None:
+        pool = np.zeros(max(8 * n, 8), dtype=NODE_DTYPE)
+    ps = ctypes.c_int(0)
+    lib.octree_build(ptr(pool), ctypes.byref(ps), ptr(bodies), n)
+    _check(lib, "octree_build")
+    return pool, ps.value
+
+
+def octree_compute_forces(pool, bodies, G, softening, theta, root=0, exact=False):
+    lib = load()
+    f = lib.csg_octree_compute_forces_exact if exact else lib.octree_compute_forces
+    f(ptr(pool), root, ptr(bodies), len(bodies), G, softening, theta)
+    _check(lib, "octree_compute_forces")
+
+
+def octree_find_neighbors(pool, bodies, center, radius, cap, root=0):
+    lib = load()
+    buf = np.full(max(cap, 1), -1, dtype=np.int32)
+    k = lib.octree_find_neighbors(ptr(pool), root, ptr(bodies), len(bodies), center[0],
+                                  center[1], center[2], radius, ptr(buf), cap)
+    _check(lib, "octree_find_neighbors")
+    return buf[:k].copy()
+
+
+def integrator_step(bodies, dt, G, softening, theta, pool, sph_enabled):
+    lib = load()
+    lib.integrator_step(ptr(bodies), len(bodies), dt, G, softening, theta, ptr(pool),
+                        int(sph_enabled))
+    _check(lib, "integrator_step")
+
+
+def integrator_init_accelerations(bodies, G, softening, theta, pool):
+    lib = load()
+    lib.integrator_init_accelerations(ptr(bodies), len(bodies), G, softening, theta, ptr(pool))
+    _check(lib, "integrator_init_accelerations")
+
+
+def sph_compute_density(bodies, pool):
+    lib = load()
+    lib.sph_compute_density(ptr(bodies), len(bodies), ptr(pool))
+    _check(lib, "sph_compute_density")
+
+
+def sph_compute_forces(bodies, pool):
+    lib = load()
+    lib.sph_compute_forces(ptr(bodies), len(bodies), ptr(pool))
+    _check(lib, "sph_compute_forces")
+
+
+def sph_apply_cooling(bodies, dt):
+    lib = load()
+    lib.sph_apply_cooling(ptr(bodies), len(bodies), dt)
+    _check(lib, "sph_apply_cooling")
+
+
+def generate_ics(kind, n, seed):
+    """Seeded initial conditions of benchmark configuration `kind` (0-4)."""
+    lib = load()
+    out = np.zeros(n, dtype=BODY_DTYPE)
+    if lib.csg_generate_ics(kind, n, seed, ptr(out)) != n:
+        raise ValueError(f"bad ICs request kind={kind} n={n}")
+    return out
+
+
+# ---- handle API (reference cosmosim_api.h) ----
+
+class Sim:
+    """A device-resident simulation handle (cosmosim_create / _create_from_bodies)."""
+
+    def __init__(self, handle):
+        if not handle:
+            lib = load()
+            raise CudaError(f"create failed: {lib.csg_error_string(lib.csg_last_error()).decode()}")
+        self.h = ctypes.c_void_p(handle)
+        self.lib = load()
+
+    @classmethod
+    def from_config(cls, config=None):
+        lib = load()
+        return cls(lib.cosmosim_create(config or lib.cosmosim_default_config()))
+
+    @classmethod
+    def from_bodies(cls, bodies, G=1.0, softening=0.01, theta=0.5, dt=1e-3, substeps=1,
+                    sph=False, precision=PREC_FP64):
+        lib = load()
+        p = CsgSimParams(G, softening, theta, dt, substeps, int(sph), precision)
+        return cls(lib.cosmosim_create_from_bodies(ptr(bodies), len(bodies), ctypes.byref(p)))
+
+    def _rc(self, rc, what):
+        if rc:
+            raise CudaError(f"{what}: {self.lib.csg_error_string(rc).decode()} (code {rc})")
+
+    def step(self):
+        self.lib.cosmosim_step(self.h)
+        self._rc(self.lib.cosmosim_last_error(self.h), "cosmosim_step")
+
+    def substeps_async(self, k):
+        self._rc(self.lib.cosmosim_substeps_async(self.h, k), "substeps")
+
+    def sync(self):
+        self._rc(self.lib.cosmosim_sync(self.h), "sync")
+
+    def set_stream(self, stream_ptr):
+        self._rc(self.lib.cosmosim_set_stream(self.h, ctypes.c_void_p(stream_ptr)), "set_stream")
+
+    def build_tree_async(self):
+        self._rc(self.lib.cosmosim_build_tree_async(self.h), "build")
+
+    def gravity_async(self):
+        self._rc(self.lib.cosmosim_gravity_async(self.h), "gravity")
+
+    def set_precision(self, p):
+        self._rc(self.lib.cosmosim_set_precision(self.h, p), "precision")
+
+    def enable_stats(self, on=True):
+        self._rc(self.lib.cosmosim_enable_stats(self.h, int(on)), "stats")
+
+    def interactions(self):
+        v = ctypes.c_int64(0)
+        self._rc(self.lib.cosmosim_interactions(self.h, ctypes.byref(v)), "interactions")
+        return v.value
+
+    def node_count(self):
+        v = ctypes.c_int(0)
+        self._rc(self.lib.cosmosim_node_count(self.h, ctypes.byref(v)), "node_count")
+        return v.value
+
+    @property
+    def count(self):
+        return self.lib.cosmosim_get_count(self.h)
+
+    @property
+    def active_count(self):
+        return self.lib.cosmosim_get_active_count(self.h)
+
+    @property
+    def sim_time(self):
+        return self.lib.cosmosim_get_sim_time(self.h)
+
+    def bodies(self):
+        """Copy of the current bodies (cosmosim_copy_bodies)."""
+        out = np.zeros(self.count, dtype=BODY_DTYPE)
+        self._rc(self.lib.cosmosim_copy_bodies(self.h, ptr(out), len(out)), "copy_bodies")
+        return out
+
+    def get_bodies_view(self):
+        """The borrowed array cosmosim_get_bodies returns, copied into numpy."""
+        p = self.lib.cosmosim_get_bodies(self.h)
+        n = self.count
+        buf = (ctypes.c_char * (n * BODY_DTYPE.itemsize)).from_address(p)
+        return np.frombuffer(buf, dtype=BODY_DTYPE, count=n).copy()
+
+    def close(self):
+        if self.h:
+            self.lib.cosmosim_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

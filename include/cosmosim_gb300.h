@@ -1,0 +1,114 @@
+/*
+ * cosmosim_gb300.h — additive entry points of libcosmosim_gb300.so.
+ *
+ * Nothing here replaces a reference symbol; these are the extensions a caller
+ * may use beside the drop-in API of cosmosim_abi.h. None has a counterpart in
+ * the reference unless its comment names one.
+ *
+ * Error convention (as the reference's API): no call aborts or traps. Free
+ * functions record their status per calling thread (csg_last_error); handle
+ * calls record it per handle (cosmosim_last_error).
+ */
+#ifndef COSMOSIM_GB300_H
+#define COSMOSIM_GB300_H
+
+#include <stdint.h>
+#include "cosmosim_abi.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Error codes. */
+#define CSG_OK 0
+#define CSG_ERR_CUDA 1
+#define CSG_ERR_NOMEM 2
+#define CSG_ERR_NODE_CAPACITY 3
+#define CSG_ERR_BAD_ARG 4
+#define CSG_ERR_BAD_POOL 5
+#define CSG_ERR_WALK_LIMIT 6
+#define CSG_ERR_NO_DEVICE 7
+#define CSG_ERR_UNSUPPORTED 8
+
+/* Walk precision. FP64 is the drop-in default. FP32_MIXED evaluates pair
+   accelerations in FP32 (positions as float hi/lo pairs, Kahan-compensated
+   per-body sums) with FP64 tree moments, drift and opening ties. */
+#define CSG_PREC_FP64 0
+#define CSG_PREC_FP32_MIXED 1
+
+/* Status of the calling thread's last free-function call (octree_*,
+   integrator_*, sph_*); 0 = success. Reset by every call. */
+CSG_EXPORT int csg_last_error(void);
+CSG_EXPORT const char *csg_error_string(int code);
+
+/* Precision the calling thread's free functions use (default FP64). */
+CSG_EXPORT void csg_set_precision(int precision);
+
+/* Status of the handle's last call; 0 = success. The reference API has no
+   error channel; this is the additive one its survey asks for. */
+CSG_EXPORT int cosmosim_last_error(SimHandle handle);
+
+/* Run-time physics parameters for a handle. */
+typedef struct {
+    double G;          /* gravitational constant (reference api: 1.0) */
+    double softening;  /* Plummer softening (reference api: 1.5) */
+    double theta;      /* opening angle */
+    double dt;         /* step */
+    int substeps;      /* substeps per cosmosim_step */
+    int sph;           /* 1: SPH density/forces/cooling every substep */
+    int precision;     /* CSG_PREC_* */
+} CsgSimParams;
+
+/* A handle over caller-supplied bodies (copied), usable with every
+   cosmosim_* call. The initial accelerations are computed as in
+   cosmosim_create (tree + gravity). Returns NULL on failure. */
+CSG_EXPORT SimHandle cosmosim_create_from_bodies(const Body *bodies, int n,
+                                                 const CsgSimParams *params);
+
+/* cosmosim_create with run-time G, softening and precision. */
+CSG_EXPORT SimHandle cosmosim_create_ex(CosmosimConfig config, double G, double softening,
+                                        int precision);
+
+/* Device-resident stepping: k substeps, asynchronous on the handle's stream
+   (no host copy). cosmosim_step calls this, then marks the host copy stale. */
+CSG_EXPORT int cosmosim_substeps_async(SimHandle handle, int k);
+CSG_EXPORT int cosmosim_sync(SimHandle handle);
+
+/* Runs the handle's work on the given cudaStream_t (NULL: its own stream). */
+CSG_EXPORT int cosmosim_set_stream(SimHandle handle, void *cuda_stream);
+
+/* Copies the bodies out (n must equal cosmosim_get_count). */
+CSG_EXPORT int cosmosim_copy_bodies(SimHandle handle, Body *out, int n);
+
+/* Phase-level calls for measurement: rebuild the tree from the current
+   positions; run only the gravity walk on the current tree. Asynchronous. */
+CSG_EXPORT int cosmosim_build_tree_async(SimHandle handle);
+CSG_EXPORT int cosmosim_gravity_async(SimHandle handle);
+
+/* Interaction counting (accepted cells + leaves, the reference walk's unit). */
+CSG_EXPORT int cosmosim_enable_stats(SimHandle handle, int on);
+CSG_EXPORT int cosmosim_interactions(SimHandle handle, int64_t *total);
+CSG_EXPORT int cosmosim_node_count(SimHandle handle, int *n_nodes);
+CSG_EXPORT int cosmosim_set_precision(SimHandle handle, int precision);
+
+/* Free-function parity mode: gravity with the reference's exact operation
+   sequence (no fused multiply-add, 1/(r2*sqrt(r2))). Same signature as
+   octree_compute_forces. */
+CSG_EXPORT void csg_octree_compute_forces_exact(const OctreeNode *pool, int root, Body *bodies,
+                                                int n, double G, double softening,
+                                                double theta);
+
+/* Seeded initial conditions following the reference generators
+   (src/initial_conditions.c) with the benchmark configurations' parameters.
+     kind 0: exponential-disk spiral, 20k default, disk mass 1, SMBH 0.01
+     kind 1: two-disk merger, mass ratio 1:1.2, 50 deg tilt, 10% gas, SPH fields
+     kind 2: Plummer bulge (30%, a = 0.5) + exponential disk (70%), total mass 1
+     kind 3: one ensemble galaxy (scale length, SMBH fraction from seed)
+     kind 4: two-disk merger, stars only
+   Returns the number of bodies written (n). */
+CSG_EXPORT int csg_generate_ics(int kind, int n, uint64_t seed, Body *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
