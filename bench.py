@@ -1,0 +1,366 @@
+"""Benchmark of the gravity/SPH substep: body-substeps/s, FP32-mixed vs FP64.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl cuda|reference]
+
+Workload (default): the 100,000-body quasar merger — two exponential disks,
+mass ratio 1:1.2, 50 deg tilt, 10% SPH gas, theta 0.5, softening 0.01,
+dt 1e-3 — seeded synthetic initial conditions of that shape (no dataset).
+A step is one kick-drift-kick substep: tree build, gravity walk, SPH density
+and forces, kicks, cooling. The headline `value` is the FP32-mixed walk; the
+FP64 plain walk is measured on the same workload beside it.
+
+Timing: W untimed warm-up substeps, then K substeps each bracketed by CUDA
+events on the library's stream (torch's current stream), with a 512 MB write
+between substeps to flush L2 (the 100k working set fits in L2). `e2e` is the
+same metric through the reference-facing C call integrator_step() with the
+Body array and pool in pinned host memory, host<->device copies included.
+Under torchrun (N > 1) every rank runs an independent replica (the path does
+not shard: replicas only); value = all ranks' body-substeps / max time.
+
+--impl reference times the reference's CPU algorithm (the oracle port in
+oracle/, OpenMP on all host cores) on the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "body-substeps/s (FP32-mixed walk; FP64 plain beside it)"
+UNIT = "body-substeps/s"
+
+CONFIGS = {
+    "merger100k": dict(kind=1, n=100_000, theta=0.5, eps=0.01, dt=1e-3, sph=True,
+                       desc="quasar merger: 2 exp. disks 1:1.2, 50deg tilt, 10% SPH gas"),
+    "disk20k": dict(kind=0, n=20_000, theta=0.5, eps=0.01, dt=1e-3, sph=False,
+                    desc="single exponential-disk galaxy (reference default run)"),
+    "bulge1m": dict(kind=2, n=1_000_000, theta=0.5, eps=0.005, dt=1e-3, sph=False,
+                    desc="Plummer bulge 300k + exponential disk 700k"),
+}
+FLOP_PER_INTERACTION = 20  # monopole body-cell interaction (SURVEY 8d unit)
+SEED = 0x5EED0000
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def flush_buffer(torch):
+    return torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+
+def time_substeps(torch, sim, k, flush):
+    """Sum of per-substep device times (events on the launching stream)."""
+    st = torch.cuda.current_stream()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(k)]
+    for a, b in evs:
+        flush.zero_()
+        a.record(st)
+        sim.substeps_async(1)
+        b.record(st)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in evs) / 1e3
+
+
+def time_phase(torch, fn, k, flush):
+    st = torch.cuda.current_stream()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(k)]
+    for a, b in evs:
+        flush.zero_()
+        a.record(st)
+        fn()
+        b.record(st)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in evs) / k / 1e3
+
+
+def rel_err_stats(a, b):
+    err = np.linalg.norm(a - b, axis=1) / np.maximum(np.linalg.norm(b, axis=1), 1e-300)
+    return {"median": float(np.median(err)), "p99": float(np.quantile(err, 0.99)),
+            "max": float(err.max()),
+            "global": float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))}
+
+
+def acc(b):
+    return np.stack([b["ax"], b["ay"], b["az"]], axis=1)
+
+
+def run_cuda(args, torch, lib, cfg, rank, world):
+    dev = torch.cuda.current_device()
+    stream = torch.cuda.current_stream()
+    assert stream.cuda_stream != 0, "the library needs a non-default stream handle"
+    flush = flush_buffer(torch)
+    bodies = lib.generate_ics(cfg["kind"], cfg["n"], SEED + rank)
+    n_alive = int((bodies["mass"] > 0).sum())
+    common = dict(softening=cfg["eps"], theta=cfg["theta"], dt=cfg["dt"], sph=cfg["sph"])
+    out = {}
+    clocks = None
+    for prec, name in ((lib.PREC_FP32_MIXED, "fp32_mixed"), (lib.PREC_FP64, "fp64")):
+        sim = lib.Sim.from_bodies(bodies, precision=prec, **common)
+        sim.set_stream(stream.cuda_stream)
+        for _ in range(args.warmup):
+            flush.zero_()
+            sim.substeps_async(1)
+        torch.cuda.synchronize()
+        k = args.steps if name == "fp32_mixed" else max(3, args.steps // args.fp64_divisor)
+        l0 = sim.launch_count()
+        sampler = ClockSampler(dev) if name == "fp32_mixed" else None
+        if sampler:
+            sampler.start()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        secs = time_substeps(torch, sim, k, flush)
+        sim.sync()  # raises if any substep reported an error
+        if sampler:
+            clocks = sampler.stop()
+        launches = sim.launch_count() - l0
+        # phases on the state reached: tree build and gravity walk alone
+        build_s = time_phase(torch, sim.build_tree_async, 5, flush)
+        walk_s = time_phase(torch, sim.gravity_async, 5, flush)
+        sim.sync()
+        sim.enable_stats(True)
+        sim.gravity_async()
+        inter = sim.interactions()
+        sim.enable_stats(False)
+        out[name] = dict(secs=secs, steps=k, launches=launches, build_s=build_s, walk_s=walk_s,
+                         interactions=inter, state=sim.bodies() if name == "fp32_mixed" else None)
+        sim.close()
+    # precision and algorithmic error on the FP32 run's final state
+    st = out["fp32_mixed"]["state"]
+    g64 = lib.Sim.from_bodies(st, precision=lib.PREC_FP64, **common)
+    g32 = lib.Sim.from_bodies(st, precision=lib.PREC_FP32_MIXED, **common)
+    a64, a32 = acc(g64.bodies()), acc(g32.bodies())
+    alive = st["mass"] > 0
+    rng = np.random.default_rng(1)
+    sample = rng.choice(np.nonzero(alive)[0], size=min(4096, int(alive.sum())), replace=False)
+    direct = g64.direct_forces(sample)
+    errors = {"fp32_vs_fp64_walk": rel_err_stats(a32[alive], a64[alive]),
+              "fp64_walk_vs_direct": rel_err_stats(a64[sample], direct),
+              "fp32_walk_vs_direct": rel_err_stats(a32[sample], direct),
+              "direct_sample": int(len(sample))}
+    g64.close()
+    g32.close()
+    # end to end through integrator_step with pinned host buffers
+    pinned = torch.empty(cfg["n"] * 168, dtype=torch.uint8, pin_memory=True)
+    hb = pinned.numpy().view(bodies.dtype)
+    hb[:] = bodies
+    from cosmosim_gb300.abi import NODE_DTYPE
+
+    pool_t = torch.empty(8 * cfg["n"] * 104, dtype=torch.uint8, pin_memory=True)
+    pool = pool_t.numpy().view(NODE_DTYPE)
+    lib.set_precision(lib.PREC_FP32_MIXED)
+    lib.integrator_init_accelerations(hb, 1.0, cfg["eps"], cfg["theta"], pool)
+    for _ in range(2):
+        lib.integrator_step(hb, cfg["dt"], 1.0, cfg["eps"], cfg["theta"], pool, int(cfg["sph"]))
+    ke = max(3, args.steps // args.e2e_divisor)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        lib.integrator_step(hb, cfg["dt"], 1.0, cfg["eps"], cfg["theta"], pool, int(cfg["sph"]))
+    e2e_s = time.perf_counter() - t0
+    lib.set_precision(lib.PREC_FP64)
+    _, nodes = lib.octree_build(hb, pool)
+    return dict(n_alive=n_alive, runs=out, errors=errors, clocks=clocks, e2e_s=e2e_s, e2e_steps=ke,
+                e2e_nodes=nodes)
+
+
+def cpu_reference(cfg, steps, seed=SEED, time_budget=None):
+    """The reference's CPU algorithm (oracle port, OpenMP on every host core)."""
+    from cosmosim_gb300 import lib
+    from cosmosim_gb300.abi import NODE_DTYPE
+    from oracle import orc
+
+    orc.build()
+    o = orc.Oracle()
+    cores = o.set_threads(os.cpu_count() or 1)
+    b = lib.generate_ics(cfg["kind"], cfg["n"], seed)
+    pool = np.zeros(8 * cfg["n"], dtype=NODE_DTYPE)
+    o.integrator_init_accelerations(b, 1.0, cfg["eps"], cfg["theta"], pool)
+    done = 0
+    t0 = time.perf_counter()
+    while done < steps:
+        o.integrator_step(b, cfg["dt"], 1.0, cfg["eps"], cfg["theta"], pool, int(cfg["sph"]))
+        done += 1
+        if time_budget and time.perf_counter() - t0 > time_budget and done >= 2:
+            break
+    secs = time.perf_counter() - t0
+    n_alive = int((b["mass"] > 0).sum())
+    return {"value": n_alive * done / secs, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{done} substeps of the {cfg['n']}-body workload (oracle/orc.c, "
+                      f"OpenMP, {cores} threads)", "secs": secs, "steps": done}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="cuda", choices=["cuda", "reference"])
+    ap.add_argument("--config", default="merger100k", choices=sorted(CONFIGS))
+    ap.add_argument("--fp64-divisor", type=int, default=8,
+                    help="FP64 run times steps/divisor substeps")
+    ap.add_argument("--e2e-divisor", type=int, default=8)
+    ap.add_argument("--cpu-budget", type=float, default=20.0,
+                    help="seconds of CPU work for the cpu_baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    cfg = CONFIGS[args.config]
+    rank, world, local = dist_env()
+    config = {"workload": f"{args.config}: {cfg['desc']}", "n_bodies": cfg["n"],
+              "theta": cfg["theta"], "softening": cfg["eps"], "dt": cfg["dt"],
+              "sph": cfg["sph"], "l2": "512 MB flush between timed substeps",
+              "parallelism": f"replicas x{world}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        ref = cpu_reference(cfg, args.steps + args.warmup, time_budget=None)
+        line = {"metric": METRIC, "value": ref["value"], "unit": UNIT, "impl": "reference",
+                "n_gpus": world, "steps": ref["steps"], "warmup": 0,
+                "ms_per_step": 1e3 * ref["secs"] / ref["steps"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": config,
+                "cpu_baseline": {k: ref[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": ref["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+
+    torch.cuda.set_device(local)
+    # a dedicated stream: the library and the timing events share it
+    work_stream = torch.cuda.Stream()
+    torch.cuda.set_stream(work_stream)
+    if world > 1:
+        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from cosmosim_gb300 import lib
+
+    lib.load()
+    fp32_peak, fp64_peak = lib.measure_fp_peaks()
+    r = run_cuda(args, torch, lib, cfg, rank, world)
+    f32, f64 = r["runs"]["fp32_mixed"], r["runs"]["fp64"]
+    # whole-job aggregation: max time over ranks
+    t32, t64, te = f32["secs"], f64["secs"], r["e2e_s"]
+    if world > 1:
+        t = torch.tensor([t32, t64, te], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t32, t64, te = t.tolist()
+    work32 = r["n_alive"] * f32["steps"] * world
+    work64 = r["n_alive"] * f64["steps"] * world
+    value = work32 / t32
+    v64 = work64 / t64
+    e2e_value = r["n_alive"] * r["e2e_steps"] * world / te
+    achieved = FLOP_PER_INTERACTION * f32["interactions"] / f32["walk_s"] / 1e12
+    achieved64 = FLOP_PER_INTERACTION * f64["interactions"] / f64["walk_s"] / 1e12
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": f32["steps"],
+        "warmup": args.warmup, "ms_per_step": 1e3 * f32["secs"] / f32["steps"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 pair forces / f64 positions, tree moments, drift", "data": "synthetic",
+        "config": config,
+        "fp64_plain": {"value": v64, "ms_per_step": 1e3 * f64["secs"] / f64["steps"],
+                       "steps": f64["steps"], "fp32_mixed_speedup": value / v64,
+                       "walk_ms": 1e3 * f64["walk_s"],
+                       "walk_tflops": achieved64, "fp64_peak_tflops": fp64_peak,
+                       "walk_frac_of_fp64_peak": achieved64 / fp64_peak},
+        "phases_ms": {"build": 1e3 * f32["build_s"], "walk_fp32": 1e3 * f32["walk_s"],
+                      "walk_fp64": 1e3 * f64["walk_s"]},
+        "interactions_per_substep": f32["interactions"],
+        "roofline": {"bound": "fp32-pipe", "kernel": "k_walk32 (gravity walk)",
+                     "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak, "traffic": None,
+                     "note": "20 flop per reference interaction / walk event time; peak = FP32 "
+                             "FMA throughput measured live by csg_measure_fp_peaks (the walk is "
+                             "CUDA-core bound: no dense contraction, tree resident in L2)"},
+        "errors": r["errors"],
+        "e2e": {"value": e2e_value, "unit": UNIT, "api": "integrator_step (pinned host Body[])",
+                "steps": r["e2e_steps"], "h2d_bytes_per_step": 168 * cfg["n"],
+                "d2h_bytes_per_step": 168 * cfg["n"] + 104 * r["e2e_nodes"]},
+        "gpu_launches": f32["launches"],
+        "clocks": r["clocks"],
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cb = cpu_reference(cfg, 10**9, time_budget=args.cpu_budget)
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        line["speedup_vs_cpu"] = {"fp32_mixed": value / cb["value"], "fp64_plain": v64 / cb["value"],
+                                  "e2e": e2e_value / cb["value"]}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

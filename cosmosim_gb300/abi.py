@@ -66,7 +66,15 @@ def new_pool(n_nodes):
 
 
 def ptr(a):
-    """Raw data pointer of a C-contiguous numpy array, as c_void_p."""
+    """Raw data pointer of a C-contiguous numpy array, as c_void_p.
+
+    Structured arrays must have exactly the ABI layout: numpy operations such
+    as concatenate repack padded dtypes (Body becomes 164 bytes), and such an
+    array would be read with the wrong stride."""
     if not a.flags["C_CONTIGUOUS"]:
         raise ValueError("array must be C-contiguous")
+    if a.dtype.names is not None and a.dtype not in (BODY_DTYPE, NODE_DTYPE):
+        raise TypeError(f"structured array has layout {a.dtype.itemsize} B, not the Body "
+                        f"({BODY_DTYPE.itemsize} B) or OctreeNode ({NODE_DTYPE.itemsize} B) ABI; "
+                        "use .astype(BODY_DTYPE)")
     return ctypes.c_void_p(a.ctypes.data)

@@ -91,6 +91,15 @@ int csgd_interactions(csgd_t *d, int64_t *total);
 /* Alive bodies (mass > 0 or NaN, as the reference's mass <= 0 test). Blocks. */
 int csgd_alive_count(csgd_t *d, int *count);
 
+/* FP64 diagnostics on the current bodies: direct-sum accelerations of the
+   ns bodies in host_idx (host_out: 3*ns doubles), and KE / softened PE. Block. */
+int csgd_direct_forces(csgd_t *d, const int *host_idx, int ns, double G, double softening,
+                       double *host_out);
+int csgd_energy(csgd_t *d, double G, double softening, double *ke, double *pe);
+
+/* Kernels launched on this state so far. */
+unsigned long long csgd_launch_count(const csgd_t *d);
+
 /* Waits for the stream; returns CSG_OK or the first error (CUDA or device). */
 int csgd_sync(csgd_t *d);
 const char *csgd_error_string(int code);

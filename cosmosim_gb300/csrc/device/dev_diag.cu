@@ -1,0 +1,280 @@
+// dev_diag.cu — FP64 diagnostics and pipe-peak probes.
+//
+// Direct-sum accelerations of a body sample over all bodies (the formula of
+// the reference's test helper, tests/test_physics.c:54-71) and the total
+// energy KE + softened PE (tests/test_physics.c:34-52), both in FP64. The
+// j range is split over blocks; each block writes its partial sums and a
+// second kernel adds them in a fixed order, so results are deterministic.
+//
+// The probes time long independent FMA chains (8 per thread) and report the
+// FP32 and FP64 CUDA-core throughput of this GPU: the denominators for the
+// walk kernels, which are bound by those pipes, not by tensor cores or HBM.
+#include "dev_internal.cuh"
+
+namespace {
+
+constexpr int DT = 256;       // threads per block
+constexpr int JCHUNKS = 64;   // j-range splits for the direct sum
+
+__global__ void __launch_bounds__(DT) k_direct(const double *__restrict__ x,
+                                               const double *__restrict__ y,
+                                               const double *__restrict__ z,
+                                               const double *__restrict__ m, int n,
+                                               const int *__restrict__ idx, int ns, double G,
+                                               double eps2, double *__restrict__ part)
+{
+    __shared__ double sx[DT], sy[DT], sz[DT], sm[DT];
+    const int k = blockIdx.x * DT + threadIdx.x;
+    const int chunk = blockIdx.y;
+    const int per = (n + JCHUNKS - 1) / JCHUNKS;
+    const int j0 = chunk * per, j1 = min(n, j0 + per);
+    const int i = (k < ns) ? idx[k] : -1;
+    const double xi = (i >= 0) ? x[i] : 0.0, yi = (i >= 0) ? y[i] : 0.0, zi = (i >= 0) ? z[i] : 0.0;
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    for (int t = j0; t < j1; t += DT) {
+        const int j = t + threadIdx.x;
+        __syncthreads();
+        if (j < j1) {
+            sx[threadIdx.x] = x[j];
+            sy[threadIdx.x] = y[j];
+            sz[threadIdx.x] = z[j];
+            sm[threadIdx.x] = (m[j] <= 0.0) ? 0.0 : m[j];
+        }
+        __syncthreads();
+        const int cnt = min(DT, j1 - t);
+        if (i >= 0) {
+            for (int q = 0; q < cnt; q++) {
+                if (t + q == i)
+                    continue;
+                double dx = sx[q] - xi, dy = sy[q] - yi, dz = sz[q] - zi;
+                double r2 = dx * dx + dy * dy + dz * dz + eps2;
+                double inv = 1.0 / (r2 * sqrt(r2));
+                double f = G * sm[q] * inv;
+                ax += f * dx;
+                ay += f * dy;
+                az += f * dz;
+            }
+        }
+    }
+    if (k < ns) {
+        double *p = part + ((size_t)chunk * ns + k) * 3;
+        p[0] = ax;
+        p[1] = ay;
+        p[2] = az;
+    }
+}
+
+__global__ void k_direct_sum(const double *__restrict__ part, int ns, double *__restrict__ out)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ns)
+        return;
+    double a[3] = {0.0, 0.0, 0.0};
+    for (int c = 0; c < JCHUNKS; c++)
+        for (int d = 0; d < 3; d++)
+            a[d] += part[((size_t)c * ns + k) * 3 + d];
+    for (int d = 0; d < 3; d++)
+        out[3 * (size_t)k + d] = a[d];
+}
+
+// Potential energy: row i against columns j > i, rows split over blocks;
+// each thread writes its row sum, reduced afterwards.
+__global__ void __launch_bounds__(DT) k_potential_rows(const double *__restrict__ x,
+                                                       const double *__restrict__ y,
+                                                       const double *__restrict__ z,
+                                                       const double *__restrict__ m, int n,
+                                                       double G, double eps2,
+                                                       double *__restrict__ row)
+{
+    __shared__ double sx[DT], sy[DT], sz[DT], sm[DT];
+    const int i = blockIdx.x * DT + threadIdx.x;
+    const double xi = (i < n) ? x[i] : 0.0, yi = (i < n) ? y[i] : 0.0, zi = (i < n) ? z[i] : 0.0;
+    const double mi = (i < n && m[i] > 0.0) ? m[i] : 0.0;
+    double pe = 0.0;
+    const int jstart = blockIdx.x * DT; // columns from the block's first row
+    for (int t = jstart; t < n; t += DT) {
+        const int j = t + threadIdx.x;
+        __syncthreads();
+        if (j < n) {
+            sx[threadIdx.x] = x[j];
+            sy[threadIdx.x] = y[j];
+            sz[threadIdx.x] = z[j];
+            sm[threadIdx.x] = (m[j] > 0.0) ? m[j] : 0.0;
+        }
+        __syncthreads();
+        const int cnt = min(DT, n - t);
+        if (i < n) {
+            for (int q = 0; q < cnt; q++) {
+                if (t + q <= i)
+                    continue;
+                double dx = sx[q] - xi, dy = sy[q] - yi, dz = sz[q] - zi;
+                double r = sqrt(dx * dx + dy * dy + dz * dz + eps2);
+                pe -= G * mi * sm[q] / r;
+            }
+        }
+    }
+    if (i < n)
+        row[i] = pe;
+}
+
+__global__ void k_energy_reduce(const double *__restrict__ row, const double *__restrict__ m,
+                                const double *__restrict__ vx, const double *__restrict__ vy,
+                                const double *__restrict__ vz, int n, double *__restrict__ out)
+{
+    // one block; fixed-order tree reduction in shared memory
+    __shared__ double ske[1024], spe[1024];
+    double ke = 0.0, pe = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double mm = (m[i] > 0.0) ? m[i] : 0.0;
+        ke += 0.5 * mm * (vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i]);
+        pe += row[i];
+    }
+    ske[threadIdx.x] = ke;
+    spe[threadIdx.x] = pe;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            ske[threadIdx.x] += ske[threadIdx.x + s];
+            spe[threadIdx.x] += spe[threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = ske[0];
+        out[1] = spe[0];
+    }
+}
+
+template <typename T>
+__global__ void k_fma_probe(T *out, int iters, T a, T b)
+{
+    T x0 = (T)threadIdx.x * (T)1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+    T x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; i++) {
+        x0 = x0 * a + b;
+        x1 = x1 * a + b;
+        x2 = x2 * a + b;
+        x3 = x3 * a + b;
+        x4 = x4 * a + b;
+        x5 = x5 * a + b;
+        x6 = x6 * a + b;
+        x7 = x7 * a + b;
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+} // namespace
+
+extern "C" int csgd_direct_forces(csgd_t *d, const int *host_idx, int ns, double G,
+                                  double softening, double *host_out)
+{
+    if (ns <= 0)
+        return CSG_OK;
+    if (ns > d->n) {
+        csgd_set_err(d, CSG_ERR_BAD_ARG);
+        return CSG_ERR_BAD_ARG;
+    }
+    int *didx = nullptr;
+    double *part = nullptr, *out = nullptr;
+    cudaError_t e = cudaMalloc((void **)&didx, sizeof(int) * (size_t)ns);
+    if (e == cudaSuccess)
+        e = cudaMalloc((void **)&part, sizeof(double) * 3 * (size_t)ns * JCHUNKS);
+    if (e == cudaSuccess)
+        e = cudaMalloc((void **)&out, sizeof(double) * 3 * (size_t)ns);
+    int rc = CSG_OK;
+    if (e == cudaSuccess) {
+        cudaMemcpyAsync(didx, host_idx, sizeof(int) * (size_t)ns, cudaMemcpyHostToDevice, d->stream);
+        dim3 grid((ns + DT - 1) / DT, JCHUNKS);
+        { k_direct<<<grid, DT, 0, d->stream>>>(d->x, d->y, d->z, d->m, d->n, didx, ns, G, softening * softening, part); d->launches++; }
+        { k_direct_sum<<<csgd_grid(ns, 256), 256, 0, d->stream>>>(part, ns, out); d->launches++; }
+        cudaMemcpyAsync(host_out, out, sizeof(double) * 3 * (size_t)ns, cudaMemcpyDeviceToHost, d->stream);
+        rc = csgd_sync(d);
+    } else {
+        cudaGetLastError();
+        rc = CSG_ERR_NOMEM;
+    }
+    cudaFree(didx);
+    cudaFree(part);
+    cudaFree(out);
+    return rc;
+}
+
+extern "C" int csgd_energy(csgd_t *d, double G, double softening, double *ke, double *pe)
+{
+    const int n = d->n;
+    double *row = nullptr, *out = nullptr;
+    cudaError_t e = cudaMalloc((void **)&row, sizeof(double) * (size_t)(n > 0 ? n : 1));
+    if (e == cudaSuccess)
+        e = cudaMalloc((void **)&out, 2 * sizeof(double));
+    int rc = CSG_OK;
+    if (e == cudaSuccess && n > 0) {
+        { k_potential_rows<<<csgd_grid(n, DT), DT, 0, d->stream>>>(d->x, d->y, d->z, d->m, n, G, softening * softening, row); d->launches++; }
+        { k_energy_reduce<<<1, 1024, 0, d->stream>>>(row, d->m, d->vx, d->vy, d->vz, n, out); d->launches++; }
+        double h[2] = {0.0, 0.0};
+        cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, d->stream);
+        rc = csgd_sync(d);
+        *ke = h[0];
+        *pe = h[1];
+    } else if (e != cudaSuccess) {
+        cudaGetLastError();
+        rc = CSG_ERR_NOMEM;
+    } else {
+        *ke = *pe = 0.0;
+    }
+    cudaFree(row);
+    cudaFree(out);
+    return rc;
+}
+
+// FP32 and FP64 FMA throughput (TFLOP/s, 2 flop per FMA) of the current device.
+extern "C" CSG_EXPORT int csg_measure_fp_peaks(double *fp32_tflops, double *fp64_tflops)
+{
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return CSG_ERR_NO_DEVICE;
+    }
+    const int blocks = sms * 8, threads = 256;
+    const size_t nthr = (size_t)blocks * threads;
+    float *o32 = nullptr;
+    double *o64 = nullptr;
+    cudaStream_t s;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
+        return CSG_ERR_CUDA;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int rc = CSG_OK;
+    if (cudaMalloc((void **)&o32, nthr * sizeof(float)) != cudaSuccess ||
+        cudaMalloc((void **)&o64, nthr * sizeof(double)) != cudaSuccess) {
+        rc = CSG_ERR_NOMEM;
+    } else {
+        const int it32 = 8192, it64 = 512;
+        float best32 = 1e30f, best64 = 1e30f, ms = 0.f;
+        for (int rep = 0; rep < 3; rep++) {
+            cudaEventRecord(e0, s);
+            k_fma_probe<float><<<blocks, threads, 0, s>>>(o32, it32, 0.999999f, 1e-7f);
+            cudaEventRecord(e1, s);
+            cudaEventSynchronize(e1);
+            cudaEventElapsedTime(&ms, e0, e1);
+            best32 = ms < best32 ? ms : best32;
+            cudaEventRecord(e0, s);
+            k_fma_probe<double><<<blocks, threads, 0, s>>>(o64, it64, 0.999999, 1e-7);
+            cudaEventRecord(e1, s);
+            cudaEventSynchronize(e1);
+            cudaEventElapsedTime(&ms, e0, e1);
+            best64 = ms < best64 ? ms : best64;
+        }
+        *fp32_tflops = 2.0 * 8.0 * it32 * (double)nthr / (best32 * 1e-3) / 1e12;
+        *fp64_tflops = 2.0 * 8.0 * it64 * (double)nthr / (best64 * 1e-3) / 1e12;
+        if (cudaGetLastError() != cudaSuccess)
+            rc = CSG_ERR_CUDA;
+    }
+    cudaFree(o32);
+    cudaFree(o64);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(s);
+    return rc;
+}

@@ -74,6 +74,7 @@ struct csgd {
     int node_cap; // node capacity (8*cap + 64)
     int stats;
     int host_err; // first error seen on the host side (launch, allocation)
+    unsigned long long launches; // kernels launched on this state (measurement)
 
     // bodies, caller index order
     double *x, *y, *z, *vx, *vy, *vz, *ax, *ay, *az, *m;
@@ -111,7 +112,8 @@ struct csgd {
     DevScalars *sc;      // device
     DevScalars *sc_host; // pinned mirror
     int geometry_valid;
-    int imported; // the tree came from a caller pool (no sorted order)
+    int imported;  // the tree came from a caller pool (no sorted order)
+    int gas_valid; // d->gas / n_gas match the current tree
 };
 
 // ---- helpers shared by the .cu files ----

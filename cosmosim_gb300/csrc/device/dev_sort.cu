@@ -181,7 +181,7 @@ int csg_scan_exclusive(csgd_t *d, const int *in, int *out, int n, const int *cou
         csgd_set_err(d, CSG_ERR_NOMEM);
         return CSG_ERR_NOMEM;
     }
-    k_scan_tile<<<nb, SCAN_THREADS, 0, d->stream>>>(in, out, n, count_limit, sums);
+    { k_scan_tile<<<nb, SCAN_THREADS, 0, d->stream>>>(in, out, n, count_limit, sums); d->launches++; }
     if (nb > 1) {
         // scan the block sums (exclusive, total at sums_out[nb]) and add back
         int *sums_out = sums + nb + 1;
@@ -195,10 +195,10 @@ int csg_scan_exclusive(csgd_t *d, const int *in, int *out, int n, const int *cou
         d->scan_tmp_cap = saved_cap;
         if (rc)
             return rc;
-        k_scan_add<<<csgd_grid(n, 256), 256, 0, d->stream>>>(out, n, sums_out);
-        k_scan_total<<<1, 1, 0, d->stream>>>(out, n, sums_out + nb);
+        { k_scan_add<<<csgd_grid(n, 256), 256, 0, d->stream>>>(out, n, sums_out); d->launches++; }
+        { k_scan_total<<<1, 1, 0, d->stream>>>(out, n, sums_out + nb); d->launches++; }
     } else {
-        k_scan_total<<<1, 1, 0, d->stream>>>(out, n, sums);
+        { k_scan_total<<<1, 1, 0, d->stream>>>(out, n, sums); d->launches++; }
     }
     return csgd_check(d, cudaGetLastError());
 }
@@ -221,12 +221,12 @@ int csg_radix_sort(csgd_t *d, unsigned long long *key, int *val, unsigned long l
     const int passes = (bits + 7) / 8;
     for (int p = 0; p < passes; p++) {
         const int shift = 8 * p;
-        k_radix_hist<<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, n, shift, hist, nblocks);
+        { k_radix_hist<<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, n, shift, hist, nblocks); d->launches++; }
         int rc = csg_scan_exclusive(d, (const int *)hist, offs, hn, nullptr);
         if (rc)
             return rc;
-        k_radix_scatter<<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, offs,
-                                                                  nblocks);
+        { k_radix_scatter<<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, offs,
+                                                                  nblocks); d->launches++; }
         unsigned long long *tk = ki;
         ki = ko;
         ko = tk;

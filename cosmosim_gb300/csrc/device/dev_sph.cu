@@ -74,7 +74,7 @@ __device__ __forceinline__ void neighbour_walk(const SphArgs &a, bool valid, dou
                                                Visit visit)
 {
     const int lane = threadIdx.x & 31;
-    const int nn = min(a.sc->n_nodes, a.node_cap);
+    const int nn = (a.sc->n_nodes > a.node_cap) ? 0 : a.sc->n_nodes;
     int skip = valid ? 0 : INT_MAX;
     int found = 0;
     int cur = 0, wbase = INT_MIN / 2;
@@ -259,7 +259,7 @@ __global__ void k_gas_scatter(DevScalars *sc, const int *__restrict__ perm,
 __global__ void k_find_one(SphArgs a, double cx, double cy, double cz, double radius, int cap,
                            int *__restrict__ buf, int *__restrict__ count)
 {
-    const int nn = min(a.sc->n_nodes, a.node_cap);
+    const int nn = (a.sc->n_nodes > a.node_cap) ? 0 : a.sc->n_nodes;
     const double r2 = radius * radius;
     int c = 0, cur = 0;
     while (cur < nn && c < cap) {
@@ -341,21 +341,24 @@ __global__ void k_gas_scatter_idx(DevScalars *sc, int n, const int *__restrict__
 
 int gas_list(csgd_t *d)
 {
+    if (d->gas_valid)
+        return CSG_OK;
     const int n = d->n;
     const int g = csgd_grid(n, 256);
     if (!d->imported) {
-        k_gas_flags<<<g, 256, 0, d->stream>>>(d->sc, d->perm, d->type, d->cnt);
+        { k_gas_flags<<<g, 256, 0, d->stream>>>(d->sc, d->perm, d->type, d->cnt); d->launches++; }
         int rc = csg_scan_exclusive(d, d->cnt, d->base, n, &d->sc->n_alive);
         if (rc)
             return rc;
-        k_gas_scatter<<<g, 256, 0, d->stream>>>(d->sc, d->perm, d->cnt, d->base, d->gas);
+        { k_gas_scatter<<<g, 256, 0, d->stream>>>(d->sc, d->perm, d->cnt, d->base, d->gas); d->launches++; }
     } else {
-        k_gas_flags_idx<<<g, 256, 0, d->stream>>>(n, d->m, d->type, d->cnt);
+        { k_gas_flags_idx<<<g, 256, 0, d->stream>>>(n, d->m, d->type, d->cnt); d->launches++; }
         int rc = csg_scan_exclusive(d, d->cnt, d->base, n, nullptr);
         if (rc)
             return rc;
-        k_gas_scatter_idx<<<g, 256, 0, d->stream>>>(d->sc, n, d->cnt, d->base, d->gas);
+        { k_gas_scatter_idx<<<g, 256, 0, d->stream>>>(d->sc, n, d->cnt, d->base, d->gas); d->launches++; }
     }
+    d->gas_valid = 1;
     return csgd_check(d, cudaGetLastError());
 }
 
@@ -373,7 +376,7 @@ extern "C" int csgd_sph_density(csgd_t *d)
     if (rc)
         return rc;
     SphArgs a = make_args(d);
-    k_sph_density<<<csgd_grid(d->n, SPH_THREADS), SPH_THREADS, 0, d->stream>>>(a);
+    { k_sph_density<<<csgd_grid(d->n, SPH_THREADS), SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
     return csgd_check(d, cudaGetLastError());
 }
 
@@ -385,8 +388,11 @@ extern "C" int csgd_sph_forces(csgd_t *d)
         csgd_set_err(d, CSG_ERR_BAD_ARG);
         return CSG_ERR_BAD_ARG;
     }
+    int rc = gas_list(d);
+    if (rc)
+        return rc;
     SphArgs a = make_args(d);
-    k_sph_forces<<<csgd_grid(d->n, SPH_THREADS), SPH_THREADS, 0, d->stream>>>(a);
+    { k_sph_forces<<<csgd_grid(d->n, SPH_THREADS), SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
     return csgd_check(d, cudaGetLastError());
 }
 
@@ -407,7 +413,7 @@ extern "C" int csgd_find_neighbors(csgd_t *d, double cx, double cy, double cz, d
     int *dbuf = d->rank;
     int *dcount = d->ord_id;
     SphArgs a = make_args(d);
-    k_find_one<<<1, 1, 0, d->stream>>>(a, cx, cy, cz, radius, cap, dbuf, dcount);
+    { k_find_one<<<1, 1, 0, d->stream>>>(a, cx, cy, cz, radius, cap, dbuf, dcount); d->launches++; }
     int c = 0;
     cudaMemcpyAsync(&c, dcount, sizeof(int), cudaMemcpyDeviceToHost, d->stream);
     int rc = csgd_sync(d);

@@ -359,10 +359,11 @@ extern "C" int csgd_upload_bodies(csgd_t *d, const Body *host, int n)
     if (n == 0)
         return CSG_OK;
     cudaMemcpyAsync(d->aos, host, sizeof(Body) * (size_t)n, cudaMemcpyHostToDevice, d->stream);
-    k_unpack<<<csgd_grid(n, 256), 256, 0, d->stream>>>(d->aos, n, d->x, d->y, d->z, d->vx, d->vy,
+    { k_unpack<<<csgd_grid(n, 256), 256, 0, d->stream>>>(d->aos, n, d->x, d->y, d->z, d->vx, d->vy,
                                                         d->vz, d->ax, d->ay, d->az, d->m, d->type,
-                                                        d->rho, d->P, d->u, d->h);
+                                                        d->rho, d->P, d->u, d->h); d->launches++; }
     d->geometry_valid = 0;
+    d->gas_valid = 0;
     return csgd_check(d, cudaGetLastError());
 }
 
@@ -374,9 +375,9 @@ extern "C" int csgd_download_bodies(csgd_t *d, Body *host, int n)
     }
     if (n == 0)
         return CSG_OK;
-    k_pack<<<csgd_grid(n, 256), 256, 0, d->stream>>>(d->aos, n, d->x, d->y, d->z, d->vx, d->vy,
+    { k_pack<<<csgd_grid(n, 256), 256, 0, d->stream>>>(d->aos, n, d->x, d->y, d->z, d->vx, d->vy,
                                                       d->vz, d->ax, d->ay, d->az, d->rho, d->P,
-                                                      d->u, d->h);
+                                                      d->u, d->h); d->launches++; }
     cudaMemcpyAsync(host, d->aos, sizeof(Body) * (size_t)n, cudaMemcpyDeviceToHost, d->stream);
     return csgd_check(d, cudaGetLastError());
 }
@@ -387,9 +388,9 @@ extern "C" int csgd_kick_drift(csgd_t *d, double dt)
 {
     if (d->n <= 0)
         return CSG_OK;
-    k_kick_drift<<<csgd_grid(d->n, 256), 256, 0, d->stream>>>(d->n, dt, d->m, d->x, d->y, d->z,
+    { k_kick_drift<<<csgd_grid(d->n, 256), 256, 0, d->stream>>>(d->n, dt, d->m, d->x, d->y, d->z,
                                                                d->vx, d->vy, d->vz, d->ax, d->ay,
-                                                               d->az);
+                                                               d->az); d->launches++; }
     return csgd_check(d, cudaGetLastError());
 }
 
@@ -397,8 +398,8 @@ extern "C" int csgd_kick(csgd_t *d, double dt)
 {
     if (d->n <= 0)
         return CSG_OK;
-    k_kick<<<csgd_grid(d->n, 256), 256, 0, d->stream>>>(d->n, dt, d->m, d->vx, d->vy, d->vz,
-                                                         d->ax, d->ay, d->az);
+    { k_kick<<<csgd_grid(d->n, 256), 256, 0, d->stream>>>(d->n, dt, d->m, d->vx, d->vy, d->vz,
+                                                         d->ax, d->ay, d->az); d->launches++; }
     return csgd_check(d, cudaGetLastError());
 }
 
@@ -406,8 +407,8 @@ extern "C" int csgd_sph_cooling(csgd_t *d, double dt)
 {
     if (d->n <= 0)
         return CSG_OK;
-    k_cooling<<<csgd_grid(d->n, 256), 256, 0, d->stream>>>(d->n, dt, d->m, d->type, d->rho, d->u,
-                                                            d->P);
+    { k_cooling<<<csgd_grid(d->n, 256), 256, 0, d->stream>>>(d->n, dt, d->m, d->type, d->rho, d->u,
+                                                            d->P); d->launches++; }
     return csgd_check(d, cudaGetLastError());
 }
 
@@ -482,9 +483,11 @@ extern "C" int csgd_alive_count(csgd_t *d, int *count)
         int g = csgd_grid(d->n, 256);
         if (g > 152 * 8)
             g = 152 * 8;
-        k_alive_count<<<g, 256, 0, d->stream>>>(d->n, d->m, d->sc);
+        { k_alive_count<<<g, 256, 0, d->stream>>>(d->n, d->m, d->sc); d->launches++; }
     }
     int rc = csgd_sync(d);
     *count = d->sc_host->alive_count;
     return rc;
 }
+
+extern "C" unsigned long long csgd_launch_count(const csgd_t *d) { return d->launches; }

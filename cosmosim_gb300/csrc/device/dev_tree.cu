@@ -480,7 +480,7 @@ __global__ void k_nodes(csgd_t dd, DevScalars *sc, const unsigned long long *__r
         write_cell(dd, sc, id, parent, L, p, hi - p + 1, base[hi + 1], -1);
     }
     if (P < CSG_MAX_LEVEL) {
-        int L = max(P, Q) + 1;
+        int L = min(max(P, Q) + 1, CSG_MAX_LEVEL); // bodies equal to depth 64 share a leaf
         int hi = (Q == CSG_MAX_LEVEL) ? search_hi(key, ext, na, p, CSG_MAX_LEVEL) : p;
         int parent = parent_id(key, ext, lcp, base, p, P, L, id);
         write_cell(dd, sc, id, parent, L, p, hi - p + 1, id + 1, perm[p]);
@@ -494,7 +494,7 @@ __global__ void k_link(csgd_t dd, DevScalars *sc, const unsigned long long *__re
     if (id >= min(sc->n_nodes, dd.node_cap))
         return;
     NodeLink l = dd.link[id];
-    if (l.parent < 0)
+    if (l.parent < 0 || l.parent >= dd.node_cap || sc->n_nodes > dd.node_cap)
         return;
     int dg = digit_at(key, ext, l.first, l.level - 1);
     dd.child[8 * (size_t)l.parent + dg] = id;
@@ -508,7 +508,7 @@ __global__ void k_moments(csgd_t dd, DevScalars *sc, const double *__restrict__ 
                           const double *__restrict__ m, const int *__restrict__ perm)
 {
     const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= min(sc->n_nodes, dd.node_cap))
+    if (id >= min(sc->n_nodes, dd.node_cap) || sc->n_nodes > dd.node_cap)
         return;
     if (dd.w64[id].body < 0)
         return;
@@ -556,8 +556,8 @@ __global__ void k_moments(csgd_t dd, DevScalars *sc, const double *__restrict__ 
         dd.w32[node] = v;
         dd.minidx[node] = mi;
         int parent = dd.link[node].parent;
-        if (parent < 0)
-            break;
+        if (parent < 0 || parent >= node)
+            break; // preorder: a parent always precedes its children
         __threadfence();
         int t = atomicAdd(&dd.ticket[parent], 1);
         if (t != __ldcg(&dd.nchild[parent]) - 1)
@@ -600,7 +600,7 @@ __global__ void k_geometry(csgd_t dd, DevScalars *sc, const unsigned long long *
                            const unsigned long long *__restrict__ ext)
 {
     const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= min(sc->n_nodes, dd.node_cap))
+    if (id >= min(sc->n_nodes, dd.node_cap) || sc->n_nodes > dd.node_cap)
         return;
     NodeLink l = dd.link[id];
     double cx = sc->c0[0], cy = sc->c0[1], cz = sc->c0[2], hs = sc->hs0;
@@ -748,8 +748,8 @@ __global__ void k_imp_write(csgd_t dd, DevScalars *sc, int nn, int root,
                             const int *__restrict__ size)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nn)
-        return;
+    if (i >= nn || sc->err != 0)
+        return; // links or sizes already found the pool is not a tree
     // preorder id = sum over the path of (1 + sizes of earlier siblings)
     int id = 0, depth = 0, node = i;
     while (node != root) {
@@ -771,7 +771,7 @@ __global__ void k_imp_write(csgd_t dd, DevScalars *sc, int nn, int root,
     }
     if (i == root)
         sc->n_nodes = size[root];
-    if (id >= dd.node_cap) {
+    if (id < 0 || id >= dd.node_cap) {
         dev_fail(sc, CSG_ERR_NODE_CAPACITY);
         return;
     }
@@ -808,37 +808,48 @@ __global__ void k_imp_write(csgd_t dd, DevScalars *sc, int nn, int root,
 
 // ---- host side -------------------------------------------------------------
 
+// Steps 1-3: root cube, keys, sorted order of the alive bodies (n_alive).
+static int order_bodies(csgd_t *d)
+{
+    const int n = d->n;
+    cudaStream_t s = d->stream;
+    DevScalars *sc = d->sc;
+    const int B = 256;
+    { k_reset<<<1, 1, 0, s>>>(sc); d->launches++; }
+    int gb = min(csgd_grid(n, B), 152 * 8);
+    { k_bbox<<<gb > 0 ? gb : 1, B, 0, s>>>(d->x, d->y, d->z, d->m, n, sc); d->launches++; }
+    { k_root<<<1, 1, 0, s>>>(sc); d->launches++; }
+    if (n > 0)
+        { k_keys<<<csgd_grid(n, B), B, 0, s>>>(d->x, d->y, d->z, d->m, n, sc, d->key, d->perm); d->launches++; }
+    return csg_radix_sort(d, d->key, d->perm, d->key_alt, d->perm_alt, n, 64);
+}
+
 extern "C" int csgd_build_tree(csgd_t *d, int geometry)
 {
     const int n = d->n;
     cudaStream_t s = d->stream;
     DevScalars *sc = d->sc;
     const int B = 256;
-    k_reset<<<1, 1, 0, s>>>(sc);
-    int gb = min(csgd_grid(n, B), 152 * 8);
-    k_bbox<<<gb > 0 ? gb : 1, B, 0, s>>>(d->x, d->y, d->z, d->m, n, sc);
-    k_root<<<1, 1, 0, s>>>(sc);
-    if (n > 0)
-        k_keys<<<csgd_grid(n, B), B, 0, s>>>(d->x, d->y, d->z, d->m, n, sc, d->key, d->perm);
-    int rc = csg_radix_sort(d, d->key, d->perm, d->key_alt, d->perm_alt, n, 64);
+    int rc = order_bodies(d);
     if (rc)
         return rc;
     const int g = csgd_grid(n > 0 ? n : 1, B);
-    k_deep_mark<<<g, B, 0, s>>>(d->x, d->y, d->z, sc, d->key, d->perm, d->ext);
-    k_deep_sort<<<g, B, 0, s>>>(sc, d->key, d->perm, d->ext);
-    k_count<<<g, B, 0, s>>>(sc, d->key, d->ext, d->lcp, d->cnt);
+    { k_deep_mark<<<g, B, 0, s>>>(d->x, d->y, d->z, sc, d->key, d->perm, d->ext); d->launches++; }
+    { k_deep_sort<<<g, B, 0, s>>>(sc, d->key, d->perm, d->ext); d->launches++; }
+    { k_count<<<g, B, 0, s>>>(sc, d->key, d->ext, d->lcp, d->cnt); d->launches++; }
     rc = csg_scan_exclusive(d, d->cnt, d->base, n, &sc->n_alive);
     if (rc)
         return rc;
-    k_nodes<<<g, B, 0, s>>>(*d, sc, d->key, d->ext, d->lcp, d->base, d->perm);
+    { k_nodes<<<g, B, 0, s>>>(*d, sc, d->key, d->ext, d->lcp, d->base, d->perm); d->launches++; }
     const int gn = csgd_grid(d->node_cap, B);
     // nodes beyond n_nodes exit at once; the grid covers the capacity
-    k_link<<<gn, B, 0, s>>>(*d, sc, d->key, d->ext);
-    k_moments<<<gn, B, 0, s>>>(*d, sc, d->x, d->y, d->z, d->m, d->perm);
+    { k_link<<<gn, B, 0, s>>>(*d, sc, d->key, d->ext); d->launches++; }
+    { k_moments<<<gn, B, 0, s>>>(*d, sc, d->x, d->y, d->z, d->m, d->perm); d->launches++; }
     d->geometry_valid = 0;
     d->imported = 0;
+    d->gas_valid = 0;
     if (geometry) {
-        k_geometry<<<gn, B, 0, s>>>(*d, sc, d->key, d->ext);
+        { k_geometry<<<gn, B, 0, s>>>(*d, sc, d->key, d->ext); d->launches++; }
         d->geometry_valid = 1;
     }
     return csgd_check(d, cudaGetLastError());
@@ -851,7 +862,7 @@ extern "C" int csgd_export_pool(csgd_t *d, OctreeNode *pool, int capacity, int *
     const int B = 256;
     if (!d->geometry_valid) {
         const int gn = csgd_grid(d->node_cap, B);
-        k_geometry<<<gn, B, 0, s>>>(*d, sc, d->key, d->ext);
+        { k_geometry<<<gn, B, 0, s>>>(*d, sc, d->key, d->ext); d->launches++; }
         d->geometry_valid = 1;
     }
     int rc = csgd_node_count(d, pool_size_out);
@@ -863,12 +874,12 @@ extern "C" int csgd_export_pool(csgd_t *d, OctreeNode *pool, int capacity, int *
         return CSG_ERR_NODE_CAPACITY;
     }
     const int g = csgd_grid(nn, B);
-    k_order_keys<<<g, B, 0, s>>>(*d, sc);
+    { k_order_keys<<<g, B, 0, s>>>(*d, sc); d->launches++; }
     rc = csg_radix_sort(d, d->ord_key, d->ord_id, d->ord_key_alt, d->ord_id_alt, nn, 40);
     if (rc)
         return rc;
-    k_rank<<<g, B, 0, s>>>(*d, sc);
-    k_export<<<g, B, 0, s>>>(*d, sc);
+    { k_rank<<<g, B, 0, s>>>(*d, sc); d->launches++; }
+    { k_export<<<g, B, 0, s>>>(*d, sc); d->launches++; }
     cudaMemcpyAsync(pool, d->pool, sizeof(OctreeNode) * (size_t)nn, cudaMemcpyDeviceToHost, s);
     return csgd_sync(d);
 }
@@ -882,16 +893,22 @@ extern "C" int csgd_import_pool(csgd_t *d, const OctreeNode *pool, int n_nodes, 
     cudaStream_t s = d->stream;
     DevScalars *sc = d->sc;
     const int B = 256;
+    // The walks take bodies in key order (neighbours share a warp): order the
+    // alive bodies as a build would, then replace the cells by the pool's.
+    int rc = order_bodies(d);
+    if (rc)
+        return rc;
     // scratch: par, slot, size in the (unused here) sort/order buffers
     int *par = d->ord_id, *slot = d->ord_id_alt, *size = d->rank;
     cudaMemcpyAsync(d->pool, pool, sizeof(OctreeNode) * (size_t)n_nodes, cudaMemcpyHostToDevice,
                     s);
     cudaMemsetAsync(par, 0xff, sizeof(int) * (size_t)n_nodes, s);
     const int g = csgd_grid(n_nodes, B);
-    k_imp_links<<<g, B, 0, s>>>(*d, sc, n_nodes, root, par, slot);
-    k_imp_sizes<<<g, B, 0, s>>>(*d, sc, n_nodes, par, size);
-    k_imp_write<<<g, B, 0, s>>>(*d, sc, n_nodes, root, par, slot, size);
+    { k_imp_links<<<g, B, 0, s>>>(*d, sc, n_nodes, root, par, slot); d->launches++; }
+    { k_imp_sizes<<<g, B, 0, s>>>(*d, sc, n_nodes, par, size); d->launches++; }
+    { k_imp_write<<<g, B, 0, s>>>(*d, sc, n_nodes, root, par, slot, size); d->launches++; }
     d->geometry_valid = 1;
     d->imported = 1;
+    d->gas_valid = 0;
     return csgd_check(d, cudaGetLastError());
 }

@@ -81,7 +81,9 @@ __global__ void __launch_bounds__(WALK_THREADS) k_walk64(WalkArgs a)
     const long long warp0 = p - lane;
     if (warp0 >= n_alive)
         return;
-    const int nn = min(a.sc->n_nodes, a.node_cap);
+    if (a.sc->n_nodes > a.node_cap || a.sc->n_nodes < 1)
+        return; // no valid tree (capacity error already recorded)
+    const int nn = a.sc->n_nodes;
     const bool valid = p < n_alive;
     const int me = valid ? a.perm[p] : -1;
     const double px = valid ? a.x[me] : 0.0, py = valid ? a.y[me] : 0.0,
@@ -184,7 +186,9 @@ __global__ void __launch_bounds__(WALK_THREADS) k_walk32(WalkArgs a)
     const long long warp0 = p - lane;
     if (warp0 >= n_alive)
         return;
-    const int nn = min(a.sc->n_nodes, a.node_cap);
+    if (a.sc->n_nodes > a.node_cap || a.sc->n_nodes < 1)
+        return; // no valid tree (capacity error already recorded)
+    const int nn = a.sc->n_nodes;
     const bool valid = p < n_alive;
     const int me = valid ? a.perm[p] : -1;
     const double px = valid ? a.x[me] : 0.0, py = valid ? a.y[me] : 0.0,
@@ -312,23 +316,23 @@ extern "C" int csgd_gravity_ex(csgd_t *d, const csgd_force_params *p, int exact)
     a.guard_rel = 0x1p-19f * (1.0f + a.theta2f);
     a.node_cap = d->node_cap;
     cudaStream_t s = d->stream;
-    k_zero_acc<<<csgd_grid(n, 256), 256, 0, s>>>(d->m, d->ax, d->ay, d->az, n);
+    { k_zero_acc<<<csgd_grid(n, 256), 256, 0, s>>>(d->m, d->ax, d->ay, d->az, n); d->launches++; }
     const int g = csgd_grid(n, WALK_THREADS);
     if (p->precision == CSG_PREC_FP32_MIXED && !exact) {
         if (d->stats)
-            k_walk32<true><<<g, WALK_THREADS, 0, s>>>(a);
+            { k_walk32<true><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
         else
-            k_walk32<false><<<g, WALK_THREADS, 0, s>>>(a);
+            { k_walk32<false><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
     } else if (exact) {
         if (d->stats)
-            k_walk64<true, true><<<g, WALK_THREADS, 0, s>>>(a);
+            { k_walk64<true, true><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
         else
-            k_walk64<true, false><<<g, WALK_THREADS, 0, s>>>(a);
+            { k_walk64<true, false><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
     } else {
         if (d->stats)
-            k_walk64<false, true><<<g, WALK_THREADS, 0, s>>>(a);
+            { k_walk64<false, true><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
         else
-            k_walk64<false, false><<<g, WALK_THREADS, 0, s>>>(a);
+            { k_walk64<false, false><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
     }
     return csgd_check(d, cudaGetLastError());
 }

@@ -429,3 +429,29 @@ CSG_EXPORT int cosmosim_set_precision(SimHandle handle, int precision)
         (precision == CSG_PREC_FP32_MIXED) ? CSG_PREC_FP32_MIXED : CSG_PREC_FP64;
     return set_err(s, CSG_OK);
 }
+
+CSG_EXPORT int cosmosim_direct_forces(SimHandle handle, const int *idx, int m, double *out)
+{
+    if (!handle || (m > 0 && (!idx || !out)) || m < 0)
+        return CSG_ERR_BAD_ARG;
+    SimState *s = (SimState *)handle;
+    for (int k = 0; k < m; k++)
+        if (idx[k] < 0 || idx[k] >= s->current_n)
+            return set_err(s, CSG_ERR_BAD_ARG);
+    return set_err(s, csgd_direct_forces(s->dev, idx, m, s->params.G, s->params.softening, out));
+}
+
+CSG_EXPORT int cosmosim_energy(SimHandle handle, double *kinetic, double *potential)
+{
+    if (!handle || !kinetic || !potential)
+        return CSG_ERR_BAD_ARG;
+    SimState *s = (SimState *)handle;
+    return set_err(s, csgd_energy(s->dev, s->params.G, s->params.softening, kinetic, potential));
+}
+
+CSG_EXPORT int64_t cosmosim_launch_count(SimHandle handle)
+{
+    if (!handle)
+        return 0;
+    return (int64_t)csgd_launch_count(((SimState *)handle)->dev);
+}

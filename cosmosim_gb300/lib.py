@@ -68,6 +68,10 @@ _SIGS = {
     "csg_error_string": ([_i], ctypes.c_char_p),
     "csg_set_precision": ([_i], None),
     "csg_generate_ics": ([_i, _i, ctypes.c_uint64, _vp], _i),
+    "cosmosim_direct_forces": ([_vp, _vp, _i, _vp], _i),
+    "cosmosim_energy": ([_vp, ctypes.POINTER(_d), ctypes.POINTER(_d)], _i),
+    "cosmosim_launch_count": ([_vp], ctypes.c_int64),
+    "csg_measure_fp_peaks": ([ctypes.POINTER(_d), ctypes.POINTER(_d)], _i),
 }
 
 _lib = None
@@ -170,6 +174,15 @@ def sph_apply_cooling(bodies, dt):
     _check(lib, "sph_apply_cooling")
 
 
+def measure_fp_peaks():
+    """(FP32, FP64) FMA throughput of the current GPU in TFLOP/s."""
+    a, b = ctypes.c_double(0), ctypes.c_double(0)
+    rc = load().csg_measure_fp_peaks(ctypes.byref(a), ctypes.byref(b))
+    if rc:
+        raise CudaError(f"peak probe failed ({rc})")
+    return a.value, b.value
+
+
 def generate_ics(kind, n, seed):
     """Seeded initial conditions of benchmark configuration `kind` (0-4)."""
     lib = load()
@@ -266,6 +279,21 @@ class Sim:
         n = self.count
         buf = (ctypes.c_char * (n * BODY_DTYPE.itemsize)).from_address(p)
         return np.frombuffer(buf, dtype=BODY_DTYPE, count=n).copy()
+
+    def direct_forces(self, idx):
+        """FP64 direct-sum accelerations of bodies idx (m x 3)."""
+        idx = np.ascontiguousarray(idx, dtype=np.int32)
+        out = np.zeros((len(idx), 3))
+        self._rc(self.lib.cosmosim_direct_forces(self.h, ptr(idx), len(idx), ptr(out)), "direct")
+        return out
+
+    def energy(self):
+        ke, pe = ctypes.c_double(0), ctypes.c_double(0)
+        self._rc(self.lib.cosmosim_energy(self.h, ctypes.byref(ke), ctypes.byref(pe)), "energy")
+        return ke.value, pe.value
+
+    def launch_count(self):
+        return self.lib.cosmosim_launch_count(self.h)
 
     def close(self):
         if self.h:

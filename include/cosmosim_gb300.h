@@ -91,6 +91,21 @@ CSG_EXPORT int cosmosim_interactions(SimHandle handle, int64_t *total);
 CSG_EXPORT int cosmosim_node_count(SimHandle handle, int *n_nodes);
 CSG_EXPORT int cosmosim_set_precision(SimHandle handle, int precision);
 
+/* FP64 diagnostics on the handle's current bodies (blocking): direct-sum
+   accelerations of the m bodies listed in idx into out[3*m] (the formula of
+   the reference's test helper, tests/test_physics.c:54-71), and kinetic /
+   softened potential energy (tests/test_physics.c:34-52, O(n^2)). */
+CSG_EXPORT int cosmosim_direct_forces(SimHandle handle, const int *idx, int m, double *out);
+CSG_EXPORT int cosmosim_energy(SimHandle handle, double *kinetic, double *potential);
+
+/* Kernels this handle has launched so far (for launch accounting). */
+CSG_EXPORT int64_t cosmosim_launch_count(SimHandle handle);
+
+/* FP32 and FP64 FMA throughput of the current GPU in TFLOP/s, measured by
+   timing independent FMA chains: the pipe peaks the gravity walks are
+   bound by. */
+CSG_EXPORT int csg_measure_fp_peaks(double *fp32_tflops, double *fp64_tflops);
+
 /* Free-function parity mode: gravity with the reference's exact operation
    sequence (no fused multiply-add, 1/(r2*sqrt(r2))). Same signature as
    octree_compute_forces. */

@@ -30,7 +30,8 @@ def body(x, y, z, m, vx=0.0, vy=0.0, vz=0.0):
 
 
 def bodies(*rows):
-    return np.concatenate([body(*r) for r in rows])
+    # concatenate repacks padded dtypes; restore the 168-byte Body layout
+    return np.concatenate([body(*r) for r in rows]).astype(BODY_DTYPE)
 
 
 # ---- known-answer tests (reference tests/test_physics.c) ----
