@@ -278,3 +278,140 @@ extern "C" CSG_EXPORT int csg_measure_fp_peaks(double *fp32_tflops, double *fp64
     cudaStreamDestroy(s);
     return rc;
 }
+
+// ---- direct sum without allocation -----------------------------------------
+//
+// Callers that cannot allocate device memory — code inside an engine or
+// renderer that owns a fixed GPU budget and its own allocator, a real-time
+// thread that must not block on cudaMalloc/cudaFree (both can synchronise the
+// device) — can still run the FP64 direct-sum check on buffers they already
+// hold. Its scratch (per-chunk partial sums) lives in the file-scope array
+// below instead of cudaMalloc'd memory: 16 chunks x 4096 bodies x 3 doubles =
+// 1.5 MiB, held by every GPU that loads the library until the process exits.
+// All calls share that array, so calls that overlap on the GPU race; every
+// call overwrites each partial it later reads, so nothing needs clearing.
+
+constexpr int NOALLOC_CHUNKS = 16;
+constexpr int NOALLOC_MAX_SAMPLE = 4096;
+constexpr int NOALLOC_MAX_DEVICES = 64;
+
+static __device__ __align__(256) double g_noalloc_partials[NOALLOC_CHUNKS * NOALLOC_MAX_SAMPLE * 3];
+
+#include <mutex>
+
+namespace {
+
+std::mutex g_noalloc_mutex;
+double *g_noalloc_ptr[NOALLOC_MAX_DEVICES];
+
+__global__ void __launch_bounds__(DT) k_direct_noalloc(const double *__restrict__ x,
+                                                       const double *__restrict__ y,
+                                                       const double *__restrict__ z,
+                                                       const double *__restrict__ m, int n,
+                                                       const int *__restrict__ idx, int ns,
+                                                       double G, double eps2,
+                                                       double *__restrict__ part)
+{
+    __shared__ double sx[DT], sy[DT], sz[DT], sm[DT];
+    const int k = blockIdx.x * DT + threadIdx.x;
+    const int chunk = blockIdx.y;
+    const int per = (n + NOALLOC_CHUNKS - 1) / NOALLOC_CHUNKS;
+    const int j0 = chunk * per, j1 = min(n, j0 + per);
+    const int i = (k < ns) ? idx[k] : -1;
+    const double xi = (i >= 0) ? x[i] : 0.0, yi = (i >= 0) ? y[i] : 0.0, zi = (i >= 0) ? z[i] : 0.0;
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    for (int t = j0; t < j1; t += DT) {
+        const int j = t + threadIdx.x;
+        __syncthreads();
+        if (j < j1) {
+            sx[threadIdx.x] = x[j];
+            sy[threadIdx.x] = y[j];
+            sz[threadIdx.x] = z[j];
+            sm[threadIdx.x] = (m[j] <= 0.0) ? 0.0 : m[j];
+        }
+        __syncthreads();
+        const int cnt = min(DT, j1 - t);
+        if (i >= 0) {
+            for (int q = 0; q < cnt; q++) {
+                if (t + q == i)
+                    continue;
+                double dx = sx[q] - xi, dy = sy[q] - yi, dz = sz[q] - zi;
+                double r2 = dx * dx + dy * dy + dz * dz + eps2;
+                double inv = 1.0 / (r2 * sqrt(r2));
+                double f = G * sm[q] * inv;
+                ax += f * dx;
+                ay += f * dy;
+                az += f * dz;
+            }
+        }
+    }
+    if (k < ns) {
+        double *p = part + ((size_t)chunk * ns + k) * 3;
+        p[0] = ax;
+        p[1] = ay;
+        p[2] = az;
+    }
+}
+
+__global__ void k_direct_noalloc_sum(const double *__restrict__ part, int ns,
+                                     double *__restrict__ out)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ns)
+        return;
+    double a[3] = {0.0, 0.0, 0.0};
+    for (int c = 0; c < NOALLOC_CHUNKS; c++)
+        for (int d = 0; d < 3; d++)
+            a[d] += part[((size_t)c * ns + k) * 3 + d];
+    for (int d = 0; d < 3; d++)
+        out[3 * (size_t)k + d] = a[d];
+}
+
+} // namespace
+
+// The device address of the scratch array on the current device, looked up
+// once per device (the first call on a device does it, so that call should
+// come before any stream capture on that device).
+static int noalloc_scratch(double **ptr)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES) {
+        cudaGetLastError();
+        return CSG_ERR_NO_DEVICE;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_partials) != cudaSuccess || !p) {
+            cudaGetLastError();
+            return CSG_ERR_CUDA;
+        }
+        g_noalloc_ptr[dev] = (double *)p;
+    }
+    *ptr = g_noalloc_ptr[dev];
+    return CSG_OK;
+}
+
+extern "C" CSG_EXPORT int csg_direct_forces_noalloc(const double *x, const double *y,
+                                                    const double *z, const double *mass, int n,
+                                                    const int *idx, int m, double G,
+                                                    double softening, double *out, void *stream)
+{
+    if (n < 0 || m < 0 || m > NOALLOC_MAX_SAMPLE)
+        return CSG_ERR_BAD_ARG;
+    if (m == 0)
+        return CSG_OK;
+    if (!x || !y || !z || !mass || !idx || !out || n == 0)
+        return CSG_ERR_BAD_ARG;
+    double *part = nullptr;
+    int rc = noalloc_scratch(&part);
+    if (rc)
+        return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    dim3 grid((m + DT - 1) / DT, NOALLOC_CHUNKS);
+    k_direct_noalloc<<<grid, DT, 0, s>>>(x, y, z, mass, n, idx, m, G, softening * softening, part);
+    k_direct_noalloc_sum<<<(m + 255) / 256, 256, 0, s>>>(part, m, out);
+    if (cudaGetLastError() != cudaSuccess)
+        return CSG_ERR_CUDA;
+    return CSG_OK;
+}

@@ -72,6 +72,7 @@ _SIGS = {
     "cosmosim_energy": ([_vp, ctypes.POINTER(_d), ctypes.POINTER(_d)], _i),
     "cosmosim_launch_count": ([_vp], ctypes.c_int64),
     "csg_measure_fp_peaks": ([ctypes.POINTER(_d), ctypes.POINTER(_d)], _i),
+    "csg_direct_forces_noalloc": ([_vp, _vp, _vp, _vp, _i, _vp, _i, _d, _d, _vp, _vp], _i),
 }
 
 _lib = None

@@ -106,6 +106,21 @@ CSG_EXPORT int64_t cosmosim_launch_count(SimHandle handle);
    bound by. */
 CSG_EXPORT int csg_measure_fp_peaks(double *fp32_tflops, double *fp64_tflops);
 
+/* FP64 direct-sum accelerations without any allocation — has no counterpart
+   in the reference. For callers that cannot allocate device memory (an
+   engine or renderer with a fixed GPU budget and its own allocator, a
+   real-time thread that must not block on cudaMalloc/cudaFree): all pointers
+   are device pointers the caller already owns — x, y, z, mass (n bodies, SoA),
+   idx (m sample indices) and out (3*m doubles); the work is queued on the
+   given cudaStream_t and not waited for. Scratch is a fixed 1.5 MiB array
+   inside the library, so m may be at most 4096 (larger m: CSG_ERR_BAD_ARG).
+   The first call on each device looks up that array's address, so make it
+   before any stream capture on that device. Calls share the array: calls
+   that overlap on the GPU race. Same formula as cosmosim_direct_forces. */
+CSG_EXPORT int csg_direct_forces_noalloc(const double *x, const double *y, const double *z,
+                                         const double *mass, int n, const int *idx, int m,
+                                         double G, double softening, double *out, void *stream);
+
 /* Free-function parity mode: gravity with the reference's exact operation
    sequence (no fused multiply-add, 1/(r2*sqrt(r2))). Same signature as
    octree_compute_forces. */
