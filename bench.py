@@ -271,6 +271,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=20.0,
                     help="seconds of CPU work for the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", default=None, choices=["fp32", "fp64"],
+                    help="only run warm-up + --steps substeps at this precision (for ncu)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -307,6 +309,17 @@ def main():
     from cosmosim_gb300 import lib
 
     lib.load()
+    if args.profile:
+        prec = lib.PREC_FP32_MIXED if args.profile == "fp32" else lib.PREC_FP64
+        b = lib.generate_ics(cfg["kind"], cfg["n"], SEED)
+        sim = lib.Sim.from_bodies(b, softening=cfg["eps"], theta=cfg["theta"], dt=cfg["dt"],
+                                  sph=cfg["sph"], precision=prec)
+        sim.set_stream(work_stream.cuda_stream)
+        sim.substeps_async(args.warmup + args.steps)
+        sim.sync()
+        print(json.dumps({"profile": args.profile, "config": args.config,
+                          "substeps": args.warmup + args.steps, "launches": sim.launch_count()}))
+        return
     fp32_peak, fp64_peak = lib.measure_fp_peaks()
     r = run_cuda(args, torch, lib, cfg, rank, world)
     f32, f64 = r["runs"]["fp32_mixed"], r["runs"]["fp64"]

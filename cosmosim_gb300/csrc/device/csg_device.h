@@ -66,6 +66,16 @@ int csgd_kick(csgd_t *d, double dt);
 /* One full KDK substep, all on the device (reference src/integrator.c:12-57). */
 int csgd_substep(csgd_t *d, double dt, const csgd_force_params *p, int sph);
 
+/* k substeps; with graphs enabled (default) one substep is captured once as a
+   CUDA graph and replayed (re-captured when dt/G/softening/theta/precision/
+   sph/n or the stream change). */
+int csgd_substeps(csgd_t *d, int k, double dt, const csgd_force_params *p, int sph);
+void csgd_enable_graphs(csgd_t *d, int on);
+
+/* Allocates the SPH neighbour lists now (they are otherwise allocated on the
+   first SPH pass, which must not happen inside a stream capture). */
+int csgd_prepare_sph(csgd_t *d);
+
 /* The tree as a reference-layout pool, in the reference's allocation order.
    Blocks until done. pool must hold *pool_size_out <= capacity nodes. */
 int csgd_export_pool(csgd_t *d, OctreeNode *pool, int capacity, int *pool_size_out);

@@ -41,6 +41,19 @@ struct __align__(16) NodeW32 {
     float pad;
 };
 
+// FP32 neighbour-search record: the cell cube, and for a leaf its body
+// position and index (body -1 for internal cells, -2 for a leaf whose body is
+// dead, -3 for a leaf that names no body). cmax = max |centre| + half size bounds the FP32
+// rounding of box tests.
+struct __align__(16) NodeS32 {
+    float cx, cy, cz, hs;
+    float bx, by, bz;
+    int body;
+    int next;
+    float cmax;
+    int pad0, pad1;
+};
+
 struct __align__(16) NodeLink {
     int parent;
     int level;
@@ -96,12 +109,16 @@ struct csgd {
     int *scan_tmp;
     int scan_tmp_cap;
     int *gas;          // gas bodies in key order (caller indices)
+    int *nb;           // SPH neighbour lists, 128 slots x cap (slot-major)
+    int *nb_count;
+    int nb_cap;
 
     // nodes
     NodeW64 *w64;
     NodeW32 *w32;
     NodeLink *link;
     double4 *geo;
+    NodeS32 *s32;
     int *child;   // 8 per node
     int *nchild;
     int *ticket;
@@ -112,6 +129,13 @@ struct csgd {
     DevScalars *sc;      // device
     DevScalars *sc_host; // pinned mirror
     int geometry_valid;
+    // captured substep (cosmosim_substeps_async path)
+    cudaGraphExec_t graph;
+    unsigned long long graph_launches; // kernels in one replay
+    double graph_key[4];               // dt, G, softening, theta it was captured for
+    int graph_prec, graph_sph, graph_n;
+    cudaStream_t graph_stream;
+    int use_graphs;
     int imported;  // the tree came from a caller pool (no sorted order)
     int gas_valid; // d->gas / n_gas match the current tree
 };

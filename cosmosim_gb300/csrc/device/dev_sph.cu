@@ -5,9 +5,12 @@
 // Neighbour order matters: the reference keeps the first 128 bodies within
 // the radius in depth-first octant order (src/octree.c:260-277, sph.h:9), and
 // the cap binds often. Walking the preorder tree with per-lane subtree skips
-// (as in dev_walk.cu) meets the leaves in exactly that order, so each lane can
-// sum its density/force terms on the fly, in the reference's order, without a
-// neighbour list. Lanes are the gas bodies in key order.
+// (as in dev_walk.cu) meets the leaves in exactly that order. Each pass runs in
+// two kernels: the walk records every gas body's capped list, then a pair
+// kernel sums over the lists in that order — the FP64 pair arithmetic (sqrt,
+// divisions: slow on this GPU) then runs densely, one lane per gas body,
+// instead of once per walk step for whichever lanes found a neighbour.
+// Lanes are the gas bodies in key order.
 //
 // Compiled with -fmad=false, with the reference's operation order, so for the
 // same inputs every sum rounds as the reference's does.
@@ -57,103 +60,183 @@ struct SphArgs {
     double *h, *rho, *P, *u;
     double *ax, *ay, *az;
     const double4 *geo;
+    const NodeS32 *s32;
     const NodeW64 *w64;
     DevScalars *sc;
-    int n, node_cap;
+    int *nb;       // neighbour lists, slot-major
+    int *nb_count; // neighbours per gas body
+    int n, node_cap, stride;
 };
 
-struct NbStep {
-    int next, body;
-};
+// ---- neighbour lists: one warp per query ----------------------------------
+//
+// The warp scans the preorder cells 32 at a time. Lane k tests cell cur+k
+// against the query sphere (the reference's box test, src/octree.c:250-256).
+// A cell is reached only if no ancestor failed; inside the window an
+// ancestor u of v satisfies u < v < next(u), so "v lies under a failed cell"
+// is an exclusive prefix-max over lanes of next(u) of failed cells, compared
+// with v. Reached leaves whose body lies within the radius are neighbours,
+// taken in lane (= depth-first) order up to the cap. The cursor then moves
+// past the window and past every failed cell's subtree.
+//
+// Tests run in FP32 with a bound on their rounding: a decision is taken in
+// FP32 only when the FP32 value clears the threshold by more than that bound
+// (position errors <= 8 ulp of the largest magnitude involved per axis, plus
+// 2^-18 relative on the squared sums); otherwise the reference's own FP64
+// expression decides. So every decision equals the reference's.
 
-// Shared traversal: calls visit(j) for each neighbour j of the lane in
-// depth-first order until the lane has `cap` neighbours.
-template <typename Visit>
-__device__ __forceinline__ void neighbour_walk(const SphArgs &a, bool valid, double qx, double qy,
-                                               double qz, double r2, double4 *wgeo, NbStep *wnb,
-                                               Visit visit)
+constexpr float FP32_EPS_POS = 0x1p-21f; // 8 x 2^-24 per axis
+constexpr float FP32_EPS_SUM = 0x1p-18f;
+
+// Box test of src/octree.c:250-256: true when the cell may hold neighbours.
+__device__ __forceinline__ bool box_reaches(const NodeS32 &c, float qx, float qy, float qz,
+                                            float mq, float r2f, const SphArgs &a, int cell,
+                                            double px, double py, double pz, double r2)
 {
-    const int lane = threadIdx.x & 31;
-    const int nn = (a.sc->n_nodes > a.node_cap) ? 0 : a.sc->n_nodes;
-    int skip = valid ? 0 : INT_MAX;
-    int found = 0;
-    int cur = 0, wbase = INT_MIN / 2;
-    while (cur < nn) {
-        if (__all_sync(0xffffffffu, skip == INT_MAX))
-            break;
-        if (cur - wbase >= CSG_WARP) {
-            wbase = cur;
-            __syncwarp();
-            if (wbase + lane < nn) {
-                wgeo[lane] = a.geo[wbase + lane];
-                wnb[lane] = NbStep{a.w64[wbase + lane].next, a.w64[wbase + lane].body};
-            }
-            __syncwarp();
-        }
-        const double4 g = wgeo[cur - wbase];
-        const NbStep s = wnb[cur - wbase];
-        bool descend = false;
-        if (cur >= skip) {
-            double gx = fmax(0.0, fabs(qx - g.x) - g.w);
-            double gy = fmax(0.0, fabs(qy - g.y) - g.w);
-            double gz = fmax(0.0, fabs(qz - g.z) - g.w);
-            if (gx * gx + gy * gy + gz * gz > r2) {
-                skip = s.next;
-            } else if (s.body >= 0) {
-                const int j = s.body;
-                if (j >= a.n) {
-                    dev_fail(a.sc, CSG_ERR_BAD_POOL);
-                } else if (!(a.m[j] <= 0.0)) {
-                    double bx = a.x[j] - qx;
-                    double by = a.y[j] - qy;
-                    double bz = a.z[j] - qz;
-                    if (bx * bx + by * by + bz * bz <= r2) {
-                        visit(j);
-                        if (++found >= CSG_SPH_MAX_NEIGHBORS)
-                            skip = INT_MAX;
-                    }
-                }
-            } else {
-                descend = true;
-            }
-        }
-        const int nxt = __any_sync(0xffffffffu, descend) ? cur + 1 : s.next;
-        if (nxt <= cur) {
-            dev_fail(a.sc, CSG_ERR_WALK_LIMIT);
-            break;
-        }
-        cur = nxt;
-    }
-    // the count is returned through visit's captured state
-    (void)found;
+    const float e = (mq + c.cmax) * FP32_EPS_POS;
+    const float dx = fmaxf(0.0f, fabsf(qx - c.cx) - c.hs);
+    const float dy = fmaxf(0.0f, fabsf(qy - c.cy) - c.hs);
+    const float dz = fmaxf(0.0f, fabsf(qz - c.cz) - c.hs);
+    const float lx = fmaxf(0.0f, dx - e), ly = fmaxf(0.0f, dy - e), lz = fmaxf(0.0f, dz - e);
+    const float lo = lx * lx + ly * ly + lz * lz;
+    if (lo > r2f * (1.0f + FP32_EPS_SUM))
+        return false;
+    const float hx = dx + e, hy = dy + e, hz = dz + e;
+    const float hi = hx * hx + hy * hy + hz * hz;
+    if (hi < r2f * (1.0f - FP32_EPS_SUM))
+        return true;
+    const double4 g = a.geo[cell]; // too close to call in FP32
+    double gx = fmax(0.0, fabs(px - g.x) - g.w);
+    double gy = fmax(0.0, fabs(py - g.y) - g.w);
+    double gz = fmax(0.0, fabs(pz - g.z) - g.w);
+    return !(gx * gx + gy * gy + gz * gz > r2);
 }
 
-// src/sph.c:45-97
-__global__ void __launch_bounds__(SPH_THREADS) k_sph_density(SphArgs a)
+// Leaf test of src/octree.c:262-272: body within the radius.
+__device__ __forceinline__ bool leaf_within(const NodeS32 &c, float qx, float qy, float qz,
+                                            float mq, float r2f, const SphArgs &a, double px,
+                                            double py, double pz, double r2)
 {
-    __shared__ double4 wgeo_all[SPH_WARPS][CSG_WARP];
-    __shared__ NbStep wnb_all[SPH_WARPS][CSG_WARP];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const float mb = fmaxf(fabsf(c.bx), fmaxf(fabsf(c.by), fabsf(c.bz)));
+    const float e = (mq + mb) * FP32_EPS_POS;
+    const float dx = fabsf(c.bx - qx), dy = fabsf(c.by - qy), dz = fabsf(c.bz - qz);
+    const float hx = dx + e, hy = dy + e, hz = dz + e;
+    const float hi = hx * hx + hy * hy + hz * hz;
+    if (hi < r2f * (1.0f - FP32_EPS_SUM))
+        return true;
+    const float lx = fmaxf(0.0f, dx - e), ly = fmaxf(0.0f, dy - e), lz = fmaxf(0.0f, dz - e);
+    const float lo = lx * lx + ly * ly + lz * lz;
+    if (lo > r2f * (1.0f + FP32_EPS_SUM))
+        return false;
+    const int j = c.body;
+    double bx = a.x[j] - px;
+    double by = a.y[j] - py;
+    double bz = a.z[j] - pz;
+    return bx * bx + by * by + bz * bz <= r2;
+}
+
+__device__ __forceinline__ int warp_excl_max(int v)
+{
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o)
+            v = max(v, t);
+    }
+    int ex = __shfl_up_sync(0xffffffffu, v, 1);
+    return lane == 0 ? INT_MIN : ex;
+}
+
+// Lists: gas body gas[k] gets its first CSG_SPH_MAX_NEIGHBORS neighbours within
+// its current smoothing length, in depth-first order, slot-major
+// (nb[slot * stride + k]) for coalesced reads in the pair kernels. The density
+// pass uses h before its update (src/sph.c:53-63), the force pass after it
+// (src/sph.c:112-126): each pass builds its list from the h it sees.
+__device__ __forceinline__ void list_one(const SphArgs &a, int k, int lane)
+{
+    const int nnodes = (a.sc->n_nodes > a.node_cap) ? 0 : a.sc->n_nodes;
+    const int i = a.gas[k];
+    const double px = a.x[i], py = a.y[i], pz = a.z[i];
+    const double h = a.h[i];
+    const double r2 = h * h;
+    const float qx = (float)px, qy = (float)py, qz = (float)pz;
+    const float mq = fmaxf(fabsf(qx), fmaxf(fabsf(qy), fabsf(qz)));
+    const float r2f = (float)r2;
+    const unsigned lt = (1u << lane) - 1u;
+    const size_t stride = (size_t)a.stride;
+    int found = 0;
+    int cur = 0;
+    while (cur < nnodes && found < CSG_SPH_MAX_NEIGHBORS) {
+        const int v = cur + lane;
+        const bool valid = v < nnodes;
+        NodeS32 c;
+        bool reach = false;
+        int fail_next = 0;
+        if (valid) {
+            c = a.s32[v];
+            reach = box_reaches(c, qx, qy, qz, mq, r2f, a, v, px, py, pz, r2);
+            if (!reach)
+                fail_next = c.next;
+            if (c.next <= v)
+                dev_fail(a.sc, CSG_ERR_WALK_LIMIT);
+        }
+        const int above = warp_excl_max(fail_next);
+        bool cand = false;
+        if (valid && reach && above <= v && c.body != -1) {
+            if (c.body == -3)
+                dev_fail(a.sc, CSG_ERR_BAD_POOL);
+            else if (c.body >= 0)
+                cand = leaf_within(c, qx, qy, qz, mq, r2f, a, px, py, pz, r2);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, cand);
+        if (cand) {
+            const int slot = found + __popc(m & lt);
+            if (slot < CSG_SPH_MAX_NEIGHBORS)
+                a.nb[stride * slot + k] = c.body;
+        }
+        found = min(CSG_SPH_MAX_NEIGHBORS, found + __popc(m));
+        // skip past the window and past every failed subtree
+        const int jump = __reduce_max_sync(0xffffffffu, (unsigned)max(fail_next, 0));
+        cur = max(cur + CSG_WARP, jump); // strictly increases: the loop ends
+    }
+    if (lane == 0)
+        a.nb_count[k] = found;
+}
+
+__global__ void __launch_bounds__(SPH_THREADS) k_sph_lists(SphArgs a)
+{
+    const int lane = threadIdx.x & 31;
     const int n_gas = a.sc->n_gas;
-    const long long k = (long long)blockIdx.x * SPH_THREADS + threadIdx.x;
-    if (k - lane >= n_gas)
+    const int nwarps = (int)((gridDim.x * (long long)SPH_THREADS) >> 5);
+    for (int k = (int)(((long long)blockIdx.x * SPH_THREADS + threadIdx.x) >> 5); k < n_gas;
+         k += nwarps) // warp-uniform
+        list_one(a, k, lane);
+}
+
+// Density, adaptive h and pressure over the recorded list, src/sph.c:45-97.
+// Lanes walk their own lists in lockstep: no work is repeated for lanes that
+// found no neighbour at a given step.
+__global__ void __launch_bounds__(SPH_THREADS) k_sph_density_pairs(SphArgs a)
+{
+    const int k = blockIdx.x * SPH_THREADS + threadIdx.x;
+    if (k >= a.sc->n_gas)
         return;
-    const bool valid = k < n_gas;
-    const int i = valid ? a.gas[k] : 0;
+    const int i = a.gas[k];
     const double qx = a.x[i], qy = a.y[i], qz = a.z[i];
     const double h = a.h[i];
+    const int nn = a.nb_count[k];
+    const int *lst = a.nb + k;
+    const size_t stride = (size_t)a.stride;
     double rho = 0.0;
-    int nn = 0;
-    neighbour_walk(a, valid, qx, qy, qz, h * h, wgeo_all[warp], wnb_all[warp], [&](int j) {
-        nn++;
+    for (int s = 0; s < nn; s++) {
+        const int j = lst[stride * s];
         double dx = qx - a.x[j];
         double dy = qy - a.y[j];
         double dz = qz - a.z[j];
         double r = sqrt(dx * dx + dy * dy + dz * dz);
         rho += a.m[j] * kernel_W(r, h);
-    });
-    if (!valid)
-        return;
+    }
     if (nn < 20 && h < 50.0)
         a.h[i] = h * 1.2;
     else if (nn > 48 && h > 0.1)
@@ -167,34 +250,34 @@ __global__ void __launch_bounds__(SPH_THREADS) k_sph_density(SphArgs a)
     a.P[i] = (GAMMA - 1.0) * rho * u;
 }
 
-// src/sph.c:101-196
-__global__ void __launch_bounds__(SPH_THREADS) k_sph_forces(SphArgs a)
+// Pressure gradient + Monaghan viscosity over the recorded list,
+// src/sph.c:101-196.
+__global__ void __launch_bounds__(SPH_THREADS) k_sph_forces_pairs(SphArgs a)
 {
-    __shared__ double4 wgeo_all[SPH_WARPS][CSG_WARP];
-    __shared__ NbStep wnb_all[SPH_WARPS][CSG_WARP];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int n_gas = a.sc->n_gas;
-    const long long k = (long long)blockIdx.x * SPH_THREADS + threadIdx.x;
-    if (k - lane >= n_gas)
+    const int k = blockIdx.x * SPH_THREADS + threadIdx.x;
+    if (k >= a.sc->n_gas)
         return;
-    const bool valid = k < n_gas;
-    const int i = valid ? a.gas[k] : 0;
+    const int i = a.gas[k];
     const double qx = a.x[i], qy = a.y[i], qz = a.z[i];
     const double h_i = a.h[i];
     const double rho_i = a.rho[i];
     const double P_i = a.P[i];
     const double c_i = sqrt(GAMMA * P_i / (rho_i + 1e-15));
     const double vxi = a.vx[i], vyi = a.vy[i], vzi = a.vz[i];
+    const int nn = a.nb_count[k];
+    const int *lst = a.nb + k;
+    const size_t stride = (size_t)a.stride;
     double sx = 0.0, sy = 0.0, sz = 0.0;
-    neighbour_walk(a, valid, qx, qy, qz, h_i * h_i, wgeo_all[warp], wnb_all[warp], [&](int j) {
+    for (int s = 0; s < nn; s++) {
+        const int j = lst[stride * s];
         if (j == i || a.type[j] != BODY_GAS)
-            return;
+            continue;
         double dx = qx - a.x[j];
         double dy = qy - a.y[j];
         double dz = qz - a.z[j];
         double r = sqrt(dx * dx + dy * dy + dz * dz);
         if (r < 1e-15)
-            return;
+            continue;
         double h_avg = 0.5 * (h_i + a.h[j]);
         double rho_j = a.rho[j];
         double P_j = a.P[j];
@@ -218,9 +301,7 @@ __global__ void __launch_bounds__(SPH_THREADS) k_sph_forces(SphArgs a)
         sx -= f * gx;
         sy -= f * gy;
         sz -= f * gz;
-    });
-    if (!valid)
-        return;
+    }
     if (isnan(sx))
         sx = 0.0;
     if (isnan(sy))
@@ -312,10 +393,14 @@ SphArgs make_args(csgd_t *d)
     a.ay = d->ay;
     a.az = d->az;
     a.geo = d->geo;
+    a.s32 = d->s32;
     a.w64 = d->w64;
     a.sc = d->sc;
+    a.nb = d->nb;
+    a.nb_count = d->nb_count;
     a.n = d->n;
     a.node_cap = d->node_cap;
+    a.stride = d->cap;
     return a;
 }
 
@@ -364,7 +449,30 @@ int gas_list(csgd_t *d)
 
 } // namespace
 
-extern "C" int csgd_sph_density(csgd_t *d)
+// Lists live in device memory sized for every body being gas (128 ints each),
+// allocated on first SPH use.
+static int ensure_lists(csgd_t *d)
+{
+    if (d->nb && d->nb_cap >= d->cap)
+        return CSG_OK;
+    if (d->nb)
+        cudaFree(d->nb);
+    if (d->nb_count)
+        cudaFree(d->nb_count);
+    d->nb = nullptr;
+    d->nb_count = nullptr;
+    size_t c = (size_t)(d->cap > 0 ? d->cap : 1);
+    if (cudaMalloc((void **)&d->nb, sizeof(int) * CSG_SPH_MAX_NEIGHBORS * c) != cudaSuccess ||
+        cudaMalloc((void **)&d->nb_count, sizeof(int) * c) != cudaSuccess) {
+        cudaGetLastError();
+        csgd_set_err(d, CSG_ERR_NOMEM);
+        return CSG_ERR_NOMEM;
+    }
+    d->nb_cap = d->cap;
+    return CSG_OK;
+}
+
+static int sph_pass(csgd_t *d, int forces)
 {
     if (d->n <= 0)
         return CSG_OK;
@@ -372,29 +480,30 @@ extern "C" int csgd_sph_density(csgd_t *d)
         csgd_set_err(d, CSG_ERR_BAD_ARG);
         return CSG_ERR_BAD_ARG;
     }
-    int rc = gas_list(d);
+    int rc = ensure_lists(d);
+    if (!rc)
+        rc = gas_list(d);
     if (rc)
         return rc;
     SphArgs a = make_args(d);
-    { k_sph_density<<<csgd_grid(d->n, SPH_THREADS), SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
+    const int g = csgd_grid(d->n, SPH_THREADS);
+    // one warp per gas body for the lists, warps striding over the gas bodies
+    int gl = csgd_grid((long long)d->n * CSG_WARP, SPH_THREADS);
+    if (gl > 152 * 16)
+        gl = 152 * 16;
+    { k_sph_lists<<<gl, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
+    if (forces)
+        { k_sph_forces_pairs<<<g, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
+    else
+        { k_sph_density_pairs<<<g, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
     return csgd_check(d, cudaGetLastError());
 }
 
-extern "C" int csgd_sph_forces(csgd_t *d)
-{
-    if (d->n <= 0)
-        return CSG_OK;
-    if (!d->geometry_valid) {
-        csgd_set_err(d, CSG_ERR_BAD_ARG);
-        return CSG_ERR_BAD_ARG;
-    }
-    int rc = gas_list(d);
-    if (rc)
-        return rc;
-    SphArgs a = make_args(d);
-    { k_sph_forces<<<csgd_grid(d->n, SPH_THREADS), SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
-    return csgd_check(d, cudaGetLastError());
-}
+extern "C" int csgd_sph_density(csgd_t *d) { return sph_pass(d, 0); }
+
+extern "C" int csgd_prepare_sph(csgd_t *d) { return ensure_lists(d); }
+
+extern "C" int csgd_sph_forces(csgd_t *d) { return sph_pass(d, 1); }
 
 extern "C" int csgd_find_neighbors(csgd_t *d, double cx, double cy, double cz, double radius,
                                    int *buf, int cap, int *count_out)

@@ -141,7 +141,7 @@ void free_bodies(csgd_t *d)
     void *ptrs[] = {d->x, d->y, d->z, d->vx, d->vy, d->vz, d->ax, d->ay, d->az, d->m,
                     d->rho, d->P, d->u, d->h, d->type, d->aos, d->key, d->key_alt, d->perm,
                     d->perm_alt, d->ext, d->sort_hist, d->lcp, d->cnt, d->base, d->scan_tmp,
-                    d->gas, d->w64, d->w32, d->link, d->geo, d->child, d->nchild, d->ticket,
+                    d->gas, d->w64, d->w32, d->link, d->geo, d->s32, d->child, d->nchild, d->ticket,
                     d->minidx, d->ord_key, d->ord_key_alt, d->ord_id, d->ord_id_alt, d->rank,
                     d->pool};
     for (void *p : ptrs)
@@ -161,6 +161,7 @@ void free_bodies(csgd_t *d)
     d->w32 = nullptr;
     d->link = nullptr;
     d->geo = nullptr;
+    d->s32 = nullptr;
     d->child = d->nchild = d->ticket = nullptr;
     d->minidx = nullptr;
     d->ord_key = d->ord_key_alt = nullptr;
@@ -235,6 +236,7 @@ extern "C" csgd_t *csgd_create(void)
         return nullptr;
     }
     d->stream = d->own_stream;
+    d->use_graphs = 1;
     if (cudaMalloc((void **)&d->sc, sizeof(DevScalars)) != cudaSuccess ||
         cudaMallocHost((void **)&d->sc_host, sizeof(DevScalars)) != cudaSuccess) {
         if (d->sc)
@@ -253,7 +255,13 @@ extern "C" void csgd_destroy(csgd_t *d)
     if (!d)
         return;
     cudaStreamSynchronize(d->stream);
+    if (d->graph)
+        cudaGraphExecDestroy(d->graph);
     free_bodies(d);
+    if (d->nb)
+        cudaFree(d->nb);
+    if (d->nb_count)
+        cudaFree(d->nb_count);
     if (d->sc)
         cudaFree(d->sc);
     if (d->sc_host)
@@ -272,7 +280,15 @@ extern "C" void *csgd_stream(csgd_t *d) { return (void *)d->stream; }
 
 extern "C" int csgd_count(const csgd_t *d) { return d->n; }
 
-extern "C" void csgd_enable_stats(csgd_t *d, int on) { d->stats = on; }
+extern "C" void csgd_enable_stats(csgd_t *d, int on)
+{
+    if (d->stats != on && d->graph) { // the captured walk variant changes
+        cudaStreamSynchronize(d->stream);
+        cudaGraphExecDestroy(d->graph);
+        d->graph = nullptr;
+    }
+    d->stats = on;
+}
 
 extern "C" int csgd_reserve(csgd_t *d, int n)
 {
@@ -284,6 +300,10 @@ extern "C" int csgd_reserve(csgd_t *d, int n)
     if (n <= d->cap && d->cap > 0)
         return CSG_OK;
     cudaStreamSynchronize(d->stream);
+    if (d->graph) { // captured pointers are about to change
+        cudaGraphExecDestroy(d->graph);
+        d->graph = nullptr;
+    }
     free_bodies(d);
     const size_t cap = (size_t)(n > 0 ? n : 1);
     const size_t ncap = 8 * cap + 64; // the reference's pool contract
@@ -324,6 +344,7 @@ extern "C" int csgd_reserve(csgd_t *d, int n)
     ok &= dalloc(&d->w32, ncap) == cudaSuccess;
     ok &= dalloc(&d->link, ncap) == cudaSuccess;
     ok &= dalloc(&d->geo, ncap) == cudaSuccess;
+    ok &= dalloc(&d->s32, ncap) == cudaSuccess;
     ok &= dalloc(&d->child, 8 * ncap) == cudaSuccess;
     ok &= dalloc(&d->nchild, ncap) == cudaSuccess;
     ok &= dalloc(&d->ticket, ncap) == cudaSuccess;
@@ -491,3 +512,86 @@ extern "C" int csgd_alive_count(csgd_t *d, int *count)
 }
 
 extern "C" unsigned long long csgd_launch_count(const csgd_t *d) { return d->launches; }
+
+extern "C" void csgd_enable_graphs(csgd_t *d, int on) { d->use_graphs = on; }
+
+static bool graph_matches(const csgd_t *d, double dt, const csgd_force_params *p, int sph)
+{
+    return d->graph && d->graph_key[0] == dt && d->graph_key[1] == p->G &&
+           d->graph_key[2] == p->softening && d->graph_key[3] == p->theta &&
+           d->graph_prec == p->precision && d->graph_sph == sph && d->graph_n == d->n &&
+           d->graph_stream == d->stream;
+}
+
+// Captures one substep on the state's stream. Returns CSG_OK or an error (the
+// caller then runs the substeps without a graph).
+static int capture_substep(csgd_t *d, double dt, const csgd_force_params *p, int sph)
+{
+    if (d->graph) {
+        cudaGraphExecDestroy(d->graph);
+        d->graph = nullptr;
+    }
+    if (sph && csgd_prepare_sph(d))
+        return CSG_ERR_NOMEM;
+    // host-side flags a substep resets anyway; start from the same state
+    d->gas_valid = 0;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return CSG_ERR_CUDA;
+    }
+    const unsigned long long l0 = d->launches;
+    int rc = csgd_substep(d, dt, p, sph);
+    cudaError_t e = cudaStreamEndCapture(d->stream, &g);
+    const unsigned long long per = d->launches - l0;
+    d->launches = l0; // counted again on every replay
+    if (rc || e != cudaSuccess || !g) {
+        if (g)
+            cudaGraphDestroy(g);
+        cudaGetLastError();
+        d->host_err = 0;
+        return rc ? rc : CSG_ERR_CUDA;
+    }
+    e = cudaGraphInstantiate(&d->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        d->graph = nullptr;
+        return CSG_ERR_CUDA;
+    }
+    d->graph_launches = per;
+    d->graph_key[0] = dt;
+    d->graph_key[1] = p->G;
+    d->graph_key[2] = p->softening;
+    d->graph_key[3] = p->theta;
+    d->graph_prec = p->precision;
+    d->graph_sph = sph;
+    d->graph_n = d->n;
+    d->graph_stream = d->stream;
+    return CSG_OK;
+}
+
+extern "C" int csgd_substeps(csgd_t *d, int k, double dt, const csgd_force_params *p, int sph)
+{
+    if (k <= 0)
+        return CSG_OK;
+    if (d->use_graphs && d->n > 0 && d->stream != nullptr) {
+        if (!graph_matches(d, dt, p, sph) && capture_substep(d, dt, p, sph) != CSG_OK)
+            d->use_graphs = 0; // run without graphs from now on
+    }
+    if (d->use_graphs && d->graph) {
+        for (int i = 0; i < k; i++) {
+            if (cudaGraphLaunch(d->graph, d->stream) != cudaSuccess)
+                return csgd_check(d, cudaGetLastError());
+            d->launches += d->graph_launches;
+        }
+        d->gas_valid = 0;
+        d->geometry_valid = sph ? 1 : 0;
+        d->imported = 0;
+        return CSG_OK;
+    }
+    int rc = CSG_OK;
+    for (int i = 0; i < k && !rc; i++)
+        rc = csgd_substep(d, dt, p, sph);
+    return rc;
+}

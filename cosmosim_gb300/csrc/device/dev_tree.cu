@@ -595,6 +595,34 @@ __global__ void k_moments(csgd_t dd, DevScalars *sc, const double *__restrict__ 
     }
 }
 
+// FP32 neighbour-search record of one cell (see NodeS32).
+__device__ __forceinline__ void write_s32(const csgd_t &dd, int id, double cx, double cy,
+                                          double cz, double hs, int body, int next)
+{
+    NodeS32 r;
+    r.cx = (float)cx;
+    r.cy = (float)cy;
+    r.cz = (float)cz;
+    r.hs = (float)hs;
+    r.cmax = fmaxf(fabsf(r.cx), fmaxf(fabsf(r.cy), fabsf(r.cz))) + r.hs;
+    r.bx = r.by = r.bz = 0.0f;
+    r.body = body;
+    if (body >= 0) {
+        if (body >= dd.n) {
+            r.body = -3; // a caller pool naming a body that does not exist
+        } else if (dd.m[body] <= 0.0) {
+            r.body = -2;
+        } else {
+            r.bx = (float)dd.x[body];
+            r.by = (float)dd.y[body];
+            r.bz = (float)dd.z[body];
+        }
+    }
+    r.next = next;
+    r.pad0 = r.pad1 = 0;
+    dd.s32[id] = r;
+}
+
 // Geometric cube of every cell, with the reference's arithmetic.
 __global__ void k_geometry(csgd_t dd, DevScalars *sc, const unsigned long long *__restrict__ key,
                            const unsigned long long *__restrict__ ext)
@@ -615,6 +643,7 @@ __global__ void k_geometry(csgd_t dd, DevScalars *sc, const unsigned long long *
         hs = hs * 0.5;
     }
     dd.geo[id] = make_double4(cx, cy, cz, hs);
+    write_s32(dd, id, cx, cy, cz, hs, dd.w64[id].body, dd.w64[id].next);
 }
 
 // ---- export in the reference's allocation order --------------------------
@@ -801,6 +830,7 @@ __global__ void k_imp_write(csgd_t dd, DevScalars *sc, int nn, int root,
     v.pad = 0.0f;
     dd.w32[id] = v;
     dd.geo[id] = make_double4(o.center_x, o.center_y, o.center_z, o.half_size);
+    write_s32(dd, id, o.center_x, o.center_y, o.center_z, o.half_size, w.body, w.next);
     dd.link[id] = NodeLink{-1, depth, -1, 0};
 }
 

@@ -14,12 +14,12 @@
 // The next 32 cells in preorder are staged per warp in shared memory with one
 // coalesced load, and re-staged only when the cursor leaves that window.
 //
-// FP64 walk: the drop-in precision. 1/r^3 from an FP32 rsqrt seed refined by
-//   two Newton steps in FP64 (error ~1 ulp); the opening test is evaluated
-//   exactly as the reference rounds it (division only for ties within 2^-50).
-//   EXACT=true instead uses the reference's own operation sequence
-//   (1/(r2*sqrt(r2)), no fused multiply-add) — bit-identical results on the
-//   reference's own tree; used by the parity tests.
+// FP64 walk: the drop-in precision (k_walk64q). Openings decided as in the
+//   FP32 walk (equal to the reference's FP64 rounding); interactions queued
+//   and evaluated densely in FP64, 1/r^3 from an FP32 rsqrt seed refined to
+//   full FP64 accuracy. k_walk64<EXACT=true> instead uses the reference's own
+//   operation sequence per step (1/(r2*sqrt(r2)), no fused multiply-add) —
+//   bit-identical results on the reference's own tree; used by parity tests.
 // FP32-mixed walk: positions and centres as float hi/lo pairs (differences
 //   keep ~48 bits), rsqrt/products in FP32, Kahan-compensated FP32 sums per
 //   body. Openings within the FP32 error band of the threshold are decided in
@@ -164,6 +164,157 @@ __global__ void __launch_bounds__(WALK_THREADS) k_walk64(WalkArgs a)
         unsigned int h = __reduce_add_sync(0xffffffffu, (unsigned int)hits);
         if (lane == 0)
             atomicAdd(&a.sc->interactions, (unsigned long long)h);
+    }
+}
+
+// 1/r^3 for the queued FP64 walk: FP32 rsqrt seed y0 (rel. error < 2^-21),
+// e = 1 - r2*y0^2 exactly enough in FP64, then y = y0 (1 + e/2 + 3e^2/8)
+// (the Taylor series of (1-e)^-1/2 to second order; residual < 2^-60).
+__device__ __forceinline__ double inv_r3_q(double r2)
+{
+    if (r2 >= 1e-30 && r2 <= 1e30) {
+        const double y0 = (double)rsqrtf((float)r2);
+        const double e = fma(-r2 * y0, y0, 1.0);
+        const double y = fma(y0 * e, fma(0.375, e, 0.5), y0);
+        return y * y * y;
+    }
+    return 1.0 / (r2 * sqrt(r2));
+}
+
+// FP64 walk with dense evaluation. The traversal is the FP32 one below (its
+// decisions equal the FP64 reference's, see k_walk32); accepted cells are
+// pushed into per-lane FIFO queues in shared memory and evaluated in FP64 in
+// batches where every lane has work, in the order they were accepted (the
+// reference's depth-first order). The FP64 pipe then does useful work on
+// (almost) every lane instead of once per traversal step for the few lanes
+// that interact at that step.
+constexpr int Q64 = 32; // queue slots per lane
+constexpr int F64 = 8;  // entries per lane per dense batch
+
+// Evaluates the lane's next `count` queued cells (count >= 0; lanes without a
+// body pass 0 and never read their queue).
+__device__ __forceinline__ void q64_eval(const WalkArgs &a, const int *q, int lane, int &head,
+                                         int count, double px, double py, double pz,
+                                         double &sx, double &sy, double &sz)
+{
+    count = max(count, 0);
+    const int kmax = (int)__reduce_max_sync(0xffffffffu, (unsigned)count);
+    for (int s = 0; s < kmax; s++) {
+        if (s < count) {
+            const int node = q[((head + s) & (Q64 - 1)) * CSG_WARP + lane];
+            const double2 c01 = __ldg((const double2 *)&a.w64[node]);     // cx, cy
+            const double2 c23 = __ldg((const double2 *)&a.w64[node] + 1); // cz, m
+            const double4 c = make_double4(c01.x, c01.y, c23.x, c23.y);
+            const double dx = c.x - px, dy = c.y - py, dz = c.z - pz;
+            const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, a.eps2)));
+            const double f = a.G * c.w * inv_r3_q(r2);
+            sx = fma(f, dx, sx);
+            sy = fma(f, dy, sy);
+            sz = fma(f, dz, sz);
+        }
+    }
+    head += count;
+}
+
+template <bool STATS>
+__global__ void __launch_bounds__(WALK_THREADS) k_walk64q(WalkArgs a)
+{
+    __shared__ NodeW32 win_all[WALK_WARPS][CSG_WARP];
+    __shared__ int q_all[WALK_WARPS][Q64 * CSG_WARP];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    NodeW32 *win = win_all[warp];
+    int *q = q_all[warp];
+    const int n_alive = a.sc->n_alive;
+    const long long p = (long long)blockIdx.x * WALK_THREADS + threadIdx.x;
+    const long long warp0 = p - lane;
+    if (warp0 >= n_alive)
+        return;
+    if (a.sc->n_nodes > a.node_cap || a.sc->n_nodes < 1)
+        return;
+    const int nn = a.sc->n_nodes;
+    const bool valid = p < n_alive;
+    const int me = valid ? a.perm[p] : -1;
+    const double px = valid ? a.x[me] : 0.0, py = valid ? a.y[me] : 0.0,
+                 pz = valid ? a.z[me] : 0.0;
+    const float hx = (float)px, hy = (float)py, hz = (float)pz;
+    const float lx = (float)(px - (double)hx), ly = (float)(py - (double)hy),
+                lz = (float)(pz - (double)hz);
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    int head = 0, tail = 0;
+    unsigned long long hits = 0;
+    int skip = valid ? 0 : INT_MAX;
+    int cur = 0, wbase = INT_MIN / 2;
+    while (cur < nn) {
+        if (cur - wbase >= CSG_WARP) {
+            wbase = cur;
+            __syncwarp();
+            if (wbase + lane < nn)
+                win[lane] = a.w32[wbase + lane];
+            __syncwarp();
+        }
+        const NodeW32 c = win[cur - wbase];
+        bool open = false;
+        if (cur >= skip) {
+            if (c.m == 0.0f && a.w64[cur].m == 0.0) {
+                skip = c.next;
+            } else {
+                bool take;
+                if (c.body >= 0) {
+                    take = (c.body != me);
+                } else {
+                    const float dx = (c.cx - hx) + (c.lx - lx);
+                    const float dy = (c.cy - hy) + (c.ly - ly);
+                    const float dz = (c.cz - hz) + (c.lz - lz);
+                    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    const float lhs = a.theta2f * d2;
+                    const float band = c.s2 * a.guard_rel;
+                    if (c.s2 < lhs - band && d2 > 0.f) {
+                        take = true;
+                    } else if (c.s2 > lhs + band) {
+                        take = false;
+                    } else {
+                        const NodeW64 e = a.w64[cur];
+                        const double ex = e.cx - px, ey = e.cy - py, ez = e.cz - pz;
+                        take = accept64(e.s2, ex * ex + ey * ey + ez * ez, a);
+                    }
+                    if (take)
+                        skip = c.next;
+                    else
+                        open = true;
+                }
+                if (take) {
+                    q[(tail & (Q64 - 1)) * CSG_WARP + lane] = cur;
+                    tail++;
+                    if (STATS)
+                        hits++;
+                }
+            }
+        }
+        const int cnt = tail - head; // 0..Q64-1; always 0 for a lane without a body
+        const int cmin = (int)__reduce_min_sync(0xffffffffu, (unsigned)(valid ? cnt : INT_MAX));
+        const int cmax = (int)__reduce_max_sync(0xffffffffu, (unsigned)cnt);
+        if (cmin >= F64)
+            q64_eval(a, q, lane, head, valid ? F64 : 0, px, py, pz, sx, sy, sz);
+        else if (cmax >= Q64 - 1) // a lane is about to overflow: drain what is there
+            q64_eval(a, q, lane, head, min(cnt, F64), px, py, pz, sx, sy, sz);
+        const int nxt = __any_sync(0xffffffffu, open) ? cur + 1 : c.next;
+        if (nxt <= cur) {
+            dev_fail(a.sc, CSG_ERR_WALK_LIMIT);
+            break;
+        }
+        cur = nxt;
+    }
+    while (__any_sync(0xffffffffu, tail - head > 0))
+        q64_eval(a, q, lane, head, min(tail - head, F64), px, py, pz, sx, sy, sz);
+    if (valid) {
+        a.ax[me] = sx;
+        a.ay[me] = sy;
+        a.az[me] = sz;
+    }
+    if (STATS) {
+        unsigned int hsum = __reduce_add_sync(0xffffffffu, (unsigned int)hits);
+        if (lane == 0)
+            atomicAdd(&a.sc->interactions, (unsigned long long)hsum);
     }
 }
 
@@ -330,9 +481,9 @@ extern "C" int csgd_gravity_ex(csgd_t *d, const csgd_force_params *p, int exact)
             { k_walk64<true, false><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
     } else {
         if (d->stats)
-            { k_walk64<false, true><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
+            { k_walk64q<true><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
         else
-            { k_walk64<false, false><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
+            { k_walk64q<false><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
     }
     return csgd_check(d, cudaGetLastError());
 }

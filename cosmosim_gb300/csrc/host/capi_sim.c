@@ -254,9 +254,7 @@ CSG_EXPORT int cosmosim_substeps_async(SimHandle handle, int k)
         return CSG_ERR_BAD_ARG;
     SimState *s = (SimState *)handle;
     csgd_force_params p = fparams(s);
-    int rc = CSG_OK;
-    for (int i = 0; i < k && !rc; i++)
-        rc = csgd_substep(s->dev, s->params.dt, &p, s->params.sph);
+    int rc = csgd_substeps(s->dev, k, s->params.dt, &p, s->params.sph);
     s->host_stale = 1;
     return set_err(s, rc);
 }
@@ -268,10 +266,14 @@ CSG_EXPORT void cosmosim_step(SimHandle handle)
     SimState *s = (SimState *)handle;
     csgd_force_params p = fparams(s);
     int rc = CSG_OK;
-    for (int sub = 0; sub < s->params.substeps && !rc; sub++) {
-        rc = csgd_substep(s->dev, s->params.dt, &p, s->params.sph);
-        if (!rc && s->quasar)
-            rc = quasar_substep(s);
+    if (!s->quasar) {
+        rc = csgd_substeps(s->dev, s->params.substeps, s->params.dt, &p, s->params.sph);
+    } else {
+        for (int sub = 0; sub < s->params.substeps && !rc; sub++) {
+            rc = csgd_substep(s->dev, s->params.dt, &p, s->params.sph);
+            if (!rc)
+                rc = quasar_substep(s);
+        }
     }
     if (!rc && s->quasar && ++s->compact_counter >= 60) { /* src/cosmosim_api.c:133-142 */
         rc = csgd_download_bodies(s->dev, s->host, s->current_n);
@@ -454,4 +456,12 @@ CSG_EXPORT int64_t cosmosim_launch_count(SimHandle handle)
     if (!handle)
         return 0;
     return (int64_t)csgd_launch_count(((SimState *)handle)->dev);
+}
+
+CSG_EXPORT int cosmosim_enable_graphs(SimHandle handle, int on)
+{
+    if (!handle)
+        return CSG_ERR_BAD_ARG;
+    csgd_enable_graphs(((SimState *)handle)->dev, on);
+    return CSG_OK;
 }

@@ -72,6 +72,7 @@ _SIGS = {
     "cosmosim_energy": ([_vp, ctypes.POINTER(_d), ctypes.POINTER(_d)], _i),
     "cosmosim_launch_count": ([_vp], ctypes.c_int64),
     "csg_measure_fp_peaks": ([ctypes.POINTER(_d), ctypes.POINTER(_d)], _i),
+    "cosmosim_enable_graphs": ([_vp, _i], _i),
     "csg_direct_forces_noalloc": ([_vp, _vp, _vp, _vp, _i, _vp, _i, _d, _d, _vp, _vp], _i),
 }
 
@@ -242,6 +243,9 @@ class Sim:
 
     def set_precision(self, p):
         self._rc(self.lib.cosmosim_set_precision(self.h, p), "precision")
+
+    def enable_graphs(self, on=True):
+        self._rc(self.lib.cosmosim_enable_graphs(self.h, int(on)), "graphs")
 
     def enable_stats(self, on=True):
         self._rc(self.lib.cosmosim_enable_stats(self.h, int(on)), "stats")

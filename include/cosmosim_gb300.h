@@ -74,6 +74,10 @@ CSG_EXPORT SimHandle cosmosim_create_ex(CosmosimConfig config, double G, double 
 CSG_EXPORT int cosmosim_substeps_async(SimHandle handle, int k);
 CSG_EXPORT int cosmosim_sync(SimHandle handle);
 
+/* Substeps of a handle replay one captured CUDA graph per substep (default
+   on); off runs them as individual launches. */
+CSG_EXPORT int cosmosim_enable_graphs(SimHandle handle, int on);
+
 /* Runs the handle's work on the given cudaStream_t (NULL: its own stream). */
 CSG_EXPORT int cosmosim_set_stream(SimHandle handle, void *cuda_stream);
 

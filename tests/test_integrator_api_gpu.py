@@ -146,3 +146,19 @@ def test_fp32_mixed_handle_tracks_fp64(lib):
     assert np.median(dx) < 1e-9 and dx.max() < 1e-6
     r64.close()
     r32.close()
+
+
+def test_graph_replay_equals_direct_launches(lib):
+    """Substeps replayed from the captured CUDA graph are bit-identical to the
+    same substeps launched one kernel at a time (every kernel is deterministic)."""
+    b = lib.generate_ics(1, 20000, 8)
+    out = []
+    for graphs in (True, False):
+        s = lib.Sim.from_bodies(b, softening=0.01, theta=0.5, dt=1e-3, sph=True,
+                                precision=lib.PREC_FP32_MIXED)
+        s.enable_graphs(graphs)
+        s.substeps_async(4)
+        s.sync()
+        out.append(fields(s.bodies(), OUT))
+        s.close()
+    np.testing.assert_array_equal(out[0], out[1])
