@@ -181,140 +181,128 @@ __device__ __forceinline__ double inv_r3_q(double r2)
     return 1.0 / (r2 * sqrt(r2));
 }
 
-// FP64 walk with dense evaluation. The traversal is the FP32 one below (its
-// decisions equal the FP64 reference's, see k_walk32); accepted cells are
-// pushed into per-lane FIFO queues in shared memory and evaluated in FP64 in
-// batches where every lane has work, in the order they were accepted (the
-// reference's depth-first order). The FP64 pipe then does useful work on
-// (almost) every lane instead of once per traversal step for the few lanes
-// that interact at that step.
-constexpr int Q64 = 32; // queue slots per lane
-constexpr int F64 = 8;  // entries per lane per dense batch
+// ---- shared FP32 traversal -------------------------------------------------
+//
+// One step = one cell for the whole warp (the cell record is staged in a
+// per-warp shared-memory window, see load_cell). Decisions: FP32 with the difference
+// held to ~48 bits (hi/lo pairs); only when theta^2 d^2 lies within the FP32
+// error band of s^2 is the reference's FP64 test redone, out of line.
 
-// Evaluates the lane's next `count` queued cells (count >= 0; lanes without a
-// body pass 0 and never read their queue).
-__device__ __forceinline__ void q64_eval(const WalkArgs &a, const int *q, int lane, int &head,
-                                         int count, double px, double py, double pz,
-                                         double &sx, double &sy, double &sz)
+__device__ __noinline__ bool decide64(const WalkArgs &a, int cur, double px, double py, double pz)
 {
-    count = max(count, 0);
-    const int kmax = (int)__reduce_max_sync(0xffffffffu, (unsigned)count);
-    for (int s = 0; s < kmax; s++) {
-        if (s < count) {
-            const int node = q[((head + s) & (Q64 - 1)) * CSG_WARP + lane];
-            const double2 c01 = __ldg((const double2 *)&a.w64[node]);     // cx, cy
-            const double2 c23 = __ldg((const double2 *)&a.w64[node] + 1); // cz, m
-            const double4 c = make_double4(c01.x, c01.y, c23.x, c23.y);
-            const double dx = c.x - px, dy = c.y - py, dz = c.z - pz;
-            const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, a.eps2)));
-            const double f = a.G * c.w * inv_r3_q(r2);
-            sx = fma(f, dx, sx);
-            sy = fma(f, dy, sy);
-            sz = fma(f, dz, sz);
-        }
-    }
-    head += count;
+    const NodeW64 e = a.w64[cur];
+    const double ex = e.cx - px, ey = e.cy - py, ez = e.cz - pz;
+    return accept64(e.s2, ex * ex + ey * ey + ez * ez, a);
 }
 
-template <bool STATS>
-__global__ void __launch_bounds__(WALK_THREADS) k_walk64q(WalkArgs a)
+struct BodyPos {
+    double px, py, pz;
+    float hx, hy, hz, lx, ly, lz;
+};
+
+__device__ __forceinline__ BodyPos body_pos(const WalkArgs &a, int me, bool valid)
 {
-    __shared__ NodeW32 win_all[WALK_WARPS][CSG_WARP];
-    __shared__ int q_all[WALK_WARPS][Q64 * CSG_WARP];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    NodeW32 *win = win_all[warp];
-    int *q = q_all[warp];
-    const int n_alive = a.sc->n_alive;
-    const long long p = (long long)blockIdx.x * WALK_THREADS + threadIdx.x;
-    const long long warp0 = p - lane;
-    if (warp0 >= n_alive)
-        return;
-    if (a.sc->n_nodes > a.node_cap || a.sc->n_nodes < 1)
-        return;
-    const int nn = a.sc->n_nodes;
-    const bool valid = p < n_alive;
-    const int me = valid ? a.perm[p] : -1;
-    const double px = valid ? a.x[me] : 0.0, py = valid ? a.y[me] : 0.0,
-                 pz = valid ? a.z[me] : 0.0;
-    const float hx = (float)px, hy = (float)py, hz = (float)pz;
-    const float lx = (float)(px - (double)hx), ly = (float)(py - (double)hy),
-                lz = (float)(pz - (double)hz);
-    double sx = 0.0, sy = 0.0, sz = 0.0;
-    int head = 0, tail = 0;
-    unsigned long long hits = 0;
+    BodyPos b;
+    b.px = valid ? a.x[me] : 0.0;
+    b.py = valid ? a.y[me] : 0.0;
+    b.pz = valid ? a.z[me] : 0.0;
+    b.hx = (float)b.px;
+    b.hy = (float)b.py;
+    b.hz = (float)b.pz;
+    b.lx = (float)(b.px - (double)b.hx);
+    b.ly = (float)(b.py - (double)b.hy);
+    b.lz = (float)(b.pz - (double)b.hz);
+    return b;
+}
+
+struct Cell {
+    float4 A; // hi centre of mass, mass
+    float4 B; // lo centre of mass, s^2
+    int next, body;
+};
+
+// The next 32 cells in preorder are staged per warp in shared memory with one
+// coalesced load and re-staged when the cursor leaves that window: the load
+// latency is paid once per window instead of on every step's critical path.
+__device__ __forceinline__ Cell load_cell(const WalkArgs &a, NodeW32 *win, int &wbase, int cur,
+                                          int nn)
+{
+    if (cur - wbase >= CSG_WARP) { // warp-uniform
+        const int lane = threadIdx.x & 31;
+        wbase = cur;
+        __syncwarp();
+        if (wbase + lane < nn)
+            win[lane] = a.w32[wbase + lane];
+        __syncwarp();
+    }
+    const float4 *w = (const float4 *)(win + (cur - wbase));
+    Cell c;
+    c.A = w[0];
+    c.B = w[1];
+    const int2 nb = *(const int2 *)(w + 2);
+    c.next = nb.x;
+    c.body = nb.y;
+    return c;
+}
+
+// Visits the preorder tree for the warp's 32 bodies; calls take(cell, dx, dy,
+// dz, d2, cur) (under a warp-uniform "some lane takes" branch) for every cell
+// the lane interacts with, in the reference's depth-first order; after(cur)
+// runs once per step for the whole warp. EMPTY: cells of zero mass may occur
+// (caller pools); the reference skips them with everything below.
+template <bool EMPTY, typename Take, typename After>
+__device__ __forceinline__ void walk_cells(const WalkArgs &a, NodeW32 *win, int nn, int me,
+                                           bool valid, const BodyPos &b, Take take_fn,
+                                           After after_fn)
+{
     int skip = valid ? 0 : INT_MAX;
     int cur = 0, wbase = INT_MIN / 2;
     while (cur < nn) {
-        if (cur - wbase >= CSG_WARP) {
-            wbase = cur;
-            __syncwarp();
-            if (wbase + lane < nn)
-                win[lane] = a.w32[wbase + lane];
-            __syncwarp();
-        }
-        const NodeW32 c = win[cur - wbase];
-        bool open = false;
-        if (cur >= skip) {
-            if (c.m == 0.0f && a.w64[cur].m == 0.0) {
-                skip = c.next;
-            } else {
-                bool take;
-                if (c.body >= 0) {
-                    take = (c.body != me);
-                } else {
-                    const float dx = (c.cx - hx) + (c.lx - lx);
-                    const float dy = (c.cy - hy) + (c.ly - ly);
-                    const float dz = (c.cz - hz) + (c.lz - lz);
-                    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    const float lhs = a.theta2f * d2;
-                    const float band = c.s2 * a.guard_rel;
-                    if (c.s2 < lhs - band && d2 > 0.f) {
-                        take = true;
-                    } else if (c.s2 > lhs + band) {
-                        take = false;
-                    } else {
-                        const NodeW64 e = a.w64[cur];
-                        const double ex = e.cx - px, ey = e.cy - py, ez = e.cz - pz;
-                        take = accept64(e.s2, ex * ex + ey * ey + ez * ez, a);
-                    }
-                    if (take)
-                        skip = c.next;
-                    else
-                        open = true;
+        const Cell c = load_cell(a, win, wbase, cur, nn);
+        const bool active = cur >= skip;
+        bool take = false, open = false;
+        if (EMPTY && c.A.w == 0.0f && __any_sync(0xffffffffu, active)) {
+            if (a.w64[cur].m == 0.0) { // empty cell (src/octree.c:181-182)
+                if (active)
+                    skip = c.next;
+                after_fn(cur);
+                if (c.next <= cur) {
+                    dev_fail(a.sc, CSG_ERR_WALK_LIMIT);
+                    break;
                 }
-                if (take) {
-                    q[(tail & (Q64 - 1)) * CSG_WARP + lane] = cur;
-                    tail++;
-                    if (STATS)
-                        hits++;
-                }
+                cur = c.next;
+                continue;
             }
         }
-        const int cnt = tail - head; // 0..Q64-1; always 0 for a lane without a body
-        const int cmin = (int)__reduce_min_sync(0xffffffffu, (unsigned)(valid ? cnt : INT_MAX));
-        const int cmax = (int)__reduce_max_sync(0xffffffffu, (unsigned)cnt);
-        if (cmin >= F64)
-            q64_eval(a, q, lane, head, valid ? F64 : 0, px, py, pz, sx, sy, sz);
-        else if (cmax >= Q64 - 1) // a lane is about to overflow: drain what is there
-            q64_eval(a, q, lane, head, min(cnt, F64), px, py, pz, sx, sy, sz);
+        const float dx = (c.A.x - b.hx) + (c.B.x - b.lx);
+        const float dy = (c.A.y - b.hy) + (c.B.y - b.ly);
+        const float dz = (c.A.z - b.hz) + (c.B.z - b.lz);
+        const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        if (c.body >= 0) { // leaf (warp-uniform)
+            take = active && c.body != me;
+        } else {
+            const float lhs = a.theta2f * d2;
+            const float band = c.B.w * a.guard_rel;
+            bool acc = (c.B.w < lhs - band) && d2 > 0.f;
+            const bool amb = active && !acc && !(c.B.w > lhs + band);
+            if (__any_sync(0xffffffffu, amb)) {
+                if (amb)
+                    acc = decide64(a, cur, b.px, b.py, b.pz);
+            }
+            take = active && acc;
+            open = active && !acc;
+            if (take)
+                skip = c.next;
+        }
+        if (__any_sync(0xffffffffu, take))
+            take_fn(take, c, dx, dy, dz, d2, cur);
+        after_fn(cur);
         const int nxt = __any_sync(0xffffffffu, open) ? cur + 1 : c.next;
-        if (nxt <= cur) {
+        if (nxt <= cur) { // a malformed tree must not loop
             dev_fail(a.sc, CSG_ERR_WALK_LIMIT);
             break;
         }
         cur = nxt;
-    }
-    while (__any_sync(0xffffffffu, tail - head > 0))
-        q64_eval(a, q, lane, head, min(tail - head, F64), px, py, pz, sx, sy, sz);
-    if (valid) {
-        a.ax[me] = sx;
-        a.ay[me] = sy;
-        a.az[me] = sz;
-    }
-    if (STATS) {
-        unsigned int hsum = __reduce_add_sync(0xffffffffu, (unsigned int)hits);
-        if (lane == 0)
-            atomicAdd(&a.sc->interactions, (unsigned long long)hsum);
     }
 }
 
@@ -326,7 +314,10 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v)
     s = t;
 }
 
-template <bool STATS>
+// FP32-mixed walk: pair terms in FP32 from ~48-bit position differences,
+// summed per lane in blocks of up to 8 terms that are added with Kahan
+// compensation (per-body compensated FP32 summation); G applied once.
+template <bool STATS, bool EMPTY>
 __global__ void __launch_bounds__(WALK_THREADS) k_walk32(WalkArgs a)
 {
     __shared__ NodeW32 win_all[WALK_WARPS][CSG_WARP];
@@ -348,6 +339,8 @@ __global__ void __launch_bounds__(WALK_THREADS) k_walk32(WalkArgs a)
     const float lx = (float)(px - (double)hx), ly = (float)(py - (double)hy),
                 lz = (float)(pz - (double)hz);
     float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+    float bx = 0.f, by = 0.f, bz = 0.f; // current block of up to 8 terms
+    int nblk = 0;
     unsigned long long hits = 0;
     int skip = valid ? 0 : INT_MAX;
     int cur = 0, wbase = INT_MIN / 2;
@@ -362,8 +355,8 @@ __global__ void __launch_bounds__(WALK_THREADS) k_walk32(WalkArgs a)
         const NodeW32 c = win[cur - wbase];
         bool open = false;
         if (cur >= skip) {
-            if (c.m == 0.0f && a.w64[cur].m == 0.0) {
-                skip = c.next;
+            if (EMPTY && c.m == 0.0f && a.w64[cur].m == 0.0) {
+                skip = c.next; // empty cell of a caller pool (src/octree.c:181-182)
             } else {
                 const float dx = (c.cx - hx) + (c.lx - lx);
                 const float dy = (c.cy - hy) + (c.ly - ly);
@@ -380,10 +373,8 @@ __global__ void __launch_bounds__(WALK_THREADS) k_walk32(WalkArgs a)
                         take = true;
                     } else if (c.s2 > lhs + band) {
                         take = false;
-                    } else {
-                        const NodeW64 e = a.w64[cur];
-                        const double ex = e.cx - px, ey = e.cy - py, ez = e.cz - pz;
-                        take = accept64(e.s2, ex * ex + ey * ey + ez * ez, a);
+                    } else { // rare: decided by the reference's FP64 test, out of line
+                        take = decide64(a, cur, px, py, pz);
                     }
                     if (take)
                         skip = c.next;
@@ -392,10 +383,17 @@ __global__ void __launch_bounds__(WALK_THREADS) k_walk32(WalkArgs a)
                 }
                 if (take) {
                     const float y = rsqrtf(d2 + a.eps2f);
-                    const float f = a.Gf * c.m * (y * y * y);
-                    kahan_add(sx, cx, f * dx);
-                    kahan_add(sy, cy, f * dy);
-                    kahan_add(sz, cz, f * dz);
+                    const float f = c.m * (y * y * y);
+                    bx = fmaf(f, dx, bx);
+                    by = fmaf(f, dy, by);
+                    bz = fmaf(f, dz, bz);
+                    if (++nblk == 8) { // compensated add of the block
+                        kahan_add(sx, cx, bx);
+                        kahan_add(sy, cy, by);
+                        kahan_add(sz, cz, bz);
+                        bx = by = bz = 0.f;
+                        nblk = 0;
+                    }
                     if (STATS)
                         hits++;
                 }
@@ -408,15 +406,104 @@ __global__ void __launch_bounds__(WALK_THREADS) k_walk32(WalkArgs a)
         }
         cur = nxt;
     }
+    kahan_add(sx, cx, bx);
+    kahan_add(sy, cy, by);
+    kahan_add(sz, cz, bz);
     if (valid) {
-        a.ax[me] = (double)sx + (double)(-cx);
-        a.ay[me] = (double)sy + (double)(-cy);
-        a.az[me] = (double)sz + (double)(-cz);
+        a.ax[me] = a.G * ((double)sx - (double)cx);
+        a.ay[me] = a.G * ((double)sy - (double)cy);
+        a.az[me] = a.G * ((double)sz - (double)cz);
     }
     if (STATS) {
         unsigned int h = __reduce_add_sync(0xffffffffu, (unsigned int)hits);
         if (lane == 0)
             atomicAdd(&a.sc->interactions, (unsigned long long)h);
+    }
+}
+
+// FP64 walk with dense evaluation. The traversal is walk_cells (decisions
+// equal the FP64 reference's); accepted cells are pushed into per-lane FIFO
+// queues in shared memory and evaluated in FP64 in batches where every lane
+// has work, in the order they were accepted (the reference's depth-first
+// order). The FP64 pipe then does useful work on (almost) every lane instead
+// of once per traversal step for the few lanes that interact at that step.
+constexpr int Q64 = 32; // queue slots per lane
+constexpr int F64 = 8;  // entries per lane per dense batch
+
+// Evaluates the lane's next `count` queued cells (count >= 0; lanes without a
+// body pass 0 and never read their queue).
+__device__ __forceinline__ void q64_eval(const WalkArgs &a, const int *q, int lane, int &head,
+                                         int count, double px, double py, double pz,
+                                         double &sx, double &sy, double &sz)
+{
+    count = max(count, 0);
+    const int kmax = (int)__reduce_max_sync(0xffffffffu, (unsigned)count);
+    for (int s = 0; s < kmax; s++) {
+        if (s < count) {
+            const int node = q[((head + s) & (Q64 - 1)) * CSG_WARP + lane];
+            const double2 c01 = __ldg((const double2 *)&a.w64[node]);     // cx, cy
+            const double2 c23 = __ldg((const double2 *)&a.w64[node] + 1); // cz, m
+            const double dx = c01.x - px, dy = c01.y - py, dz = c23.x - pz;
+            const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, a.eps2)));
+            const double f = c23.y * inv_r3_q(r2);
+            sx = fma(f, dx, sx);
+            sy = fma(f, dy, sy);
+            sz = fma(f, dz, sz);
+        }
+    }
+    head += count;
+}
+
+template <bool STATS, bool EMPTY>
+__global__ void __launch_bounds__(WALK_THREADS) k_walk64q(WalkArgs a)
+{
+    __shared__ int q_all[WALK_WARPS][Q64 * CSG_WARP];
+    __shared__ NodeW32 win_all[WALK_WARPS][CSG_WARP];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int *q = q_all[warp];
+    NodeW32 *win = win_all[warp];
+    const int n_alive = a.sc->n_alive;
+    const long long p = (long long)blockIdx.x * WALK_THREADS + threadIdx.x;
+    if (p - lane >= n_alive)
+        return;
+    if (a.sc->n_nodes > a.node_cap || a.sc->n_nodes < 1)
+        return;
+    const int nn = a.sc->n_nodes;
+    const bool valid = p < n_alive;
+    const int me = valid ? a.perm[p] : -1;
+    const BodyPos b = body_pos(a, me, valid);
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    int head = 0, tail = 0;
+    unsigned int hits = 0;
+    walk_cells<EMPTY>(a, win, nn, me, valid, b,
+        [&](bool take, const Cell &, float, float, float, float, int cur) {
+            if (take) {
+                q[(tail & (Q64 - 1)) * CSG_WARP + lane] = cur;
+                tail++;
+                if (STATS)
+                    hits++;
+            }
+        },
+        [&](int) {
+            const int cnt = tail - head; // 0..Q64-1; always 0 for a lane without a body
+            const int cmin = (int)__reduce_min_sync(0xffffffffu, (unsigned)(valid ? cnt : INT_MAX));
+            const int cmax = (int)__reduce_max_sync(0xffffffffu, (unsigned)cnt);
+            if (cmin >= F64)
+                q64_eval(a, q, lane, head, valid ? F64 : 0, b.px, b.py, b.pz, sx, sy, sz);
+            else if (cmax >= Q64 - 1) // a lane is about to overflow: drain what is there
+                q64_eval(a, q, lane, head, min(cnt, F64), b.px, b.py, b.pz, sx, sy, sz);
+        });
+    while (__any_sync(0xffffffffu, tail - head > 0))
+        q64_eval(a, q, lane, head, min(tail - head, F64), b.px, b.py, b.pz, sx, sy, sz);
+    if (valid) {
+        a.ax[me] = a.G * sx;
+        a.ay[me] = a.G * sy;
+        a.az[me] = a.G * sz;
+    }
+    if (STATS) {
+        unsigned int hsum = __reduce_add_sync(0xffffffffu, hits);
+        if (lane == 0)
+            atomicAdd(&a.sc->interactions, (unsigned long long)hsum);
     }
 }
 
@@ -469,21 +556,32 @@ extern "C" int csgd_gravity_ex(csgd_t *d, const csgd_force_params *p, int exact)
     cudaStream_t s = d->stream;
     { k_zero_acc<<<csgd_grid(n, 256), 256, 0, s>>>(d->m, d->ax, d->ay, d->az, n); d->launches++; }
     const int g = csgd_grid(n, WALK_THREADS);
+    // trees built here have no empty cell below a non-empty root; a caller's
+    // pool may (the reference skips those cells)
+    const bool empty = d->imported != 0;
     if (p->precision == CSG_PREC_FP32_MIXED && !exact) {
-        if (d->stats)
-            { k_walk32<true><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
+        if (d->stats && empty)
+            { k_walk32<true, true><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
+        else if (d->stats)
+            { k_walk32<true, false><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
+        else if (empty)
+            { k_walk32<false, true><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
         else
-            { k_walk32<false><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
+            { k_walk32<false, false><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
     } else if (exact) {
         if (d->stats)
             { k_walk64<true, true><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
         else
             { k_walk64<true, false><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
     } else {
-        if (d->stats)
-            { k_walk64q<true><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
+        if (d->stats && empty)
+            { k_walk64q<true, true><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
+        else if (d->stats)
+            { k_walk64q<true, false><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
+        else if (empty)
+            { k_walk64q<false, true><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
         else
-            { k_walk64q<false><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
+            { k_walk64q<false, false><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
     }
     return csgd_check(d, cudaGetLastError());
 }
