@@ -111,6 +111,7 @@ struct csgd {
     int *gas;          // gas bodies in key order (caller indices)
     int *nb;           // SPH neighbour lists, 128 slots x cap (slot-major)
     int *nb_count;
+    double *pr2, *cs; // SPH per-body force terms
     int nb_cap;
 
     // nodes

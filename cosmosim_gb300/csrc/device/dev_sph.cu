@@ -65,6 +65,7 @@ struct SphArgs {
     DevScalars *sc;
     int *nb;       // neighbour lists, slot-major
     int *nb_count; // neighbours per gas body
+    double *pr2, *cs; // per-body force terms (k_sph_body_terms)
     int n, node_cap, stride;
 };
 
@@ -250,6 +251,21 @@ __global__ void __launch_bounds__(SPH_THREADS) k_sph_density_pairs(SphArgs a)
     a.P[i] = (GAMMA - 1.0) * rho * u;
 }
 
+// Per-body terms of the force pass: P/(rho^2 + 1e-15) and the sound speed
+// sqrt(gamma P/(rho + 1e-15)) (src/sph.c:112, :153-154, :170-171). The pair
+// loop needs them for both bodies of every pair; computing them once per body
+// gives the same values as the reference's per-pair evaluation.
+__global__ void __launch_bounds__(SPH_THREADS) k_sph_body_terms(SphArgs a)
+{
+    const int k = blockIdx.x * SPH_THREADS + threadIdx.x;
+    if (k >= a.sc->n_gas)
+        return;
+    const int j = a.gas[k];
+    const double rho = a.rho[j], P = a.P[j];
+    a.pr2[j] = P / (rho * rho + 1e-15);
+    a.cs[j] = sqrt(GAMMA * P / (rho + 1e-15));
+}
+
 // Pressure gradient + Monaghan viscosity over the recorded list,
 // src/sph.c:101-196.
 __global__ void __launch_bounds__(SPH_THREADS) k_sph_forces_pairs(SphArgs a)
@@ -261,8 +277,8 @@ __global__ void __launch_bounds__(SPH_THREADS) k_sph_forces_pairs(SphArgs a)
     const double qx = a.x[i], qy = a.y[i], qz = a.z[i];
     const double h_i = a.h[i];
     const double rho_i = a.rho[i];
-    const double P_i = a.P[i];
-    const double c_i = sqrt(GAMMA * P_i / (rho_i + 1e-15));
+    const double c_i = a.cs[i];
+    const double pr2_i = a.pr2[i];
     const double vxi = a.vx[i], vyi = a.vy[i], vzi = a.vz[i];
     const int nn = a.nb_count[k];
     const int *lst = a.nb + k;
@@ -280,7 +296,6 @@ __global__ void __launch_bounds__(SPH_THREADS) k_sph_forces_pairs(SphArgs a)
             continue;
         double h_avg = 0.5 * (h_i + a.h[j]);
         double rho_j = a.rho[j];
-        double P_j = a.P[j];
         double dvx = vxi - a.vx[j];
         double dvy = vyi - a.vy[j];
         double dvz = vzi - a.vz[j];
@@ -288,8 +303,7 @@ __global__ void __launch_bounds__(SPH_THREADS) k_sph_forces_pairs(SphArgs a)
         double visc = 0.0;
         if (vr < 0.0) {
             double mu = h_avg * vr / (r * r + 0.01 * h_avg * h_avg);
-            double c_j = sqrt(GAMMA * P_j / (rho_j + 1e-15));
-            double c_avg = 0.5 * (c_i + c_j);
+            double c_avg = 0.5 * (c_i + a.cs[j]);
             double rho_avg = 0.5 * (rho_i + rho_j);
             visc = (-1.0 * c_avg * mu + 2.0 * mu * mu) / (rho_avg + 1e-15);
         }
@@ -297,7 +311,7 @@ __global__ void __launch_bounds__(SPH_THREADS) k_sph_forces_pairs(SphArgs a)
         double gx = g * dx / r;
         double gy = g * dy / r;
         double gz = g * dz / r;
-        double f = a.m[j] * (P_i / (rho_i * rho_i + 1e-15) + P_j / (rho_j * rho_j + 1e-15) + visc);
+        double f = a.m[j] * (pr2_i + a.pr2[j] + visc);
         sx -= f * gx;
         sy -= f * gy;
         sz -= f * gz;
@@ -398,6 +412,8 @@ SphArgs make_args(csgd_t *d)
     a.sc = d->sc;
     a.nb = d->nb;
     a.nb_count = d->nb_count;
+    a.pr2 = d->pr2;
+    a.cs = d->cs;
     a.n = d->n;
     a.node_cap = d->node_cap;
     a.stride = d->cap;
@@ -459,11 +475,18 @@ static int ensure_lists(csgd_t *d)
         cudaFree(d->nb);
     if (d->nb_count)
         cudaFree(d->nb_count);
+    if (d->pr2)
+        cudaFree(d->pr2);
+    if (d->cs)
+        cudaFree(d->cs);
     d->nb = nullptr;
     d->nb_count = nullptr;
+    d->pr2 = d->cs = nullptr;
     size_t c = (size_t)(d->cap > 0 ? d->cap : 1);
     if (cudaMalloc((void **)&d->nb, sizeof(int) * CSG_SPH_MAX_NEIGHBORS * c) != cudaSuccess ||
-        cudaMalloc((void **)&d->nb_count, sizeof(int) * c) != cudaSuccess) {
+        cudaMalloc((void **)&d->nb_count, sizeof(int) * c) != cudaSuccess ||
+        cudaMalloc((void **)&d->pr2, sizeof(double) * c) != cudaSuccess ||
+        cudaMalloc((void **)&d->cs, sizeof(double) * c) != cudaSuccess) {
         cudaGetLastError();
         csgd_set_err(d, CSG_ERR_NOMEM);
         return CSG_ERR_NOMEM;
@@ -492,8 +515,10 @@ static int sph_pass(csgd_t *d, int forces)
     if (gl > 152 * 16)
         gl = 152 * 16;
     { k_sph_lists<<<gl, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
-    if (forces)
+    if (forces) {
+        { k_sph_body_terms<<<g, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
         { k_sph_forces_pairs<<<g, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
+    }
     else
         { k_sph_density_pairs<<<g, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
     return csgd_check(d, cudaGetLastError());

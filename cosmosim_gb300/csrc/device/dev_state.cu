@@ -262,6 +262,10 @@ extern "C" void csgd_destroy(csgd_t *d)
         cudaFree(d->nb);
     if (d->nb_count)
         cudaFree(d->nb_count);
+    if (d->pr2)
+        cudaFree(d->pr2);
+    if (d->cs)
+        cudaFree(d->cs);
     if (d->sc)
         cudaFree(d->sc);
     if (d->sc_host)
