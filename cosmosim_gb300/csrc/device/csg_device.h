@@ -41,6 +41,24 @@ void *csgd_stream(csgd_t *d);
 int csgd_reserve(csgd_t *d, int n);
 int csgd_count(const csgd_t *d);
 
+/* Forest: the n bodies form n_sys independent systems, system g holding the
+   host_counts[g] bodies that follow those of systems 0..g-1 (caller order;
+   counts sum to n). Every system gets its own root cube and tree; walks never
+   cross systems. n_sys = 1 (the default, counts ignored) is one simulation.
+   SPH, pool export/import and neighbour queries need n_sys = 1. A later
+   csgd_reserve with another n returns to one system. */
+int csgd_set_systems(csgd_t *d, int n_sys, const int *host_counts);
+int csgd_system_count(const csgd_t *d);
+
+/* Walk launch shape (CsgWalkShape, cosmosim_gb300.h). */
+int csgd_set_walk_shape(csgd_t *d, const CsgWalkShape *w);
+void csgd_get_walk_shape(const csgd_t *d, CsgWalkShape *w);
+/* Times every candidate shape on the current tree (reps walks each, median)
+   and keeps the fastest; *out gets it, all[0..all_cap) every candidate with
+   its time, *n_all their number. Blocks; not inside a stream capture. */
+int csgd_autotune_walk(csgd_t *d, const csgd_force_params *p, int reps, CsgWalkShape *out,
+                       CsgWalkShape *all, int all_cap, int *n_all);
+
 /* Body array-of-structs <-> device SoA (host buffers may be pageable). */
 int csgd_upload_bodies(csgd_t *d, const Body *host, int n);
 int csgd_download_bodies(csgd_t *d, Body *host, int n);

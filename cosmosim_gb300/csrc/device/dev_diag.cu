@@ -1,6 +1,6 @@
 // dev_diag.cu — FP64 diagnostics and pipe-peak probes.
 //
-// Direct-sum accelerations of a body sample over all bodies (the formula of
+// Direct-sum accelerations of a body sample over all bodies of its system (the formula of
 // the reference's test helper, tests/test_physics.c:54-71) and the total
 // energy KE + softened PE (tests/test_physics.c:34-52), both in FP64. The
 // j range is split over blocks; each block writes its partial sums and a
@@ -19,17 +19,20 @@ constexpr int JCHUNKS = 64;   // j-range splits for the direct sum
 __global__ void __launch_bounds__(DT) k_direct(const double *__restrict__ x,
                                                const double *__restrict__ y,
                                                const double *__restrict__ z,
-                                               const double *__restrict__ m, int n,
+                                               const double *__restrict__ m,
+                                               const int *__restrict__ gid, int n,
                                                const int *__restrict__ idx, int ns, double G,
                                                double eps2, double *__restrict__ part)
 {
     __shared__ double sx[DT], sy[DT], sz[DT], sm[DT];
+    __shared__ int sg[DT];
     const int k = blockIdx.x * DT + threadIdx.x;
     const int chunk = blockIdx.y;
     const int per = (n + JCHUNKS - 1) / JCHUNKS;
     const int j0 = chunk * per, j1 = min(n, j0 + per);
     const int i = (k < ns) ? idx[k] : -1;
     const double xi = (i >= 0) ? x[i] : 0.0, yi = (i >= 0) ? y[i] : 0.0, zi = (i >= 0) ? z[i] : 0.0;
+    const int gi = (i >= 0) ? gid[i] : -1; // only bodies of the same system attract
     double ax = 0.0, ay = 0.0, az = 0.0;
     for (int t = j0; t < j1; t += DT) {
         const int j = t + threadIdx.x;
@@ -39,12 +42,13 @@ __global__ void __launch_bounds__(DT) k_direct(const double *__restrict__ x,
             sy[threadIdx.x] = y[j];
             sz[threadIdx.x] = z[j];
             sm[threadIdx.x] = (m[j] <= 0.0) ? 0.0 : m[j];
+            sg[threadIdx.x] = gid[j];
         }
         __syncthreads();
         const int cnt = min(DT, j1 - t);
         if (i >= 0) {
             for (int q = 0; q < cnt; q++) {
-                if (t + q == i)
+                if (t + q == i || sg[q] != gi)
                     continue;
                 double dx = sx[q] - xi, dy = sy[q] - yi, dz = sz[q] - zi;
                 double r2 = dx * dx + dy * dy + dz * dz + eps2;
@@ -82,13 +86,16 @@ __global__ void k_direct_sum(const double *__restrict__ part, int ns, double *__
 __global__ void __launch_bounds__(DT) k_potential_rows(const double *__restrict__ x,
                                                        const double *__restrict__ y,
                                                        const double *__restrict__ z,
-                                                       const double *__restrict__ m, int n,
+                                                       const double *__restrict__ m,
+                                                       const int *__restrict__ gid, int n,
                                                        double G, double eps2,
                                                        double *__restrict__ row)
 {
     __shared__ double sx[DT], sy[DT], sz[DT], sm[DT];
+    __shared__ int sg[DT];
     const int i = blockIdx.x * DT + threadIdx.x;
     const double xi = (i < n) ? x[i] : 0.0, yi = (i < n) ? y[i] : 0.0, zi = (i < n) ? z[i] : 0.0;
+    const int gi = (i < n) ? gid[i] : -1;
     const double mi = (i < n && m[i] > 0.0) ? m[i] : 0.0;
     double pe = 0.0;
     const int jstart = blockIdx.x * DT; // columns from the block's first row
@@ -100,12 +107,13 @@ __global__ void __launch_bounds__(DT) k_potential_rows(const double *__restrict_
             sy[threadIdx.x] = y[j];
             sz[threadIdx.x] = z[j];
             sm[threadIdx.x] = (m[j] > 0.0) ? m[j] : 0.0;
+            sg[threadIdx.x] = gid[j];
         }
         __syncthreads();
         const int cnt = min(DT, n - t);
         if (i < n) {
             for (int q = 0; q < cnt; q++) {
-                if (t + q <= i)
+                if (t + q <= i || sg[q] != gi)
                     continue;
                 double dx = sx[q] - xi, dy = sy[q] - yi, dz = sz[q] - zi;
                 double r = sqrt(dx * dx + dy * dy + dz * dz + eps2);
@@ -185,7 +193,7 @@ extern "C" int csgd_direct_forces(csgd_t *d, const int *host_idx, int ns, double
     if (e == cudaSuccess) {
         cudaMemcpyAsync(didx, host_idx, sizeof(int) * (size_t)ns, cudaMemcpyHostToDevice, d->stream);
         dim3 grid((ns + DT - 1) / DT, JCHUNKS);
-        { k_direct<<<grid, DT, 0, d->stream>>>(d->x, d->y, d->z, d->m, d->n, didx, ns, G, softening * softening, part); d->launches++; }
+        { k_direct<<<grid, DT, 0, d->stream>>>(d->x, d->y, d->z, d->m, d->gid, d->n, didx, ns, G, softening * softening, part); d->launches++; }
         { k_direct_sum<<<csgd_grid(ns, 256), 256, 0, d->stream>>>(part, ns, out); d->launches++; }
         cudaMemcpyAsync(host_out, out, sizeof(double) * 3 * (size_t)ns, cudaMemcpyDeviceToHost, d->stream);
         rc = csgd_sync(d);
@@ -208,7 +216,7 @@ extern "C" int csgd_energy(csgd_t *d, double G, double softening, double *ke, do
         e = cudaMalloc((void **)&out, 2 * sizeof(double));
     int rc = CSG_OK;
     if (e == cudaSuccess && n > 0) {
-        { k_potential_rows<<<csgd_grid(n, DT), DT, 0, d->stream>>>(d->x, d->y, d->z, d->m, n, G, softening * softening, row); d->launches++; }
+        { k_potential_rows<<<csgd_grid(n, DT), DT, 0, d->stream>>>(d->x, d->y, d->z, d->m, d->gid, n, G, softening * softening, row); d->launches++; }
         { k_energy_reduce<<<1, 1024, 0, d->stream>>>(row, d->m, d->vx, d->vy, d->vz, n, out); d->launches++; }
         double h[2] = {0.0, 0.0};
         cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, d->stream);

@@ -61,19 +61,38 @@ struct __align__(16) NodeLink {
     int count;  // number of bodies in the cell
 };
 
-// Per-build scalars kept on the device so that no step needs a host round trip.
-struct DevScalars {
+// One system of the forest (a single simulation is a forest of one): its
+// alive-body bounding box, root cube, key parameters, where its bodies sit in
+// the sorted order and where its cells sit in the preorder node array.
+struct DevRoot {
     unsigned long long omin[3], omax[3]; // order-preserving bbox encodings
     double c0[3];                        // root centre
     double hs0;                          // root half size
     double key_scale;                    // 2^20 / hs0 (fast key path)
     double key_tol;                      // fast-path guard, in key grid units
     int fast_keys;                       // 1 when the fast key path is safe
+    int n_alive;                         // alive bodies of this system
+    int first;                           // their first sorted position
+    int root;                            // preorder id of the root cell
+    int end;                             // one past the system's last cell
+    int pad;
+};
+
+// A walk task: up to 32 consecutive sorted bodies of one system (one warp).
+struct WalkTask {
+    int gal, pos0, count, pad;
+};
+
+// Per-build scalars kept on the device so that no step needs a host round trip.
+struct DevScalars {
+    int n_tasks;       // walk tasks of the current tree
+    int task_next;     // persistent walks: next task to take
     int n_alive;
     int n_nodes;
     int deep;                            // positions that share a 63-bit key
     int err;                             // first device error code (0 = none)
     int n_gas;
+    int pad0;
     unsigned long long interactions;     // walk statistics (when enabled)
     unsigned long long key_slow;         // bodies that took the exact key path
     int alive_count;                     // csgd_alive_count result
@@ -95,6 +114,20 @@ struct csgd {
     int *type;
     Body *aos;        // Body staging for host I/O
     OctreeNode *pool; // reference-layout staging for export/import
+
+    // forest: system id of every body (caller order) and of every sorted
+    // position; per-system roots; walk tasks
+    int n_gal;
+    int gal_cap;
+    int *gid, *sgid;
+    DevRoot *roots;
+    WalkTask *tasks;
+    int task_cap;
+    // walk launch shape: warps per block (4 or 8), task group (0 = one warp
+    // per task, else tasks taken from an atomic counter this many at a time)
+    // and, for the persistent form, blocks per SM
+    int walk_warps, walk_group, walk_bps;
+    int num_sms;
 
     // keys and sort
     unsigned long long *key, *key_alt;
@@ -143,6 +176,7 @@ struct csgd {
 
 // ---- helpers shared by the .cu files ----
 int csgd_check(csgd_t *d, cudaError_t e);
+void csgd_drop_graph(csgd_t *d); // destroys the captured substep (after a sync)
 void csgd_set_err(csgd_t *d, int code);
 int csgd_grid(long long n, int block);
 

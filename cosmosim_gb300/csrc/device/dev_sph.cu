@@ -497,6 +497,10 @@ static int ensure_lists(csgd_t *d)
 
 static int sph_pass(csgd_t *d, int forces)
 {
+    if (d->n_gal > 1) { // one system only (see csgd_set_systems)
+        csgd_set_err(d, CSG_ERR_UNSUPPORTED);
+        return CSG_ERR_UNSUPPORTED;
+    }
     if (d->n <= 0)
         return CSG_OK;
     if (!d->geometry_valid) {
@@ -533,6 +537,10 @@ extern "C" int csgd_sph_forces(csgd_t *d) { return sph_pass(d, 1); }
 extern "C" int csgd_find_neighbors(csgd_t *d, double cx, double cy, double cz, double radius,
                                    int *buf, int cap, int *count_out)
 {
+    if (d->n_gal > 1) { // one system only (see csgd_set_systems)
+        csgd_set_err(d, CSG_ERR_UNSUPPORTED);
+        return CSG_ERR_UNSUPPORTED;
+    }
     *count_out = 0;
     if (cap <= 0)
         return CSG_OK;

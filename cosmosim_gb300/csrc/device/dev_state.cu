@@ -143,7 +143,7 @@ void free_bodies(csgd_t *d)
                     d->perm_alt, d->ext, d->sort_hist, d->lcp, d->cnt, d->base, d->scan_tmp,
                     d->gas, d->w64, d->w32, d->link, d->geo, d->s32, d->child, d->nchild, d->ticket,
                     d->minidx, d->ord_key, d->ord_key_alt, d->ord_id, d->ord_id_alt, d->rank,
-                    d->pool};
+                    d->pool, d->gid, d->sgid, d->tasks};
     for (void *p : ptrs)
         if (p)
             cudaFree(p);
@@ -167,6 +167,9 @@ void free_bodies(csgd_t *d)
     d->ord_key = d->ord_key_alt = nullptr;
     d->ord_id = d->ord_id_alt = d->rank = nullptr;
     d->pool = nullptr;
+    d->gid = d->sgid = nullptr;
+    d->tasks = nullptr;
+    d->task_cap = 0;
     d->cap = 0;
     d->node_cap = 0;
 }
@@ -237,10 +240,25 @@ extern "C" csgd_t *csgd_create(void)
     }
     d->stream = d->own_stream;
     d->use_graphs = 1;
+    d->n_gal = 1;
+    d->walk_warps = 8;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0)
+        d->num_sms = sms;
+    else
+        d->num_sms = 152;
+    d->gal_cap = 1;
+    if (cudaMalloc((void **)&d->roots, sizeof(DevRoot)) != cudaSuccess) {
+        cudaStreamDestroy(d->own_stream);
+        free(d);
+        return nullptr;
+    }
     if (cudaMalloc((void **)&d->sc, sizeof(DevScalars)) != cudaSuccess ||
         cudaMallocHost((void **)&d->sc_host, sizeof(DevScalars)) != cudaSuccess) {
         if (d->sc)
             cudaFree(d->sc);
+        cudaFree(d->roots);
         cudaStreamDestroy(d->own_stream);
         free(d);
         return nullptr;
@@ -268,6 +286,8 @@ extern "C" void csgd_destroy(csgd_t *d)
         cudaFree(d->cs);
     if (d->sc)
         cudaFree(d->sc);
+    if (d->roots)
+        cudaFree(d->roots);
     if (d->sc_host)
         cudaFreeHost(d->sc_host);
     if (d->own_stream)
@@ -294,20 +314,32 @@ extern "C" void csgd_enable_stats(csgd_t *d, int on)
     d->stats = on;
 }
 
+void csgd_drop_graph(csgd_t *d)
+{
+    if (d->graph) {
+        cudaStreamSynchronize(d->stream);
+        cudaGraphExecDestroy(d->graph);
+        d->graph = nullptr;
+    }
+}
+
 extern "C" int csgd_reserve(csgd_t *d, int n)
 {
     if (n < 0) {
         csgd_set_err(d, CSG_ERR_BAD_ARG);
         return CSG_ERR_BAD_ARG;
     }
+    if (n != d->n && d->n_gal > 1) { // the system layout no longer fits: one system
+        csgd_drop_graph(d);
+        d->n_gal = 1;
+        if (d->gid)
+            cudaMemsetAsync(d->gid, 0, sizeof(int) * (size_t)d->cap, d->stream);
+    }
     d->n = n;
     if (n <= d->cap && d->cap > 0)
         return CSG_OK;
     cudaStreamSynchronize(d->stream);
-    if (d->graph) { // captured pointers are about to change
-        cudaGraphExecDestroy(d->graph);
-        d->graph = nullptr;
-    }
+    csgd_drop_graph(d); // captured pointers are about to change
     free_bodies(d);
     const size_t cap = (size_t)(n > 0 ? n : 1);
     const size_t ncap = 8 * cap + 64; // the reference's pool contract
@@ -359,6 +391,10 @@ extern "C" int csgd_reserve(csgd_t *d, int n)
     ok &= dalloc(&d->ord_id_alt, ncap) == cudaSuccess;
     ok &= dalloc(&d->rank, ncap) == cudaSuccess;
     ok &= dalloc(&d->pool, ncap) == cudaSuccess;
+    ok &= dalloc(&d->gid, cap) == cudaSuccess;
+    ok &= dalloc(&d->sgid, cap) == cudaSuccess;
+    const size_t tcap = cap / CSG_WARP + (size_t)d->gal_cap + 2; // >= tasks of any layout
+    ok &= dalloc(&d->tasks, tcap) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
         free_bodies(d);
@@ -368,11 +404,82 @@ extern "C" int csgd_reserve(csgd_t *d, int n)
     }
     d->cap = (int)cap;
     d->node_cap = (int)ncap;
+    d->task_cap = (int)tcap;
     d->n = n;
+    d->n_gal = 1;
+    cudaMemsetAsync(d->gid, 0, sizeof(int) * cap, d->stream);
     // the tree stays empty-but-valid until the first build
     cudaMemsetAsync(d->sc, 0, sizeof(DevScalars), d->stream);
     return csgd_check(d, cudaGetLastError());
 }
+
+// ---- forests ---------------------------------------------------------------
+
+extern "C" int csgd_set_systems(csgd_t *d, int n_sys, const int *host_counts)
+{
+    if (n_sys < 1 || n_sys > CSG_MAX_SYSTEMS || (n_sys > 1 && !host_counts)) {
+        csgd_set_err(d, CSG_ERR_BAD_ARG);
+        return CSG_ERR_BAD_ARG;
+    }
+    long long total = 0;
+    for (int g = 0; n_sys > 1 && g < n_sys; g++) {
+        if (host_counts[g] < 0) {
+            csgd_set_err(d, CSG_ERR_BAD_ARG);
+            return CSG_ERR_BAD_ARG;
+        }
+        total += host_counts[g];
+    }
+    if (n_sys > 1 && total != d->n) {
+        csgd_set_err(d, CSG_ERR_BAD_ARG);
+        return CSG_ERR_BAD_ARG;
+    }
+    csgd_drop_graph(d); // grid shapes and the system pass change
+    if (n_sys > d->gal_cap || (size_t)(d->cap / CSG_WARP) + n_sys + 2 > (size_t)d->task_cap) {
+        cudaStreamSynchronize(d->stream);
+        DevRoot *r = nullptr;
+        WalkTask *t = nullptr;
+        const size_t tcap = (size_t)(d->cap > 0 ? d->cap : 1) / CSG_WARP + (size_t)n_sys + 2;
+        if (dalloc(&r, (size_t)n_sys) != cudaSuccess || dalloc(&t, tcap) != cudaSuccess) {
+            cudaGetLastError();
+            if (r)
+                cudaFree(r);
+            csgd_set_err(d, CSG_ERR_NOMEM);
+            return CSG_ERR_NOMEM;
+        }
+        cudaFree(d->roots);
+        if (d->tasks)
+            cudaFree(d->tasks);
+        d->roots = r;
+        d->tasks = t;
+        d->gal_cap = n_sys;
+        d->task_cap = (int)tcap;
+    }
+    d->n_gal = n_sys;
+    d->geometry_valid = 0;
+    d->gas_valid = 0;
+    if (d->n == 0 || !d->gid)
+        return csgd_check(d, cudaGetLastError());
+    if (n_sys == 1) {
+        cudaMemsetAsync(d->gid, 0, sizeof(int) * (size_t)d->n, d->stream);
+        return csgd_check(d, cudaGetLastError());
+    }
+    int *h = (int *)malloc(sizeof(int) * (size_t)d->n);
+    if (!h) {
+        csgd_set_err(d, CSG_ERR_NOMEM);
+        return CSG_ERR_NOMEM;
+    }
+    for (int g = 0, i = 0; g < n_sys; g++)
+        for (int k = 0; k < host_counts[g]; k++)
+            h[i++] = g;
+    cudaError_t e = cudaMemcpyAsync(d->gid, h, sizeof(int) * (size_t)d->n, cudaMemcpyHostToDevice,
+                                    d->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(d->stream); // h is pageable and freed next
+    free(h);
+    return csgd_check(d, e);
+}
+
+extern "C" int csgd_system_count(const csgd_t *d) { return d->n_gal; }
 
 // ---- host I/O --------------------------------------------------------------
 

@@ -77,10 +77,10 @@ __device__ __forceinline__ int descend_one(double px, double py, double pz, doub
 
 // Digits of levels [l0, l0+nl) packed most-significant-first, after descending
 // l0 levels; also returns the cube reached.
-__device__ unsigned long long exact_digits(double px, double py, double pz, const DevScalars *sc,
+__device__ unsigned long long exact_digits(double px, double py, double pz, const DevRoot *r,
                                            int l0, int nl)
 {
-    double cx = sc->c0[0], cy = sc->c0[1], cz = sc->c0[2], hs = sc->hs0;
+    double cx = r->c0[0], cy = r->c0[1], cz = r->c0[2], hs = r->hs0;
     for (int l = 0; l < l0; l++)
         descend_one(px, py, pz, cx, cy, cz, hs);
     unsigned long long k = 0;
@@ -91,10 +91,14 @@ __device__ unsigned long long exact_digits(double px, double py, double pz, cons
 
 __device__ __forceinline__ int clz_levels(unsigned long long x) { return (__clzll(x) - 1) / 3; }
 
-// Number of leading levels two sorted positions share (0..64).
+// Number of leading levels two sorted positions share (0..64); -1 when they
+// belong to different systems of a forest (no common cell).
 __device__ __forceinline__ int lcp_pos(const unsigned long long *__restrict__ key,
-                                       const unsigned long long *__restrict__ ext, int a, int b)
+                                       const unsigned long long *__restrict__ ext,
+                                       const int *__restrict__ sgid, int a, int b)
 {
+    if (sgid[a] != sgid[b])
+        return -1;
     unsigned long long ka = key[a], kb = key[b];
     if (ka != kb)
         return clz_levels(ka ^ kb);
@@ -121,16 +125,23 @@ __device__ __forceinline__ int digit_at(const unsigned long long *__restrict__ k
 
 // ---- 1. bbox -----------------------------------------------------------
 
-__global__ void k_reset(DevScalars *sc)
+__global__ void k_reset(DevScalars *sc, DevRoot *roots, int n_gal)
 {
-    for (int a = 0; a < 3; a++) {
-        sc->omin[a] = ~0ull;
-        sc->omax[a] = 0ull;
+    for (int g = threadIdx.x; g < n_gal; g += blockDim.x) {
+        for (int a = 0; a < 3; a++) {
+            roots[g].omin[a] = ~0ull;
+            roots[g].omax[a] = 0ull;
+        }
+        roots[g].n_alive = 0;
     }
-    sc->n_alive = 0;
-    sc->deep = 0;
-    sc->n_gas = 0;
-    sc->key_slow = 0;
+    if (threadIdx.x == 0) {
+        sc->n_alive = 0;
+        sc->deep = 0;
+        sc->n_gas = 0;
+        sc->key_slow = 0;
+        sc->n_tasks = 0;
+        sc->task_next = 0;
+    }
 }
 
 __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v)
@@ -152,48 +163,63 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
 
 // Alive-body bbox (src/octree.c:118-139). NaN coordinates never win a
 // comparison in the reference, so they are left out here too.
+// One pass over the bodies; each warp reduces its lanes' boxes and counts
+// when its bodies belong to one system (the usual case: a system's bodies are
+// contiguous) and falls back to per-lane atomics at system boundaries.
 __global__ void k_bbox(const double *__restrict__ x, const double *__restrict__ y,
-                       const double *__restrict__ z, const double *__restrict__ m, int n,
-                       DevScalars *sc)
+                       const double *__restrict__ z, const double *__restrict__ m,
+                       const int *__restrict__ gid, int n, DevRoot *roots)
 {
-    unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
-    int cnt = 0;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x) {
-        if (!is_alive(m[i]))
-            continue;
-        cnt++;
-        double p[3] = {x[i], y[i], z[i]};
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
+         base += (long long)gridDim.x * blockDim.x) {
+        const long long i = base + threadIdx.x;
+        unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
+        int cnt = 0;
+        const int g = (i < n) ? gid[i] : -1;
+        if (i < n && is_alive(m[i])) {
+            cnt = 1;
+            double p[3] = {x[i], y[i], z[i]};
 #pragma unroll
-        for (int a = 0; a < 3; a++) {
-            if (p[a] != p[a])
-                continue;
-            unsigned long long e = ord_enc(p[a]);
-            lo[a] = e < lo[a] ? e : lo[a];
-            hi[a] = e > hi[a] ? e : hi[a];
+            for (int a = 0; a < 3; a++) {
+                if (p[a] != p[a])
+                    continue;
+                lo[a] = hi[a] = ord_enc(p[a]);
+            }
         }
-    }
+        const int g0 = __shfl_sync(0xffffffffu, g, 0);
+        if (__all_sync(0xffffffffu, g == g0 || g < 0)) {
 #pragma unroll
-    for (int a = 0; a < 3; a++) {
-        lo[a] = warp_min_u64(lo[a]);
-        hi[a] = warp_max_u64(hi[a]);
-    }
-    for (int o = 16; o > 0; o >>= 1)
-        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    if ((threadIdx.x & 31) == 0) {
-        for (int a = 0; a < 3; a++) {
-            if (lo[a] != ~0ull)
-                atomicMin(&sc->omin[a], lo[a]);
-            if (hi[a] != 0ull)
-                atomicMax(&sc->omax[a], hi[a]);
+            for (int a = 0; a < 3; a++) {
+                lo[a] = warp_min_u64(lo[a]);
+                hi[a] = warp_max_u64(hi[a]);
+            }
+            for (int o = 16; o > 0; o >>= 1)
+                cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+            if ((threadIdx.x & 31) == 0 && g0 >= 0) {
+                for (int a = 0; a < 3; a++) {
+                    if (lo[a] != ~0ull)
+                        atomicMin(&roots[g0].omin[a], lo[a]);
+                    if (hi[a] != 0ull)
+                        atomicMax(&roots[g0].omax[a], hi[a]);
+                }
+                if (cnt)
+                    atomicAdd(&roots[g0].n_alive, cnt);
+            }
+        } else if (g >= 0) {
+            for (int a = 0; a < 3; a++) {
+                if (lo[a] != ~0ull)
+                    atomicMin(&roots[g].omin[a], lo[a]);
+                if (hi[a] != 0ull)
+                    atomicMax(&roots[g].omax[a], hi[a]);
+            }
+            if (cnt)
+                atomicAdd(&roots[g].n_alive, cnt);
         }
-        if (cnt)
-            atomicAdd(&sc->n_alive, cnt);
     }
 }
 
 // Root cube, reference src/octree.c:141-159, plus the fast-key parameters.
-__global__ void k_root(DevScalars *sc)
+__device__ void root_cube(DevRoot *sc)
 {
     if (sc->n_alive == 0) {
         sc->c0[0] = sc->c0[1] = sc->c0[2] = 0.0;
@@ -231,6 +257,24 @@ __global__ void k_root(DevScalars *sc)
     sc->key_scale = finite ? 1048576.0 / hs : 0.0;
 }
 
+// Root cube of every system, then where each system's alive bodies start in
+// the sorted order (systems sort in id order) and the total alive count.
+__global__ void k_root(DevScalars *sc, DevRoot *roots, int n_gal)
+{
+    for (int g = threadIdx.x; g < n_gal; g += blockDim.x)
+        root_cube(&roots[g]);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int off = 0;
+        for (int g = 0; g < n_gal; g++) {
+            roots[g].first = off;
+            roots[g].root = roots[g].end = 0;
+            off += roots[g].n_alive;
+        }
+        sc->n_alive = off;
+    }
+}
+
 // ---- 2. keys -----------------------------------------------------------
 
 __device__ __forceinline__ bool fast_coord(double p, double c, double scale, double tol, int &i)
@@ -246,8 +290,9 @@ __device__ __forceinline__ bool fast_coord(double p, double c, double scale, dou
 }
 
 __global__ void k_keys(const double *__restrict__ x, const double *__restrict__ y,
-                       const double *__restrict__ z, const double *__restrict__ m, int n,
-                       DevScalars *sc, unsigned long long *__restrict__ key,
+                       const double *__restrict__ z, const double *__restrict__ m,
+                       const int *__restrict__ gid, int n, DevScalars *gsc,
+                       const DevRoot *__restrict__ roots, unsigned long long *__restrict__ key,
                        int *__restrict__ perm)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -258,6 +303,7 @@ __global__ void k_keys(const double *__restrict__ x, const double *__restrict__ 
         key[i] = CSG_DEAD_KEY;
         return;
     }
+    const DevRoot *sc = &roots[gid[i]];
     const double px = x[i], py = y[i], pz = z[i];
     int ix, iy, iz;
     if (sc->fast_keys && fast_coord(px, sc->c0[0], sc->key_scale, sc->key_tol, ix) &&
@@ -270,29 +316,47 @@ __global__ void k_keys(const double *__restrict__ x, const double *__restrict__ 
         key[i] = spread3(sx) | (spread3(sy) << 1) | (spread3(sz) << 2);
     } else {
         key[i] = exact_digits(px, py, pz, sc, 0, 21);
-        atomicAdd(&sc->key_slow, 1ull);
+        atomicAdd(&gsc->key_slow, 1ull);
     }
 }
 
 // ---- 4. positions that share a 63-bit key ------------------------------
 
+// System of every sorted position (-1 past the alive bodies).
+__global__ void k_sgid(const DevScalars *sc, const int *__restrict__ perm,
+                       const int *__restrict__ gid, int *__restrict__ sgid, int n)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n)
+        sgid[p] = (p < sc->n_alive) ? gid[perm[p]] : -1;
+}
+
+__device__ __forceinline__ bool same_key(const unsigned long long *key, const int *sgid, int a,
+                                         int b)
+{
+    return key[a] == key[b] && sgid[a] == sgid[b];
+}
+
 __global__ void k_deep_mark(const double *__restrict__ x, const double *__restrict__ y,
                             const double *__restrict__ z, DevScalars *sc,
+                            const DevRoot *__restrict__ roots,
                             const unsigned long long *__restrict__ key,
-                            const int *__restrict__ perm, unsigned long long *__restrict__ ext)
+                            const int *__restrict__ sgid, const int *__restrict__ perm,
+                            unsigned long long *__restrict__ ext)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const int na = sc->n_alive;
     if (p >= na)
         return;
-    const unsigned long long k = key[p];
-    bool deep = (p > 0 && key[p - 1] == k) || (p + 1 < na && key[p + 1] == k);
+    bool deep = (p > 0 && same_key(key, sgid, p - 1, p)) ||
+                (p + 1 < na && same_key(key, sgid, p, p + 1));
     if (!deep)
         return;
     const int b = perm[p];
-    ext[3 * (size_t)p + 0] = exact_digits(x[b], y[b], z[b], sc, 21, 21);
-    ext[3 * (size_t)p + 1] = exact_digits(x[b], y[b], z[b], sc, 42, 21);
-    ext[3 * (size_t)p + 2] = exact_digits(x[b], y[b], z[b], sc, 63, 1);
+    const DevRoot *r = &roots[sgid[p]];
+    ext[3 * (size_t)p + 0] = exact_digits(x[b], y[b], z[b], r, 21, 21);
+    ext[3 * (size_t)p + 1] = exact_digits(x[b], y[b], z[b], r, 42, 21);
+    ext[3 * (size_t)p + 2] = exact_digits(x[b], y[b], z[b], r, 63, 1);
     atomicAdd(&sc->deep, 1);
 }
 
@@ -309,7 +373,8 @@ __device__ __forceinline__ bool ext_less(const unsigned long long *e, int a, int
 // Orders each run of equal 63-bit keys by its deeper digits; insertion sort is
 // stable, so equal full keys keep body index order.
 __global__ void k_deep_sort(DevScalars *sc, const unsigned long long *__restrict__ key,
-                            int *__restrict__ perm, unsigned long long *__restrict__ ext)
+                            const int *__restrict__ sgid, int *__restrict__ perm,
+                            unsigned long long *__restrict__ ext)
 {
     if (sc->deep == 0)
         return;
@@ -317,11 +382,10 @@ __global__ void k_deep_sort(DevScalars *sc, const unsigned long long *__restrict
     const int na = sc->n_alive;
     if (p >= na)
         return;
-    const unsigned long long k = key[p];
-    if (!(p + 1 < na && key[p + 1] == k) || (p > 0 && key[p - 1] == k))
+    if (!(p + 1 < na && same_key(key, sgid, p, p + 1)) || (p > 0 && same_key(key, sgid, p - 1, p)))
         return; // not the start of a run
     int e = p + 1;
-    while (e < na && key[e] == k)
+    while (e < na && same_key(key, sgid, p, e))
         e++;
     for (int i = p + 1; i < e; i++) {
         unsigned long long t0 = ext[3 * (size_t)i], t1 = ext[3 * (size_t)i + 1],
@@ -350,27 +414,27 @@ __global__ void k_deep_sort(DevScalars *sc, const unsigned long long *__restrict
 // ---- 5/6. cells ----------------------------------------------------------
 
 __global__ void k_count(DevScalars *sc, const unsigned long long *__restrict__ key,
-                        const unsigned long long *__restrict__ ext, signed char *__restrict__ lcp,
-                        int *__restrict__ cnt)
+                        const unsigned long long *__restrict__ ext, const int *__restrict__ sgid,
+                        signed char *__restrict__ lcp, int *__restrict__ cnt)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const int na = sc->n_alive;
     if (p >= na)
         return;
-    int P = (p > 0) ? lcp_pos(key, ext, p - 1, p) : -1;
-    int Q = (p + 1 < na) ? lcp_pos(key, ext, p, p + 1) : -1;
+    int P = (p > 0) ? lcp_pos(key, ext, sgid, p - 1, p) : -1;
+    int Q = (p + 1 < na) ? lcp_pos(key, ext, sgid, p, p + 1) : -1;
     lcp[p] = (signed char)Q;
     int internal = min(Q, CSG_MAX_LEVEL - 1) - P;
     cnt[p] = (internal > 0 ? internal : 0) + (P < CSG_MAX_LEVEL ? 1 : 0);
 }
 
-__device__ int search_hi(const unsigned long long *key, const unsigned long long *ext, int na,
-                         int p, int L)
+__device__ int search_hi(const unsigned long long *key, const unsigned long long *ext,
+                         const int *sgid, int na, int p, int L)
 {
     int q = p, step = 1;
     while (true) {
         int t = q + step;
-        if (t >= na || lcp_pos(key, ext, p, t) < L)
+        if (t >= na || lcp_pos(key, ext, sgid, p, t) < L)
             break;
         q = t;
         step <<= 1;
@@ -378,19 +442,19 @@ __device__ int search_hi(const unsigned long long *key, const unsigned long long
     while (step > 1) {
         step >>= 1;
         int t = q + step;
-        if (t < na && lcp_pos(key, ext, p, t) >= L)
+        if (t < na && lcp_pos(key, ext, sgid, p, t) >= L)
             q = t;
     }
     return q;
 }
 
-__device__ int search_lo(const unsigned long long *key, const unsigned long long *ext, int p,
-                         int L)
+__device__ int search_lo(const unsigned long long *key, const unsigned long long *ext,
+                         const int *sgid, int p, int L)
 {
     int q = p, step = 1;
     while (true) {
         int t = q - step;
-        if (t < 0 || lcp_pos(key, ext, t, p) < L)
+        if (t < 0 || lcp_pos(key, ext, sgid, t, p) < L)
             break;
         q = t;
         step <<= 1;
@@ -398,14 +462,14 @@ __device__ int search_lo(const unsigned long long *key, const unsigned long long
     while (step > 1) {
         step >>= 1;
         int t = q - step;
-        if (t >= 0 && lcp_pos(key, ext, t, p) >= L)
+        if (t >= 0 && lcp_pos(key, ext, sgid, t, p) >= L)
             q = t;
     }
     return q;
 }
 
 __device__ __forceinline__ int parent_id(const unsigned long long *key,
-                                         const unsigned long long *ext,
+                                         const unsigned long long *ext, const int *sgid,
                                          const signed char *lcp, const int *base, int p, int P,
                                          int L, int id)
 {
@@ -413,19 +477,20 @@ __device__ __forceinline__ int parent_id(const unsigned long long *key,
         return -1;
     if (L - 1 > P)
         return id - 1; // the cell one level up starts at p as well
-    int a = search_lo(key, ext, p, L - 1);
+    int a = search_lo(key, ext, sgid, p, L - 1);
     int Pa = (a > 0) ? (int)lcp[a - 1] : -1;
     return base[a] + (L - 1) - (Pa + 1);
 }
 
-__device__ __forceinline__ void write_cell(csgd_t dd, DevScalars *sc, int id, int parent, int L,
-                                           int first, int count, int next, int body)
+__device__ __forceinline__ void write_cell(csgd_t dd, DevScalars *sc, double hs0, int id,
+                                           int parent, int L, int first, int count, int next,
+                                           int body)
 {
     if (id >= dd.node_cap) {
         dev_fail(sc, CSG_ERR_NODE_CAPACITY);
         return;
     }
-    double hs = ldexp(sc->hs0, -L);
+    double hs = ldexp(hs0, -L);
     double s = 2.0 * hs;
     double s2 = s * s;
     NodeW64 w;
@@ -451,8 +516,9 @@ __device__ __forceinline__ void write_cell(csgd_t dd, DevScalars *sc, int id, in
     dd.ticket[id] = 0;
 }
 
-__global__ void k_nodes(csgd_t dd, DevScalars *sc, const unsigned long long *__restrict__ key,
-                        const unsigned long long *__restrict__ ext,
+__global__ void k_nodes(csgd_t dd, DevScalars *sc, const DevRoot *__restrict__ roots,
+                        const unsigned long long *__restrict__ key,
+                        const unsigned long long *__restrict__ ext, const int *__restrict__ sgid,
                         const signed char *__restrict__ lcp, const int *__restrict__ base,
                         const int *__restrict__ perm)
 {
@@ -464,26 +530,77 @@ __global__ void k_nodes(csgd_t dd, DevScalars *sc, const unsigned long long *__r
         if (total > dd.node_cap)
             dev_fail(sc, CSG_ERR_NODE_CAPACITY);
         if (na == 0) { // empty root, reference src/octree.c:141-144
-            write_cell(dd, sc, 0, -1, 0, 0, 0, 1, -1);
+            write_cell(dd, sc, 1.0, 0, -1, 0, 0, 0, 1, -1);
             return;
         }
     }
     if (p >= na)
         return;
+    const double hs0 = roots[sgid[p]].hs0;
     const int P = (p > 0) ? (int)lcp[p - 1] : -1;
     const int Q = (int)lcp[p];
     int id = base[p];
     const int Lhi = min(Q, CSG_MAX_LEVEL - 1);
     for (int L = P + 1; L <= Lhi; L++, id++) {
-        int hi = search_hi(key, ext, na, p, L);
-        int parent = parent_id(key, ext, lcp, base, p, P, L, id);
-        write_cell(dd, sc, id, parent, L, p, hi - p + 1, base[hi + 1], -1);
+        int hi = search_hi(key, ext, sgid, na, p, L);
+        int parent = parent_id(key, ext, sgid, lcp, base, p, P, L, id);
+        write_cell(dd, sc, hs0, id, parent, L, p, hi - p + 1, base[hi + 1], -1);
     }
     if (P < CSG_MAX_LEVEL) {
         int L = min(max(P, Q) + 1, CSG_MAX_LEVEL); // bodies equal to depth 64 share a leaf
-        int hi = (Q == CSG_MAX_LEVEL) ? search_hi(key, ext, na, p, CSG_MAX_LEVEL) : p;
-        int parent = parent_id(key, ext, lcp, base, p, P, L, id);
-        write_cell(dd, sc, id, parent, L, p, hi - p + 1, id + 1, perm[p]);
+        int hi = (Q == CSG_MAX_LEVEL) ? search_hi(key, ext, sgid, na, p, CSG_MAX_LEVEL) : p;
+        int parent = parent_id(key, ext, sgid, lcp, base, p, P, L, id);
+        write_cell(dd, sc, hs0, id, parent, L, p, hi - p + 1, id + 1, perm[p]);
+    }
+}
+
+// Root and end cell of every system, and the walk tasks: each system's
+// sorted bodies in groups of 32 (one warp each). For a tree imported from a
+// caller pool (one system) the root is cell 0 and the end the cell count.
+__global__ void k_tasks(DevScalars *sc, DevRoot *roots, int n_gal, const int *__restrict__ base,
+                        WalkTask *tasks, int task_cap, int imported)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        int t = 0;
+        for (int g = 0; g < n_gal; g++) {
+            DevRoot &r = roots[g];
+            if (imported) {
+                r.first = 0;
+                r.root = 0;
+                r.end = sc->n_nodes;
+            } else if (r.n_alive > 0) {
+                r.root = base[r.first];
+                r.end = base[r.first + r.n_alive];
+            } else {
+                r.root = r.end = 0;
+            }
+            t += (r.n_alive + 31) / 32;
+        }
+        if (t > task_cap) {
+            dev_fail(sc, CSG_ERR_NODE_CAPACITY);
+            t = task_cap;
+        }
+        sc->n_tasks = t;
+        sc->task_next = 0;
+    }
+    // every block fills the tasks of its systems (roots[].first and n_alive
+    // were final before this kernel)
+    for (int g = blockIdx.x; g < n_gal; g += gridDim.x) {
+        int t0 = 0;
+        for (int h = 0; h < g; h++) // systems are few; recompute the offset
+            t0 += (roots[h].n_alive + 31) / 32;
+        const int n = roots[g].n_alive;
+        const int first = imported ? 0 : roots[g].first;
+        for (int j = threadIdx.x; j * 32 < n; j += blockDim.x) {
+            if (t0 + j >= task_cap)
+                break;
+            WalkTask w;
+            w.gal = g;
+            w.pos0 = first + 32 * j;
+            w.count = min(32, n - 32 * j);
+            w.pad = 0;
+            tasks[t0 + j] = w;
+        }
     }
 }
 
@@ -624,14 +741,17 @@ __device__ __forceinline__ void write_s32(const csgd_t &dd, int id, double cx, d
 }
 
 // Geometric cube of every cell, with the reference's arithmetic.
-__global__ void k_geometry(csgd_t dd, DevScalars *sc, const unsigned long long *__restrict__ key,
-                           const unsigned long long *__restrict__ ext)
+__global__ void k_geometry(csgd_t dd, DevScalars *sc, const DevRoot *__restrict__ roots,
+                           const unsigned long long *__restrict__ key,
+                           const unsigned long long *__restrict__ ext,
+                           const int *__restrict__ sgid)
 {
     const int id = blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= min(sc->n_nodes, dd.node_cap) || sc->n_nodes > dd.node_cap)
         return;
     NodeLink l = dd.link[id];
-    double cx = sc->c0[0], cy = sc->c0[1], cz = sc->c0[2], hs = sc->hs0;
+    const DevRoot *r = &roots[sc->n_alive > 0 ? sgid[l.first] : 0];
+    double cx = r->c0[0], cy = r->c0[1], cz = r->c0[2], hs = r->hs0;
     for (int lev = 0; lev < l.level; lev++) {
         int q = digit_at(key, ext, l.first, lev);
         double ox = (q & 1) ? 0.5 : -0.5;
@@ -839,19 +959,69 @@ __global__ void k_imp_write(csgd_t dd, DevScalars *sc, int nn, int root,
 // ---- host side -------------------------------------------------------------
 
 // Steps 1-3: root cube, keys, sorted order of the alive bodies (n_alive).
+// Sort key of the system pass: the system of each key-sorted body (dead
+// bodies, already last, get the largest value).
+__global__ void k_gal_keys(const DevScalars *sc, const int *__restrict__ perm,
+                           const int *__restrict__ gid, unsigned long long *__restrict__ gk,
+                           int *__restrict__ idx, int n, int n_gal)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n)
+        return;
+    gk[p] = (p < sc->n_alive) ? (unsigned long long)gid[perm[p]] : (unsigned long long)n_gal;
+    idx[p] = p;
+}
+
+__global__ void k_gather_sorted(const int *__restrict__ idx,
+                                const unsigned long long *__restrict__ key,
+                                const int *__restrict__ perm, unsigned long long *__restrict__ key2,
+                                int *__restrict__ perm2, int n)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n)
+        return;
+    const int p = idx[q];
+    key2[q] = key[p];
+    perm2[q] = perm[p];
+}
+
+// Steps 1-3: root cubes, keys, sorted order of the alive bodies (n_alive),
+// by (system, key) for a forest, and each sorted position's system.
 static int order_bodies(csgd_t *d)
 {
     const int n = d->n;
     cudaStream_t s = d->stream;
     DevScalars *sc = d->sc;
     const int B = 256;
-    { k_reset<<<1, 1, 0, s>>>(sc); d->launches++; }
+    const int G = d->n_gal;
+    { k_reset<<<1, 256, 0, s>>>(sc, d->roots, G); d->launches++; }
     int gb = min(csgd_grid(n, B), 152 * 8);
-    { k_bbox<<<gb > 0 ? gb : 1, B, 0, s>>>(d->x, d->y, d->z, d->m, n, sc); d->launches++; }
-    { k_root<<<1, 1, 0, s>>>(sc); d->launches++; }
+    { k_bbox<<<gb > 0 ? gb : 1, B, 0, s>>>(d->x, d->y, d->z, d->m, d->gid, n, d->roots); d->launches++; }
+    { k_root<<<1, 256, 0, s>>>(sc, d->roots, G); d->launches++; }
     if (n > 0)
-        { k_keys<<<csgd_grid(n, B), B, 0, s>>>(d->x, d->y, d->z, d->m, n, sc, d->key, d->perm); d->launches++; }
-    return csg_radix_sort(d, d->key, d->perm, d->key_alt, d->perm_alt, n, 64);
+        { k_keys<<<csgd_grid(n, B), B, 0, s>>>(d->x, d->y, d->z, d->m, d->gid, n, sc, d->roots, d->key, d->perm); d->launches++; }
+    int rc = csg_radix_sort(d, d->key, d->perm, d->key_alt, d->perm_alt, n, 64);
+    if (rc)
+        return rc;
+    if (G > 1 && n > 1) {
+        // stable pass on the system id: order (system, key)
+        const int g = csgd_grid(n, B);
+        { k_gal_keys<<<g, B, 0, s>>>(sc, d->perm, d->gid, d->ord_key, d->ord_id, n, G); d->launches++; }
+        int bits = 1; // system ids 0..G (G marks dead bodies)
+        while (bits < 31 && (1 << bits) <= G)
+            bits++;
+        rc = csg_radix_sort(d, d->ord_key, d->ord_id, d->ord_key_alt, d->ord_id_alt, n, bits);
+        if (rc)
+            return rc;
+        { k_gather_sorted<<<g, B, 0, s>>>(d->ord_id, d->key, d->perm, d->key_alt, d->perm_alt, n); d->launches++; }
+        // back into (key, perm): the buffers keep their roles, so a captured
+        // substep and direct launches always agree on where the order is
+        cudaMemcpyAsync(d->key, d->key_alt, sizeof(unsigned long long) * (size_t)n,
+                        cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(d->perm, d->perm_alt, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, s);
+    }
+    { k_sgid<<<csgd_grid(n > 0 ? n : 1, B), B, 0, s>>>(sc, d->perm, d->gid, d->sgid, n); d->launches++; }
+    return csgd_check(d, cudaGetLastError());
 }
 
 extern "C" int csgd_build_tree(csgd_t *d, int geometry)
@@ -864,22 +1034,23 @@ extern "C" int csgd_build_tree(csgd_t *d, int geometry)
     if (rc)
         return rc;
     const int g = csgd_grid(n > 0 ? n : 1, B);
-    { k_deep_mark<<<g, B, 0, s>>>(d->x, d->y, d->z, sc, d->key, d->perm, d->ext); d->launches++; }
-    { k_deep_sort<<<g, B, 0, s>>>(sc, d->key, d->perm, d->ext); d->launches++; }
-    { k_count<<<g, B, 0, s>>>(sc, d->key, d->ext, d->lcp, d->cnt); d->launches++; }
+    { k_deep_mark<<<g, B, 0, s>>>(d->x, d->y, d->z, sc, d->roots, d->key, d->sgid, d->perm, d->ext); d->launches++; }
+    { k_deep_sort<<<g, B, 0, s>>>(sc, d->key, d->sgid, d->perm, d->ext); d->launches++; }
+    { k_count<<<g, B, 0, s>>>(sc, d->key, d->ext, d->sgid, d->lcp, d->cnt); d->launches++; }
     rc = csg_scan_exclusive(d, d->cnt, d->base, n, &sc->n_alive);
     if (rc)
         return rc;
-    { k_nodes<<<g, B, 0, s>>>(*d, sc, d->key, d->ext, d->lcp, d->base, d->perm); d->launches++; }
+    { k_nodes<<<g, B, 0, s>>>(*d, sc, d->roots, d->key, d->ext, d->sgid, d->lcp, d->base, d->perm); d->launches++; }
     const int gn = csgd_grid(d->node_cap, B);
     // nodes beyond n_nodes exit at once; the grid covers the capacity
     { k_link<<<gn, B, 0, s>>>(*d, sc, d->key, d->ext); d->launches++; }
     { k_moments<<<gn, B, 0, s>>>(*d, sc, d->x, d->y, d->z, d->m, d->perm); d->launches++; }
+    { k_tasks<<<min(d->n_gal, 152), 256, 0, s>>>(sc, d->roots, d->n_gal, d->base, d->tasks, d->task_cap, 0); d->launches++; }
     d->geometry_valid = 0;
     d->imported = 0;
     d->gas_valid = 0;
     if (geometry) {
-        { k_geometry<<<gn, B, 0, s>>>(*d, sc, d->key, d->ext); d->launches++; }
+        { k_geometry<<<gn, B, 0, s>>>(*d, sc, d->roots, d->key, d->ext, d->sgid); d->launches++; }
         d->geometry_valid = 1;
     }
     return csgd_check(d, cudaGetLastError());
@@ -887,12 +1058,16 @@ extern "C" int csgd_build_tree(csgd_t *d, int geometry)
 
 extern "C" int csgd_export_pool(csgd_t *d, OctreeNode *pool, int capacity, int *pool_size_out)
 {
+    if (d->n_gal > 1) { // one system only (see csgd_set_systems)
+        csgd_set_err(d, CSG_ERR_UNSUPPORTED);
+        return CSG_ERR_UNSUPPORTED;
+    }
     cudaStream_t s = d->stream;
     DevScalars *sc = d->sc;
     const int B = 256;
     if (!d->geometry_valid) {
         const int gn = csgd_grid(d->node_cap, B);
-        { k_geometry<<<gn, B, 0, s>>>(*d, sc, d->key, d->ext); d->launches++; }
+        { k_geometry<<<gn, B, 0, s>>>(*d, sc, d->roots, d->key, d->ext, d->sgid); d->launches++; }
         d->geometry_valid = 1;
     }
     int rc = csgd_node_count(d, pool_size_out);
@@ -916,6 +1091,10 @@ extern "C" int csgd_export_pool(csgd_t *d, OctreeNode *pool, int capacity, int *
 
 extern "C" int csgd_import_pool(csgd_t *d, const OctreeNode *pool, int n_nodes, int root)
 {
+    if (d->n_gal > 1) { // one system only (see csgd_set_systems)
+        csgd_set_err(d, CSG_ERR_UNSUPPORTED);
+        return CSG_ERR_UNSUPPORTED;
+    }
     if (n_nodes <= 0 || n_nodes > d->node_cap || root < 0 || root >= n_nodes) {
         csgd_set_err(d, CSG_ERR_BAD_ARG);
         return CSG_ERR_BAD_ARG;
@@ -937,6 +1116,7 @@ extern "C" int csgd_import_pool(csgd_t *d, const OctreeNode *pool, int n_nodes, 
     { k_imp_links<<<g, B, 0, s>>>(*d, sc, n_nodes, root, par, slot); d->launches++; }
     { k_imp_sizes<<<g, B, 0, s>>>(*d, sc, n_nodes, par, size); d->launches++; }
     { k_imp_write<<<g, B, 0, s>>>(*d, sc, n_nodes, root, par, slot, size); d->launches++; }
+    { k_tasks<<<1, 256, 0, s>>>(sc, d->roots, 1, d->base, d->tasks, d->task_cap, 1); d->launches++; }
     d->geometry_valid = 1;
     d->imported = 1;
     d->gas_valid = 0;

@@ -28,20 +28,76 @@
 
 namespace {
 
-constexpr int WALK_THREADS = 256;
-constexpr int WALK_WARPS = WALK_THREADS / CSG_WARP;
-
 struct WalkArgs {
     const int *perm;
     const double *x, *y, *z;
     const NodeW64 *w64;
     const NodeW32 *w32;
+    const WalkTask *tasks;
+    const DevRoot *roots;
     DevScalars *sc;
     double *ax, *ay, *az;
     double G, eps2, theta2, t2lo, t2hi;
     float Gf, eps2f, theta2f, guard_abs, guard_rel;
     int node_cap;
+    int group; // 0: one warp per task; g > 0: take g tasks at a time from a counter
 };
+
+// Work distribution shared by the walks. A task is up to 32 consecutive
+// sorted bodies of one system. With group == 0 warp w of the grid walks task
+// w; otherwise (persistent launch, a few blocks per SM) each warp takes the
+// next `group` tasks from sc->task_next until none are left. Every take
+// advances the counter, so the loop ends after at most n_tasks/group + 1
+// takes per warp.
+__device__ __forceinline__ int take_tasks(const WalkArgs &a)
+{
+    int v = 0;
+    if ((threadIdx.x & 31) == 0)
+        v = atomicAdd(&a.sc->task_next, a.group);
+    return __shfl_sync(0xffffffffu, v, 0);
+}
+
+// Resident warps per SM the register allocation is sized for: 32 (64
+// registers a thread) for one-warp-per-task launches, 24 (up to 85) for
+// persistent ones, whose task loop state would otherwise spill.
+constexpr int persist_min_blocks(int warps, bool persist) { return (persist ? 24 : 32) / warps; }
+
+// Validated task: bodies [pos0, pos0+count) and the system's cells [root, end).
+struct TaskRange {
+    int pos0, count, root, end;
+};
+
+template <int WARPS, bool PERSIST, typename Fn>
+__device__ __forceinline__ void for_each_task(const WalkArgs &a, Fn fn)
+{
+    const int nn = a.sc->n_nodes;
+    if (nn > a.node_cap || nn < 1)
+        return; // no valid tree (capacity error already recorded)
+    const int nt = a.sc->n_tasks;
+    auto run = [&](int t) {
+        const WalkTask w = a.tasks[t];
+        const DevRoot &r = a.roots[w.gal];
+        const TaskRange tr{w.pos0, w.count, r.root, r.end};
+        if (tr.root < 0 || tr.end > nn || tr.root >= tr.end)
+            dev_fail(a.sc, CSG_ERR_WALK_LIMIT);
+        else
+            fn(tr);
+    };
+    if (!PERSIST) {
+        const int t = blockIdx.x * WARPS + (threadIdx.x >> 5);
+        if (t < nt)
+            run(t);
+        return;
+    }
+    int t = take_tasks(a), tend = t + a.group;
+    while (t < nt) {
+        run(t);
+        if (++t >= tend) {
+            t = take_tasks(a);
+            tend = t + a.group;
+        }
+    }
+}
 
 // Reference opening decision fl(s2/d2) < theta2 (src/octree.c:202-203),
 // without a division unless s2 is within 2^-50 of theta2*d2.
@@ -71,27 +127,18 @@ __device__ __forceinline__ double inv_r3_fast(double r2)
 }
 
 template <bool EXACT, bool STATS>
-__global__ void __launch_bounds__(WALK_THREADS) k_walk64(WalkArgs a)
+__device__ __forceinline__ void walk64_task(const WalkArgs &a, NodeW64 *win, const TaskRange &tr,
+                                            unsigned long long &hits)
 {
-    __shared__ NodeW64 win_all[WALK_WARPS][CSG_WARP];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    NodeW64 *win = win_all[warp];
-    const int n_alive = a.sc->n_alive;
-    const long long p = (long long)blockIdx.x * WALK_THREADS + threadIdx.x;
-    const long long warp0 = p - lane;
-    if (warp0 >= n_alive)
-        return;
-    if (a.sc->n_nodes > a.node_cap || a.sc->n_nodes < 1)
-        return; // no valid tree (capacity error already recorded)
-    const int nn = a.sc->n_nodes;
-    const bool valid = p < n_alive;
-    const int me = valid ? a.perm[p] : -1;
+    const int lane = threadIdx.x & 31;
+    const int nn = tr.end;
+    const bool valid = lane < tr.count;
+    const int me = valid ? a.perm[tr.pos0 + lane] : -1;
     const double px = valid ? a.x[me] : 0.0, py = valid ? a.y[me] : 0.0,
                  pz = valid ? a.z[me] : 0.0;
     double sx = 0.0, sy = 0.0, sz = 0.0;
-    unsigned long long hits = 0;
     int skip = valid ? 0 : INT_MAX;
-    int cur = 0, wbase = INT_MIN / 2;
+    int cur = tr.root, wbase = INT_MIN / 2;
     while (cur < nn) {
         if (cur - wbase >= CSG_WARP) {
             wbase = cur;
@@ -160,11 +207,24 @@ __global__ void __launch_bounds__(WALK_THREADS) k_walk64(WalkArgs a)
         a.ay[me] = sy;
         a.az[me] = sz;
     }
-    if (STATS) {
-        unsigned int h = __reduce_add_sync(0xffffffffu, (unsigned int)hits);
-        if (lane == 0)
-            atomicAdd(&a.sc->interactions, (unsigned long long)h);
-    }
+}
+
+__device__ __forceinline__ void add_hits(const WalkArgs &a, unsigned long long hits)
+{
+    unsigned int h = __reduce_add_sync(0xffffffffu, (unsigned int)hits);
+    if ((threadIdx.x & 31) == 0 && h)
+        atomicAdd(&a.sc->interactions, (unsigned long long)h);
+}
+
+template <bool EXACT, bool STATS>
+__global__ void __launch_bounds__(8 * CSG_WARP) k_walk64(WalkArgs a)
+{
+    __shared__ NodeW64 win_all[8][CSG_WARP];
+    NodeW64 *win = win_all[threadIdx.x >> 5];
+    unsigned long long hits = 0;
+    for_each_task<8, false>(a, [&](const TaskRange &tr) { walk64_task<EXACT, STATS>(a, win, tr, hits); });
+    if (STATS)
+        add_hits(a, hits);
 }
 
 // 1/r^3 for the queued FP64 walk: FP32 rsqrt seed y0 (rel. error < 2^-21),
@@ -251,12 +311,12 @@ __device__ __forceinline__ Cell load_cell(const WalkArgs &a, NodeW32 *win, int &
 // runs once per step for the whole warp. EMPTY: cells of zero mass may occur
 // (caller pools); the reference skips them with everything below.
 template <bool EMPTY, typename Take, typename After>
-__device__ __forceinline__ void walk_cells(const WalkArgs &a, NodeW32 *win, int nn, int me,
-                                           bool valid, const BodyPos &b, Take take_fn,
+__device__ __forceinline__ void walk_cells(const WalkArgs &a, NodeW32 *win, int root, int nn,
+                                           int me, bool valid, const BodyPos &b, Take take_fn,
                                            After after_fn)
 {
     int skip = valid ? 0 : INT_MAX;
-    int cur = 0, wbase = INT_MIN / 2;
+    int cur = root, wbase = INT_MIN / 2;
     while (cur < nn) {
         const Cell c = load_cell(a, win, wbase, cur, nn);
         const bool active = cur >= skip;
@@ -318,21 +378,13 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v)
 // summed per lane in blocks of up to 8 terms that are added with Kahan
 // compensation (per-body compensated FP32 summation); G applied once.
 template <bool STATS, bool EMPTY>
-__global__ void __launch_bounds__(WALK_THREADS) k_walk32(WalkArgs a)
+__device__ __forceinline__ void walk32_task(const WalkArgs &a, NodeW32 *win, const TaskRange &tr,
+                                            unsigned long long &hits)
 {
-    __shared__ NodeW32 win_all[WALK_WARPS][CSG_WARP];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    NodeW32 *win = win_all[warp];
-    const int n_alive = a.sc->n_alive;
-    const long long p = (long long)blockIdx.x * WALK_THREADS + threadIdx.x;
-    const long long warp0 = p - lane;
-    if (warp0 >= n_alive)
-        return;
-    if (a.sc->n_nodes > a.node_cap || a.sc->n_nodes < 1)
-        return; // no valid tree (capacity error already recorded)
-    const int nn = a.sc->n_nodes;
-    const bool valid = p < n_alive;
-    const int me = valid ? a.perm[p] : -1;
+    const int lane = threadIdx.x & 31;
+    const int nn = tr.end;
+    const bool valid = lane < tr.count;
+    const int me = valid ? a.perm[tr.pos0 + lane] : -1;
     const double px = valid ? a.x[me] : 0.0, py = valid ? a.y[me] : 0.0,
                  pz = valid ? a.z[me] : 0.0;
     const float hx = (float)px, hy = (float)py, hz = (float)pz;
@@ -341,9 +393,8 @@ __global__ void __launch_bounds__(WALK_THREADS) k_walk32(WalkArgs a)
     float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
     float bx = 0.f, by = 0.f, bz = 0.f; // current block of up to 8 terms
     int nblk = 0;
-    unsigned long long hits = 0;
     int skip = valid ? 0 : INT_MAX;
-    int cur = 0, wbase = INT_MIN / 2;
+    int cur = tr.root, wbase = INT_MIN / 2;
     while (cur < nn) {
         if (cur - wbase >= CSG_WARP) {
             wbase = cur;
@@ -414,11 +465,17 @@ __global__ void __launch_bounds__(WALK_THREADS) k_walk32(WalkArgs a)
         a.ay[me] = a.G * ((double)sy - (double)cy);
         a.az[me] = a.G * ((double)sz - (double)cz);
     }
-    if (STATS) {
-        unsigned int h = __reduce_add_sync(0xffffffffu, (unsigned int)hits);
-        if (lane == 0)
-            atomicAdd(&a.sc->interactions, (unsigned long long)h);
-    }
+}
+
+template <bool STATS, bool EMPTY, int WARPS, bool PERSIST>
+__global__ void __launch_bounds__(WARPS * CSG_WARP, persist_min_blocks(WARPS, PERSIST)) k_walk32(WalkArgs a)
+{
+    __shared__ NodeW32 win_all[WARPS][CSG_WARP];
+    NodeW32 *win = win_all[threadIdx.x >> 5];
+    unsigned long long hits = 0;
+    for_each_task<WARPS, PERSIST>(a, [&](const TaskRange &tr) { walk32_task<STATS, EMPTY>(a, win, tr, hits); });
+    if (STATS)
+        add_hits(a, hits);
 }
 
 // FP64 walk with dense evaluation. The traversal is walk_cells (decisions
@@ -455,27 +512,16 @@ __device__ __forceinline__ void q64_eval(const WalkArgs &a, const int *q, int la
 }
 
 template <bool STATS, bool EMPTY>
-__global__ void __launch_bounds__(WALK_THREADS) k_walk64q(WalkArgs a)
+__device__ __forceinline__ void walk64q_task(const WalkArgs &a, NodeW32 *win, int *q,
+                                             const TaskRange &tr, unsigned long long &hits)
 {
-    __shared__ int q_all[WALK_WARPS][Q64 * CSG_WARP];
-    __shared__ NodeW32 win_all[WALK_WARPS][CSG_WARP];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int *q = q_all[warp];
-    NodeW32 *win = win_all[warp];
-    const int n_alive = a.sc->n_alive;
-    const long long p = (long long)blockIdx.x * WALK_THREADS + threadIdx.x;
-    if (p - lane >= n_alive)
-        return;
-    if (a.sc->n_nodes > a.node_cap || a.sc->n_nodes < 1)
-        return;
-    const int nn = a.sc->n_nodes;
-    const bool valid = p < n_alive;
-    const int me = valid ? a.perm[p] : -1;
+    const int lane = threadIdx.x & 31;
+    const bool valid = lane < tr.count;
+    const int me = valid ? a.perm[tr.pos0 + lane] : -1;
     const BodyPos b = body_pos(a, me, valid);
     double sx = 0.0, sy = 0.0, sz = 0.0;
     int head = 0, tail = 0;
-    unsigned int hits = 0;
-    walk_cells<EMPTY>(a, win, nn, me, valid, b,
+    walk_cells<EMPTY>(a, win, tr.root, tr.end, me, valid, b,
         [&](bool take, const Cell &, float, float, float, float, int cur) {
             if (take) {
                 q[(tail & (Q64 - 1)) * CSG_WARP + lane] = cur;
@@ -500,18 +546,31 @@ __global__ void __launch_bounds__(WALK_THREADS) k_walk64q(WalkArgs a)
         a.ay[me] = a.G * sy;
         a.az[me] = a.G * sz;
     }
-    if (STATS) {
-        unsigned int hsum = __reduce_add_sync(0xffffffffu, hits);
-        if (lane == 0)
-            atomicAdd(&a.sc->interactions, (unsigned long long)hsum);
-    }
+}
+
+template <bool STATS, bool EMPTY, int WARPS, bool PERSIST>
+__global__ void __launch_bounds__(WARPS * CSG_WARP, persist_min_blocks(WARPS, PERSIST)) k_walk64q(WalkArgs a)
+{
+    __shared__ int q_all[WARPS][Q64 * CSG_WARP];
+    __shared__ NodeW32 win_all[WARPS][CSG_WARP];
+    const int warp = threadIdx.x >> 5;
+    int *q = q_all[warp];
+    NodeW32 *win = win_all[warp];
+    unsigned long long hits = 0;
+    for_each_task<WARPS, PERSIST>(a, [&](const TaskRange &tr) { walk64q_task<STATS, EMPTY>(a, win, q, tr, hits); });
+    if (STATS)
+        add_hits(a, hits);
 }
 
 // Dead bodies get a = 0 (src/octree.c:226-230); alive ones are overwritten by
 // the walk.
-__global__ void k_zero_acc(const double *__restrict__ m, double *ax, double *ay, double *az, int n)
+// Also rewinds the task counter of the persistent walks.
+__global__ void k_zero_acc(const double *__restrict__ m, double *ax, double *ay, double *az, int n,
+                           DevScalars *sc)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0)
+        sc->task_next = 0;
     if (i >= n)
         return;
     if (m[i] <= 0.0) {
@@ -523,12 +582,12 @@ __global__ void k_zero_acc(const double *__restrict__ m, double *ax, double *ay,
 
 } // namespace
 
-// Host mirror of the scalars needed to size the FP32 error band.
-extern "C" int csgd_gravity_ex(csgd_t *d, const csgd_force_params *p, int exact)
+// ---- host side -------------------------------------------------------------
+
+namespace {
+
+WalkArgs walk_args(csgd_t *d, const csgd_force_params *p)
 {
-    const int n = d->n;
-    if (n <= 0)
-        return CSG_OK;
     WalkArgs a;
     a.perm = d->perm;
     a.x = d->x;
@@ -536,6 +595,8 @@ extern "C" int csgd_gravity_ex(csgd_t *d, const csgd_force_params *p, int exact)
     a.z = d->z;
     a.w64 = d->w64;
     a.w32 = d->w32;
+    a.tasks = d->tasks;
+    a.roots = d->roots;
     a.sc = d->sc;
     a.ax = d->ax;
     a.ay = d->ay;
@@ -553,35 +614,88 @@ extern "C" int csgd_gravity_ex(csgd_t *d, const csgd_force_params *p, int exact)
     a.guard_abs = 0.0f;
     a.guard_rel = 0x1p-19f * (1.0f + a.theta2f);
     a.node_cap = d->node_cap;
+    a.group = d->walk_group;
+    return a;
+}
+
+// Kernel variant by (stats, empty cells, persistent); persistent launches
+// exist for trees built here only (no empty cells).
+#define CSG_LAUNCH_WALK(K, W, grid, s, a)                                                  \
+    do {                                                                                    \
+        if (persist && stats)                                                               \
+            K<true, false, W, true><<<grid, W * CSG_WARP, 0, s>>>(a);                       \
+        else if (persist)                                                                   \
+            K<false, false, W, true><<<grid, W * CSG_WARP, 0, s>>>(a);                      \
+        else if (stats && empty)                                                            \
+            K<true, true, W, false><<<grid, W * CSG_WARP, 0, s>>>(a);                       \
+        else if (stats)                                                                     \
+            K<true, false, W, false><<<grid, W * CSG_WARP, 0, s>>>(a);                      \
+        else if (empty)                                                                     \
+            K<false, true, W, false><<<grid, W * CSG_WARP, 0, s>>>(a);                      \
+        else                                                                                \
+            K<false, false, W, false><<<grid, W * CSG_WARP, 0, s>>>(a);                     \
+    } while (0)
+
+// One walk launch with the state's launch shape.
+void launch_walk(csgd_t *d, const WalkArgs &a, int precision, int exact)
+{
     cudaStream_t s = d->stream;
-    { k_zero_acc<<<csgd_grid(n, 256), 256, 0, s>>>(d->m, d->ax, d->ay, d->az, n); d->launches++; }
-    const int g = csgd_grid(n, WALK_THREADS);
+    const int W = d->walk_warps == 4 ? 4 : 8;
     // trees built here have no empty cell below a non-empty root; a caller's
     // pool may (the reference skips those cells)
     const bool empty = d->imported != 0;
-    if (p->precision == CSG_PREC_FP32_MIXED && !exact) {
-        if (d->stats && empty)
-            { k_walk32<true, true><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
-        else if (d->stats)
-            { k_walk32<true, false><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
-        else if (empty)
-            { k_walk32<false, true><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
-        else
-            { k_walk32<false, false><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
-    } else if (exact) {
-        if (d->stats)
-            { k_walk64<true, true><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
-        else
-            { k_walk64<true, false><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
+    const bool stats = d->stats != 0;
+    const bool persist = a.group > 0 && !empty && !exact;
+    WalkArgs b = a;
+    if (!persist)
+        b.group = 0;
+    int grid;
+    if (persist) {
+        grid = d->num_sms * d->walk_bps;
     } else {
-        if (d->stats && empty)
-            { k_walk64q<true, true><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
-        else if (d->stats)
-            { k_walk64q<true, false><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
-        else if (empty)
-            { k_walk64q<false, true><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
+        const long long tasks = (long long)d->n / CSG_WARP + d->n_gal + 1; // >= n_tasks
+        grid = (int)((tasks + W - 1) / W);
+    }
+    if (grid < 1)
+        grid = 1;
+    if (exact) {
+        if (stats)
+            k_walk64<true, true><<<grid, 8 * CSG_WARP, 0, s>>>(b);
         else
-            { k_walk64q<false, false><<<g, WALK_THREADS, 0, s>>>(a); d->launches++; }
+            k_walk64<true, false><<<grid, 8 * CSG_WARP, 0, s>>>(b);
+    } else if (precision == CSG_PREC_FP32_MIXED) {
+        if (W == 4)
+            CSG_LAUNCH_WALK(k_walk32, 4, grid, s, b);
+        else
+            CSG_LAUNCH_WALK(k_walk32, 8, grid, s, b);
+    } else {
+        if (W == 4)
+            CSG_LAUNCH_WALK(k_walk64q, 4, grid, s, b);
+        else
+            CSG_LAUNCH_WALK(k_walk64q, 8, grid, s, b);
+    }
+    d->launches++;
+}
+
+} // namespace
+
+extern "C" int csgd_gravity_ex(csgd_t *d, const csgd_force_params *p, int exact)
+{
+    const int n = d->n;
+    if (n <= 0)
+        return CSG_OK;
+    WalkArgs a = walk_args(d, p);
+    if (exact) // the parity walk keeps one warp per task, 8 warps per block
+        a.group = 0;
+    cudaStream_t s = d->stream;
+    { k_zero_acc<<<csgd_grid(n, 256), 256, 0, s>>>(d->m, d->ax, d->ay, d->az, n, d->sc); d->launches++; }
+    if (exact) {
+        const int saved = d->walk_warps;
+        d->walk_warps = 8;
+        launch_walk(d, a, p->precision, 1);
+        d->walk_warps = saved;
+    } else {
+        launch_walk(d, a, p->precision, 0);
     }
     return csgd_check(d, cudaGetLastError());
 }
@@ -589,4 +703,107 @@ extern "C" int csgd_gravity_ex(csgd_t *d, const csgd_force_params *p, int exact)
 extern "C" int csgd_gravity(csgd_t *d, const csgd_force_params *p)
 {
     return csgd_gravity_ex(d, p, 0);
+}
+
+// ---- launch shape and its autotuner ------------------------------------------
+
+extern "C" int csgd_set_walk_shape(csgd_t *d, const CsgWalkShape *w)
+{
+    if (!w || (w->warps_per_block != 4 && w->warps_per_block != 8) || w->task_group < 0 ||
+        w->task_group > 64 || (w->task_group > 0 && (w->blocks_per_sm < 1 || w->blocks_per_sm > 32))) {
+        csgd_set_err(d, CSG_ERR_BAD_ARG);
+        return CSG_ERR_BAD_ARG;
+    }
+    if (d->walk_warps != w->warps_per_block || d->walk_group != w->task_group ||
+        d->walk_bps != w->blocks_per_sm)
+        csgd_drop_graph(d); // the captured walk launch changes
+    d->walk_warps = w->warps_per_block;
+    d->walk_group = w->task_group;
+    d->walk_bps = w->task_group > 0 ? w->blocks_per_sm : 0;
+    return CSG_OK;
+}
+
+extern "C" void csgd_get_walk_shape(const csgd_t *d, CsgWalkShape *w)
+{
+    w->warps_per_block = d->walk_warps;
+    w->task_group = d->walk_group;
+    w->blocks_per_sm = d->walk_bps;
+    w->ms = 0.0f;
+}
+
+// Times every candidate launch shape on the current tree (reps walks each,
+// the median kept) and keeps the fastest. The walk's results do not depend on
+// the shape: every body's sum is formed by one lane in the same order.
+extern "C" int csgd_autotune_walk(csgd_t *d, const csgd_force_params *p, int reps,
+                                  CsgWalkShape *out, CsgWalkShape *all, int all_cap,
+                                  int *n_all)
+{
+    if (reps < 1 || reps > 64) {
+        csgd_set_err(d, CSG_ERR_BAD_ARG);
+        return CSG_ERR_BAD_ARG;
+    }
+    // persistent candidates: 8, 16 or 24 resident warps per SM (24 is what
+    // their register allocation allows), task groups of 1, 2 or 4
+    static const int groups[] = {1, 2, 4};
+    static const int resident[] = {8, 16, 24};
+    CsgWalkShape cand[2 * (1 + 9)];
+    int nc = 0;
+    for (int w = 4; w <= 8; w += 4) {
+        cand[nc++] = CsgWalkShape{w, 0, 0, 0.0f};
+        for (int g : groups)
+            for (int rw : resident)
+                cand[nc++] = CsgWalkShape{w, g, rw / w, 0.0f};
+    }
+    CsgWalkShape saved;
+    csgd_get_walk_shape(d, &saved);
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess)
+        return csgd_check(d, cudaGetLastError());
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return csgd_check(d, cudaGetLastError());
+    }
+    int rc = CSG_OK;
+    int best = -1;
+    for (int c = 0; c < nc && rc == CSG_OK; c++) {
+        d->walk_warps = cand[c].warps_per_block;
+        d->walk_group = cand[c].task_group;
+        d->walk_bps = cand[c].blocks_per_sm;
+        float t[64];
+        for (int r = 0; r <= reps && rc == CSG_OK; r++) { // first run warms up
+            cudaEventRecord(e0, d->stream);
+            rc = csgd_gravity(d, p);
+            cudaEventRecord(e1, d->stream);
+            if (rc == CSG_OK)
+                rc = csgd_sync(d);
+            if (rc == CSG_OK && r > 0)
+                cudaEventElapsedTime(&t[r - 1], e0, e1);
+        }
+        if (rc != CSG_OK)
+            break;
+        for (int i = 1; i < reps; i++) // insertion sort for the median
+            for (int j = i; j > 0 && t[j] < t[j - 1]; j--) {
+                float x = t[j];
+                t[j] = t[j - 1];
+                t[j - 1] = x;
+            }
+        cand[c].ms = t[reps / 2];
+        if (best < 0 || cand[c].ms < cand[best].ms)
+            best = c;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    d->walk_warps = saved.warps_per_block;
+    d->walk_group = saved.task_group;
+    d->walk_bps = saved.blocks_per_sm;
+    if (rc != CSG_OK)
+        return rc;
+    if (n_all)
+        *n_all = nc;
+    for (int c = 0; all && c < nc && c < all_cap; c++)
+        all[c] = cand[c];
+    rc = csgd_set_walk_shape(d, &cand[best]);
+    if (out)
+        *out = cand[best];
+    return rc;
 }

@@ -88,9 +88,10 @@ static void destroy_state(SimState *s)
     free(s);
 }
 
-/* Uploads host[0..current_n) and sets the initial accelerations
-   (src/integrator.c:4-10: tree + gravity, no SPH). */
-static SimState *start(SimState *s)
+/* Uploads host[0..current_n), declares the systems (n_sys > 1: an
+   ensemble) and sets the initial accelerations (src/integrator.c:4-10: tree +
+   gravity, no SPH). */
+static SimState *start_systems(SimState *s, int n_sys, const int *counts)
 {
     s->dev = csgd_create();
     if (!s->dev) {
@@ -102,6 +103,8 @@ static SimState *start(SimState *s)
     int rc = csgd_reserve(s->dev, s->n_alloc);
     if (!rc)
         rc = csgd_upload_bodies(s->dev, s->host, s->current_n);
+    if (!rc && n_sys > 1)
+        rc = csgd_set_systems(s->dev, n_sys, counts);
     if (!rc)
         rc = csgd_build_tree(s->dev, 0);
     if (!rc)
@@ -118,6 +121,8 @@ static SimState *start(SimState *s)
     csg_thread_set_error(CSG_OK);
     return s;
 }
+
+static SimState *start(SimState *s) { return start_systems(s, 1, NULL); }
 
 CSG_EXPORT CosmosimConfig cosmosim_default_config(void)
 {
@@ -234,6 +239,105 @@ CSG_EXPORT SimHandle cosmosim_create_from_bodies(const Body *bodies, int n,
     s->config.theta = params->theta;
     s->config.substeps = params->substeps;
     return (SimHandle)start(s);
+}
+
+CSG_EXPORT SimHandle cosmosim_create_ensemble(const Body *bodies, int n, int n_sys,
+                                              const int *counts, const CsgSimParams *params)
+{
+    if (n < 1 || !bodies || n_sys < 1 || n_sys > CSG_MAX_SYSTEMS || !counts || !params) {
+        csg_thread_set_error(CSG_ERR_BAD_ARG);
+        return NULL;
+    }
+    if (params->sph) {
+        csg_thread_set_error(CSG_ERR_UNSUPPORTED);
+        return NULL;
+    }
+    long long total = 0;
+    for (int g = 0; g < n_sys; g++) {
+        if (counts[g] < 0) {
+            csg_thread_set_error(CSG_ERR_BAD_ARG);
+            return NULL;
+        }
+        total += counts[g];
+    }
+    if (total != n) {
+        csg_thread_set_error(CSG_ERR_BAD_ARG);
+        return NULL;
+    }
+    SimState *s = (SimState *)calloc(1, sizeof(SimState));
+    Body *host = (Body *)calloc((size_t)n, sizeof(Body));
+    if (!s || !host) {
+        free(s);
+        free(host);
+        csg_thread_set_error(CSG_ERR_NOMEM);
+        return NULL;
+    }
+    memcpy(host, bodies, sizeof(Body) * (size_t)n);
+    s->host = host;
+    s->n_alloc = n;
+    s->current_n = n;
+    s->params = *params;
+    s->config = cosmosim_default_config();
+    s->config.n_bodies = n;
+    s->config.dt = params->dt;
+    s->config.theta = params->theta;
+    s->config.substeps = params->substeps;
+    return (SimHandle)start_systems(s, n_sys, counts);
+}
+
+CSG_EXPORT int cosmosim_system_count(SimHandle handle)
+{
+    if (!handle)
+        return 0;
+    return csgd_system_count(((SimState *)handle)->dev);
+}
+
+CSG_EXPORT int cosmosim_set_walk_shape(SimHandle handle, const CsgWalkShape *shape)
+{
+    if (!handle || !shape)
+        return CSG_ERR_BAD_ARG;
+    SimState *s = (SimState *)handle;
+    int rc = csgd_set_walk_shape(s->dev, shape);
+    if (rc)
+        csgd_sync(s->dev); /* clears the recorded argument error */
+    return set_err(s, rc);
+}
+
+CSG_EXPORT int cosmosim_get_walk_shape(SimHandle handle, CsgWalkShape *shape)
+{
+    if (!handle || !shape)
+        return CSG_ERR_BAD_ARG;
+    csgd_get_walk_shape(((SimState *)handle)->dev, shape);
+    return CSG_OK;
+}
+
+CSG_EXPORT int cosmosim_autotune_walk(SimHandle handle, int reps, CsgWalkShape *best,
+                                      CsgWalkShape *all, int all_cap, int *n_all)
+{
+    if (!handle || reps < 1 || reps > 64 || all_cap < 0)
+        return CSG_ERR_BAD_ARG;
+    SimState *s = (SimState *)handle;
+    csgd_force_params p = fparams(s);
+    /* the walks overwrite the accelerations; keep the handle's own */
+    int rc = csgd_sync(s->dev);
+    Body *keep = NULL;
+    if (!rc) {
+        keep = (Body *)malloc(sizeof(Body) * (size_t)(s->current_n > 0 ? s->current_n : 1));
+        if (!keep)
+            rc = CSG_ERR_NOMEM;
+    }
+    if (!rc)
+        rc = csgd_download_bodies(s->dev, keep, s->current_n);
+    if (!rc)
+        rc = csgd_build_tree(s->dev, 0);
+    if (!rc)
+        rc = csgd_autotune_walk(s->dev, &p, reps, best, all, all_cap, n_all);
+    if (!rc)
+        rc = csgd_upload_bodies(s->dev, keep, s->current_n);
+    if (!rc)
+        rc = csgd_sync(s->dev);
+    free(keep);
+    return set_err(s, rc);
 }
 
 /* Runs the CPU quasar step between device substeps (src/cosmosim_api.c:130-132). */

@@ -29,6 +29,15 @@ class CsgSimParams(ctypes.Structure):
                 ("substeps", _i), ("sph", _i), ("precision", _i)]
 
 
+class CsgWalkShape(ctypes.Structure):
+    _fields_ = [("warps_per_block", _i), ("task_group", _i), ("blocks_per_sm", _i),
+                ("ms", ctypes.c_float)]
+
+    def as_dict(self):
+        return {"warps_per_block": self.warps_per_block, "task_group": self.task_group,
+                "blocks_per_sm": self.blocks_per_sm, "ms": round(float(self.ms), 4)}
+
+
 class CudaError(RuntimeError):
     pass
 
@@ -74,6 +83,12 @@ _SIGS = {
     "csg_measure_fp_peaks": ([ctypes.POINTER(_d), ctypes.POINTER(_d)], _i),
     "cosmosim_enable_graphs": ([_vp, _i], _i),
     "csg_direct_forces_noalloc": ([_vp, _vp, _vp, _vp, _i, _vp, _i, _d, _d, _vp, _vp], _i),
+    "cosmosim_create_ensemble": ([_vp, _i, _i, _ip, ctypes.POINTER(CsgSimParams)], _vp),
+    "cosmosim_system_count": ([_vp], _i),
+    "cosmosim_set_walk_shape": ([_vp, ctypes.POINTER(CsgWalkShape)], _i),
+    "cosmosim_get_walk_shape": ([_vp, ctypes.POINTER(CsgWalkShape)], _i),
+    "cosmosim_autotune_walk": ([_vp, _i, ctypes.POINTER(CsgWalkShape),
+                                ctypes.POINTER(CsgWalkShape), _i, _ip], _i),
 }
 
 _lib = None
@@ -217,6 +232,40 @@ class Sim:
         lib = load()
         p = CsgSimParams(G, softening, theta, dt, substeps, int(sph), precision)
         return cls(lib.cosmosim_create_from_bodies(ptr(bodies), len(bodies), ctypes.byref(p)))
+
+    @classmethod
+    def ensemble(cls, bodies, counts, G=1.0, softening=0.01, theta=0.5, dt=1e-3, substeps=1,
+                 precision=PREC_FP64):
+        """One handle over len(counts) independent systems (cosmosim_create_ensemble):
+        system g is the counts[g] bodies after those of systems 0..g-1."""
+        lib = load()
+        c = np.ascontiguousarray(counts, dtype=np.int32)
+        p = CsgSimParams(G, softening, theta, dt, substeps, 0, precision)
+        return cls(lib.cosmosim_create_ensemble(ptr(bodies), len(bodies), len(c),
+                                                c.ctypes.data_as(_ip), ctypes.byref(p)))
+
+    @property
+    def system_count(self):
+        return self.lib.cosmosim_system_count(self.h)
+
+    def set_walk_shape(self, warps_per_block=8, task_group=0, blocks_per_sm=0):
+        w = CsgWalkShape(warps_per_block, task_group, blocks_per_sm, 0.0)
+        self._rc(self.lib.cosmosim_set_walk_shape(self.h, ctypes.byref(w)), "set_walk_shape")
+
+    def walk_shape(self):
+        w = CsgWalkShape()
+        self._rc(self.lib.cosmosim_get_walk_shape(self.h, ctypes.byref(w)), "walk_shape")
+        return w.as_dict()
+
+    def autotune_walk(self, reps=3):
+        """Times every candidate walk shape, keeps the fastest; returns
+        (best, [all candidates]) as dicts."""
+        best = CsgWalkShape()
+        cand = (CsgWalkShape * 64)()
+        n = ctypes.c_int(0)
+        self._rc(self.lib.cosmosim_autotune_walk(self.h, reps, ctypes.byref(best), cand, 64,
+                                                 ctypes.byref(n)), "autotune_walk")
+        return best.as_dict(), [cand[i].as_dict() for i in range(min(n.value, 64))]
 
     def _rc(self, rc, what):
         if rc:

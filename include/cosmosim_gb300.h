@@ -36,6 +36,26 @@ extern "C" {
 #define CSG_PREC_FP64 0
 #define CSG_PREC_FP32_MIXED 1
 
+/* Most independent systems one handle may hold (cosmosim_create_ensemble). */
+#define CSG_MAX_SYSTEMS 65536
+
+/* Launch shape of the gravity walk. A walk task is up to 32 consecutive
+   key-ordered bodies of one system, walked by one warp.
+     warps_per_block  4 or 8
+     task_group       0: one warp per task (grid covers every task);
+                      g > 0: persistent launch, each warp takes g tasks at a
+                      time from a device counter until none are left
+     blocks_per_sm    persistent launch only: blocks per SM (1..32)
+     ms               filled by the autotuner: median walk time, ms
+   Results do not depend on the shape (each body's sum is formed by one lane
+   in the reference's order); only the time does. */
+typedef struct {
+    int warps_per_block;
+    int task_group;
+    int blocks_per_sm;
+    float ms;
+} CsgWalkShape;
+
 /* Status of the calling thread's last free-function call (octree_*,
    integrator_*, sph_*); 0 = success. Reset by every call. */
 CSG_EXPORT int csg_last_error(void);
@@ -64,6 +84,33 @@ typedef struct {
    cosmosim_create (tree + gravity). Returns NULL on failure. */
 CSG_EXPORT SimHandle cosmosim_create_from_bodies(const Body *bodies, int n,
                                                  const CsgSimParams *params);
+
+/* Batched ensemble: n_sys independent systems in one handle — no
+   counterpart in the reference, which runs one system per process. System g
+   is the counts[g] bodies that follow those of systems 0..g-1 in `bodies`
+   (counts sum to n). Every system gets its own root cube and octree (the
+   cells the reference would build for that system alone); one walk launch
+   covers all systems and never crosses between them, so each system's
+   accelerations equal those of a handle created over it alone. Substeps run
+   as one captured CUDA graph for the whole ensemble. params->sph must be 0
+   (CSG_ERR_UNSUPPORTED otherwise). Returns NULL on failure. */
+CSG_EXPORT SimHandle cosmosim_create_ensemble(const Body *bodies, int n, int n_sys,
+                                              const int *counts, const CsgSimParams *params);
+CSG_EXPORT int cosmosim_system_count(SimHandle handle);
+
+/* Walk launch shape of a handle (see CsgWalkShape). */
+CSG_EXPORT int cosmosim_set_walk_shape(SimHandle handle, const CsgWalkShape *shape);
+CSG_EXPORT int cosmosim_get_walk_shape(SimHandle handle, CsgWalkShape *shape);
+
+/* Autotuner: builds the tree of the handle's current bodies, times the walk
+   (at the handle's precision) with every candidate shape — warps per block
+   {4, 8} x {one warp per task, persistent with task groups {1, 2, 4} and
+   8, 16 or 24 resident warps per SM} — `reps` times each, keeps the fastest on the
+   handle and writes it to *best. all (may be NULL) receives up to all_cap
+   candidates with their times, *n_all (may be NULL) their number. Blocking;
+   changes no body. */
+CSG_EXPORT int cosmosim_autotune_walk(SimHandle handle, int reps, CsgWalkShape *best,
+                                      CsgWalkShape *all, int all_cap, int *n_all);
 
 /* cosmosim_create with run-time G, softening and precision. */
 CSG_EXPORT SimHandle cosmosim_create_ex(CosmosimConfig config, double G, double softening,

@@ -76,6 +76,31 @@ def test_no_device_fails_loudly(lib):
         lib.octree_build(b)
 
 
+def test_ensemble_arguments_are_checked_before_any_device_work(lib):
+    """cosmosim_create_ensemble: SPH is refused (CSG_ERR_UNSUPPORTED), counts
+    that do not sum to n or are negative are CSG_ERR_BAD_ARG."""
+    L = lib.load()
+    b = np.zeros(10, dtype=BODY_DTYPE)
+    b["mass"] = 1.0
+    b["x"] = np.arange(10)
+
+    def create(counts, sph=0):
+        c = np.asarray(counts, dtype=np.int32)
+        p = lib.CsgSimParams(1.0, 0.01, 0.5, 1e-3, 1, sph, 0)
+        return L.cosmosim_create_ensemble(b.ctypes.data, len(b), len(c),
+                                          c.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                          ctypes.byref(p))
+
+    assert not create([5, 5], sph=1)
+    assert L.csg_last_error() == 8
+    assert not create([5, 4])
+    assert L.csg_last_error() == 4
+    assert not create([11, -1])
+    assert L.csg_last_error() == 4
+    assert not create([])
+    assert L.csg_last_error() == 4
+
+
 def test_missing_library_raises(tmp_path):
     from cosmosim_gb300 import lib as libmod
 
