@@ -45,7 +45,12 @@ CONFIGS = {
     "bulge1m": dict(kind=2, n=1_000_000, theta=0.5, eps=0.005, dt=1e-3, sph=False,
                     desc="Plummer bulge 300k + exponential disk 700k"),
 }
-FLOP_PER_INTERACTION = 20  # monopole body-cell interaction (SURVEY 8d unit)
+# batched ensemble: 64 exponential-disk galaxies, N log-uniform in [2000, 50000]
+# (size seed 12: 1,102,884 bodies), each with its own seed, scale length in
+# [0.5, 2] and SMBH fraction in [0.001, 0.02]; FP32-mixed walk, FP64 drift
+ENSEMBLE = dict(n_gal=64, n_min=2000, n_max=50000, size_seed=12, theta=0.5, eps=0.01, dt=1e-3,
+                desc="64 independent exp.-disk galaxies, N log-uniform [2000, 50000], one handle")
+FLOP_PER_INTERACTION = 20  # monopole body-cell interaction: 3 sub, 3 fma d2, rsqrt, 3 mul, 3 fma acc
 SEED = 0x5EED0000
 
 
@@ -232,6 +237,231 @@ def run_cuda(args, torch, lib, cfg, rank, world):
                 e2e_nodes=nodes)
 
 
+def ensemble_sizes():
+    r = np.random.default_rng(ENSEMBLE["size_seed"])
+    lo, hi = np.log(ENSEMBLE["n_min"]), np.log(ENSEMBLE["n_max"])
+    return np.exp(r.uniform(lo, hi, ENSEMBLE["n_gal"])).astype(np.int64)
+
+
+def ensemble_bodies(lib, rank):
+    from cosmosim_gb300.abi import BODY_DTYPE
+
+    sizes = ensemble_sizes()
+    parts = [lib.generate_ics(3, int(n), SEED + 1000 * rank + g) for g, n in enumerate(sizes)]
+    return np.concatenate(parts).astype(BODY_DTYPE), parts
+
+
+def time_calls(torch, fn, k, flush):
+    """Total device time of k calls of fn, each bracketed by events (L2 flushed before)."""
+    st = torch.cuda.current_stream()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(k)]
+    for a, b in evs:
+        flush.zero_()
+        a.record(st)
+        fn()
+        b.record(st)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in evs) / 1e3
+
+
+def run_ensemble(args, torch, lib, rank, world):
+    """64 galaxies in one handle (one walk launch per substep, one graph) vs the
+    same galaxies as 64 handles stepped one after another."""
+    e = ENSEMBLE
+    dev = torch.cuda.current_device()
+    stream = torch.cuda.current_stream()
+    flush = flush_buffer(torch)
+    allb, parts = ensemble_bodies(lib, rank)
+    sizes = [len(p) for p in parts]
+    n_total = len(allb)
+    common = dict(softening=e["eps"], theta=e["theta"], dt=e["dt"])
+    res = {}
+    # the batched handle, FP32-mixed: autotune the walk shape, then time substeps
+    ens = lib.Sim.ensemble(allb, sizes, precision=lib.PREC_FP32_MIXED, **common)
+    ens.set_stream(stream.cuda_stream)
+    best, cands = ens.autotune_walk(reps=3)
+    for _ in range(args.warmup):
+        flush.zero_()
+        ens.substeps_async(1)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(dev)
+    sampler.start()
+    if world > 1:
+        torch.distributed.barrier()
+    l0 = ens.launch_count()
+    secs = time_substeps(torch, ens, args.steps, flush)
+    ens.sync()
+    clocks = sampler.stop()
+    launches = ens.launch_count() - l0
+    build_s = time_phase(torch, ens.build_tree_async, 5, flush)
+    walk_s = time_phase(torch, ens.gravity_async, 5, flush)
+    ens.enable_stats(True)
+    ens.gravity_async()
+    inter = ens.interactions()
+    ens.enable_stats(False)
+    state = ens.bodies()
+    # end to end through the handle API: pinned host Body[] in, result out
+    pin_in = torch.empty(n_total * 168, dtype=torch.uint8, pin_memory=True)
+    pin_out = torch.empty(n_total * 168, dtype=torch.uint8, pin_memory=True)
+    hin = pin_in.numpy().view(allb.dtype)
+    hout = pin_out.numpy().view(allb.dtype)
+    hin[:] = state
+    ke = max(3, args.steps // args.e2e_divisor)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        ens.set_bodies(hin)
+        ens.substeps_async(1)
+        lib.load().cosmosim_copy_bodies(ens.h, hout.ctypes.data, n_total)
+    e2e_s = time.perf_counter() - t0
+    ens.sync()
+    ens.close()
+    res["fp32"] = dict(secs=secs, steps=args.steps, launches=launches, build_s=build_s,
+                       walk_s=walk_s, interactions=inter)
+    # the batched handle, FP64 plain (default walk shape)
+    k64 = max(3, args.steps // args.fp64_divisor)
+    ens64 = lib.Sim.ensemble(allb, sizes, precision=lib.PREC_FP64, **common)
+    ens64.set_stream(stream.cuda_stream)
+    for _ in range(args.warmup):
+        ens64.substeps_async(1)
+    res["fp64"] = dict(secs=time_substeps(torch, ens64, k64, flush), steps=k64)
+    ens64.sync()
+    ens64.close()
+    # the same galaxies as 64 separate handles, stepped one after another
+    kseq = max(3, args.steps // args.fp64_divisor)
+    for prec, name in ((lib.PREC_FP64, "seq_fp64"), (lib.PREC_FP32_MIXED, "seq_fp32")):
+        sims = [lib.Sim.from_bodies(p, precision=prec, **common) for p in parts]
+        for sm in sims:
+            sm.set_stream(stream.cuda_stream)
+            for _ in range(args.warmup):
+                sm.substeps_async(1)
+
+        def one_substep_all():
+            for sm in sims:
+                sm.substeps_async(1)
+
+        torch.cuda.synchronize()
+        res[name] = dict(secs=time_calls(torch, one_substep_all, kseq, flush), steps=kseq)
+        for sm in sims:
+            sm.sync()
+            sm.close()
+    # per-galaxy error of the FP32-mixed walk vs the FP64 walk, and of both
+    # against an FP64 direct sum on 64 bodies per galaxy (4096 in all)
+    g64 = lib.Sim.ensemble(state, sizes, precision=lib.PREC_FP64, **common)
+    g32 = lib.Sim.ensemble(state, sizes, precision=lib.PREC_FP32_MIXED, **common)
+    a64, a32 = acc(g64.bodies()), acc(g32.bodies())
+    rng = np.random.default_rng(1)
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    sample = np.concatenate([offs[g] + rng.choice(sizes[g], size=64, replace=False)
+                             for g in range(len(sizes))])
+    direct = g64.direct_forces(sample)
+    g64.close()
+    g32.close()
+    per_gal = []
+    for g in range(len(sizes)):
+        sl = slice(offs[g], offs[g + 1])
+        st = rel_err_stats(a32[sl], a64[sl])
+        per_gal.append({"n": int(sizes[g]), "median": st["median"], "max": st["max"]})
+    errors = {
+        "fp32_vs_fp64_walk_per_galaxy": {
+            "worst_median": max(p["median"] for p in per_gal),
+            "worst_max": max(p["max"] for p in per_gal),
+            "galaxies": [[p["n"], float(f"{p['median']:.3g}"), float(f"{p['max']:.3g}")]
+                         for p in per_gal]},
+        "fp32_walk_vs_direct": rel_err_stats(a32[sample], direct),
+        "fp64_walk_vs_direct": rel_err_stats(a64[sample], direct),
+        "direct_sample": int(len(sample))}
+    return dict(n_total=n_total, sizes=sizes, runs=res, best=best, candidates=cands,
+                errors=errors, clocks=clocks, e2e_s=e2e_s, e2e_steps=ke)
+
+
+def ensemble_line(args, torch, lib, rank, world, fp32_peak):
+    r = run_ensemble(args, torch, lib, rank, world)
+    runs = r["runs"]
+    times = [runs["fp32"]["secs"], r["e2e_s"]]
+    if world > 1:
+        t = torch.tensor(times, device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        times = t.tolist()
+    n = r["n_total"]
+
+    def rate(run):
+        return n * run["steps"] / run["secs"]
+
+    value = n * runs["fp32"]["steps"] * world / times[0]
+    f32 = runs["fp32"]
+    achieved = FLOP_PER_INTERACTION * f32["interactions"] / f32["walk_s"] / 1e12
+    e = ENSEMBLE
+    return {
+        "metric": "body-substeps/s (batched ensemble, FP32-mixed walk)", "value": value,
+        "unit": UNIT, "n_gpus": world, "steps": f32["steps"], "warmup": args.warmup,
+        "ms_per_step": 1e3 * f32["secs"] / f32["steps"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 pair forces / f64 positions, tree moments, drift", "data": "synthetic",
+        "config": {"workload": f"ensemble64: {e['desc']}", "n_bodies": n, "n_systems": e["n_gal"],
+                   "sizes_min_max": [int(min(r["sizes"])), int(max(r["sizes"]))],
+                   "theta": e["theta"], "softening": e["eps"], "dt": e["dt"], "sph": False,
+                   "l2": "512 MB flush between timed substeps",
+                   "parallelism": f"replicas x{world}"},
+        "walk_shape": {"autotuned": r["best"], "candidates": r["candidates"]},
+        "baselines": {
+            "ensemble_fp64_plain": rate(runs["fp64"]),
+            "sequential_64_handles_fp64_plain": rate(runs["seq_fp64"]),
+            "sequential_64_handles_fp32_mixed": rate(runs["seq_fp32"]),
+            "speedup_vs_sequential_fp64_plain": value / world / rate(runs["seq_fp64"]),
+            "speedup_vs_sequential_fp32_mixed": value / world / rate(runs["seq_fp32"])},
+        "phases_ms": {"build": 1e3 * f32["build_s"], "walk_fp32": 1e3 * f32["walk_s"]},
+        "interactions_per_substep": f32["interactions"],
+        "roofline": {"bound": "fp32-pipe", "kernel": "k_walk32 (gravity walk, all systems)",
+                     "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak, "traffic": None},
+        "errors": r["errors"],
+        "e2e": {"value": n * r["e2e_steps"] * world / times[1], "unit": UNIT,
+                "api": "cosmosim_set_bodies + cosmosim_substeps_async(1) + cosmosim_copy_bodies "
+                       "(pinned host Body[])",
+                "steps": r["e2e_steps"], "h2d_bytes_per_step": 168 * n,
+                "d2h_bytes_per_step": 168 * n},
+        "gpu_launches": f32["launches"],
+        "clocks": r["clocks"],
+    }
+
+
+def ensemble_reference(args, world):
+    """The reference's CPU algorithm over the 64 galaxies (one system at a time,
+    as the reference runs them), substep sweeps within --cpu-budget seconds."""
+    from cosmosim_gb300 import lib
+    from cosmosim_gb300.abi import NODE_DTYPE
+    from oracle import orc
+
+    orc.build()
+    o = orc.Oracle()
+    cores = o.set_threads(os.cpu_count() or 1)
+    e = ENSEMBLE
+    _, parts = ensemble_bodies(lib, 0)
+    pools = [np.zeros(8 * len(p), dtype=NODE_DTYPE) for p in parts]
+    for p, pool in zip(parts, pools):
+        o.integrator_init_accelerations(p, 1.0, e["eps"], e["theta"], pool)
+    sweeps = 0
+    t0 = time.perf_counter()
+    while sweeps < max(1, args.steps) and (sweeps < 1 or time.perf_counter() - t0 < args.cpu_budget):
+        for p, pool in zip(parts, pools):
+            o.integrator_step(p, e["dt"], 1.0, e["eps"], e["theta"], pool, 0)
+        sweeps += 1
+    secs = time.perf_counter() - t0
+    n = sum(len(p) for p in parts)
+    v = n * sweeps / secs
+    return {"metric": "body-substeps/s (batched ensemble, FP32-mixed walk)", "value": v,
+            "unit": UNIT, "impl": "reference", "n_gpus": world, "steps": sweeps, "warmup": 0,
+            "ms_per_step": 1e3 * secs / sweeps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"ensemble64: {e['desc']}", "n_bodies": n},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{sweeps} substep sweeps over the 64 galaxies "
+                                       f"(oracle/orc.c, OpenMP, {cores} threads)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def cpu_reference(cfg, steps, seed=SEED, time_budget=None):
     """The reference's CPU algorithm (oracle port, OpenMP on every host core)."""
     from cosmosim_gb300 import lib
@@ -264,7 +494,7 @@ def main():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="cuda", choices=["cuda", "reference"])
-    ap.add_argument("--config", default="merger100k", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="merger100k", choices=sorted(CONFIGS) + ["ensemble64"])
     ap.add_argument("--fp64-divisor", type=int, default=8,
                     help="FP64 run times steps/divisor substeps")
     ap.add_argument("--e2e-divisor", type=int, default=8)
@@ -276,8 +506,36 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    cfg = CONFIGS[args.config]
     rank, world, local = dist_env()
+    if args.config == "ensemble64":
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps(ensemble_reference(args, world)))
+            return
+        import torch
+
+        torch.cuda.set_device(local)
+        work_stream = torch.cuda.Stream()
+        torch.cuda.set_stream(work_stream)
+        if world > 1:
+            torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
+        from cosmosim_gb300 import lib
+
+        lib.load()
+        fp32_peak, _ = lib.measure_fp_peaks()
+        line = ensemble_line(args, torch, lib, rank, world, fp32_peak)
+        if rank == 0 and world == 1 and not args.no_cpu_baseline:
+            cb = ensemble_reference(args, world)["cpu_baseline"]
+            line["cpu_baseline"] = cb
+            line["speedup_vs_cpu"] = {"fp32_mixed": line["value"] / cb["value"],
+                                      "e2e": line["e2e"]["value"] / cb["value"]}
+        if rank == 0:
+            print(json.dumps(line))
+        if world > 1:
+            torch.distributed.barrier()
+            torch.distributed.destroy_process_group()
+        return
+    cfg = CONFIGS[args.config]
     config = {"workload": f"{args.config}: {cfg['desc']}", "n_bodies": cfg["n"],
               "theta": cfg["theta"], "softening": cfg["eps"], "dt": cfg["dt"],
               "sph": cfg["sph"], "l2": "512 MB flush between timed substeps",

@@ -434,6 +434,18 @@ CSG_EXPORT int cosmosim_copy_bodies(SimHandle handle, Body *out, int n)
     return set_err(s, rc);
 }
 
+CSG_EXPORT int cosmosim_set_bodies(SimHandle handle, const Body *bodies, int n)
+{
+    if (!handle || !bodies)
+        return CSG_ERR_BAD_ARG;
+    SimState *s = (SimState *)handle;
+    if (n != s->current_n)
+        return set_err(s, CSG_ERR_BAD_ARG);
+    int rc = csgd_upload_bodies(s->dev, bodies, n);
+    s->host_stale = 1;
+    return set_err(s, rc);
+}
+
 CSG_EXPORT int cosmosim_get_count(SimHandle handle)
 {
     if (!handle)

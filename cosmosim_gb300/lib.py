@@ -67,6 +67,7 @@ _SIGS = {
     "cosmosim_sync": ([_vp], _i),
     "cosmosim_set_stream": ([_vp, _vp], _i),
     "cosmosim_copy_bodies": ([_vp, _vp, _i], _i),
+    "cosmosim_set_bodies": ([_vp, _vp, _i], _i),
     "cosmosim_build_tree_async": ([_vp], _i),
     "cosmosim_gravity_async": ([_vp], _i),
     "cosmosim_enable_stats": ([_vp, _i], _i),
@@ -326,6 +327,11 @@ class Sim:
         out = np.zeros(self.count, dtype=BODY_DTYPE)
         self._rc(self.lib.cosmosim_copy_bodies(self.h, ptr(out), len(out)), "copy_bodies")
         return out
+
+    def set_bodies(self, bodies):
+        """Uploads bodies into the handle (cosmosim_set_bodies; asynchronous:
+        keep `bodies` alive and unchanged until the next sync)."""
+        self._rc(self.lib.cosmosim_set_bodies(self.h, ptr(bodies), len(bodies)), "set_bodies")
 
     def get_bodies_view(self):
         """The borrowed array cosmosim_get_bodies returns, copied into numpy."""

@@ -131,6 +131,13 @@ CSG_EXPORT int cosmosim_set_stream(SimHandle handle, void *cuda_stream);
 /* Copies the bodies out (n must equal cosmosim_get_count). */
 CSG_EXPORT int cosmosim_copy_bodies(SimHandle handle, Body *out, int n);
 
+/* Replaces the handle's bodies by the caller's (n must equal
+   cosmosim_get_count; every field is taken, the accelerations too, as the
+   next substep's first kick uses them). Asynchronous on the handle's stream:
+   the caller keeps `bodies` unchanged until cosmosim_sync. The system layout
+   of an ensemble is kept. */
+CSG_EXPORT int cosmosim_set_bodies(SimHandle handle, const Body *bodies, int n);
+
 /* Phase-level calls for measurement: rebuild the tree from the current
    positions; run only the gravity walk on the current tree. Asynchronous. */
 CSG_EXPORT int cosmosim_build_tree_async(SimHandle handle);

@@ -137,3 +137,27 @@ def test_ensemble_interaction_count_is_the_sum_of_its_systems(lib):
         want += one.interactions()
         one.close()
     assert total == want
+
+
+def test_set_bodies_replaces_the_state_and_keeps_the_systems(lib):
+    parts = _make(lib, [1500, 2500], dead=None)
+    allb = _concat(parts)
+    ens = lib.Sim.ensemble(allb, [1500, 2500], softening=0.01, precision=1)
+    other = _concat(_systems(lib, [1500, 2500], seed0=500))
+    ens.set_bodies(other)
+    ens.sync()
+    np.testing.assert_array_equal(fields(ens.bodies(), OUT), fields(other, OUT))
+    assert ens.system_count == 2
+    ens.substeps_async(2)
+    ens.sync()
+    got = ens.bodies()
+    ens.close()
+    off = 0
+    for p in _systems(lib, [1500, 2500], seed0=500):
+        one = lib.Sim.from_bodies(p, softening=0.01, precision=1)
+        one.set_bodies(p)  # same accelerations as uploaded into the ensemble
+        one.substeps_async(2)
+        one.sync()
+        np.testing.assert_array_equal(fields(got[off:off + len(p)], OUT), fields(one.bodies(), OUT))
+        one.close()
+        off += len(p)
