@@ -462,6 +462,96 @@ def ensemble_reference(args, world):
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+# differentiable merger: two disks as the 100k merger, 10,000 stars, no SPH,
+# 200 substeps at dt 2e-3, checkpoints every 20, loss = mean squared distance
+# of the final positions to a seeded target snapshot
+ADJOINT = dict(n=10_000, substeps=200, dt=2e-3, checkpoint_every=20, eps=0.01, theta=0.5,
+               desc="two-disk merger, 10k stars, 200 KDK substeps dt 2e-3, checkpoints every 20")
+
+
+def adjoint_line(args):
+    """Gradient of the loss w.r.t. all initial positions/velocities and three
+    orbital parameters: the C-ABI adjoint (Barnes-Hut, frozen interaction
+    lists) timed, checked against central differences (h = 1e-6, 32 random
+    directions) and against the FP64 direct-sum adjoint."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from adjoint_harness import MergerProblem, floored_errors, rel_errors
+    from cosmosim_gb300 import lib
+
+    e = ADJOINT
+    kw = dict(n=e["n"], substeps=e["substeps"], dt=e["dt"],
+              checkpoint_every=e["checkpoint_every"], softening=e["eps"], theta=e["theta"])
+    pr = MergerProblem(**kw)
+    b0 = pr.ic.bodies(*[t.numpy() for t in pr.ic.state(__import__("torch").tensor(pr.p0))])
+    # timing: checkpointed forward + backward (the production path)
+    for _ in range(max(1, args.warmup // 3)):
+        pr.adj.forward(b0, pr.target)
+        pr.adj.backward()
+    reps = 3
+    t0 = time.perf_counter()
+    l0 = pr.adj.stats()["launches"]
+    for _ in range(reps):
+        pr.adj.forward(b0, pr.target)
+    t_fwd = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        pr.adj.backward()
+    t_bwd = (time.perf_counter() - t0) / reps
+    launches = (pr.adj.stats()["launches"] - l0) // reps
+    mem_ckpt = pr.adj.stats()["device_bytes"]
+    # gradients through the autograd Function (recorded lists for the checks)
+    loss, gp, gx, gv = pr.gradients(record=True)
+    st = pr.adj.stats()
+    gnorm = float(np.sqrt((gx ** 2).sum() + (gv ** 2).sum()))
+    fd6 = pr.fd_directions(gx, gv, k=32, h=1e-6)
+    fd5 = pr.fd_directions(gx, gv, k=32, h=1e-5)
+    fdp = pr.fd_params(gp, h=1e-6)
+    r6, r5, rp = rel_errors(fd6), rel_errors(fd5), rel_errors(fdp)
+    f6 = floored_errors(fd6, gnorm)
+    pr.close()
+    # FP64 direct-sum adjoint of the same run
+    dr = MergerProblem(mode=lib.ADJ_DIRECT, **kw)
+    t0 = time.perf_counter()
+    _, dgp, dgx, dgv = dr.gradients(record=False)
+    t_direct = time.perf_counter() - t0
+    dfd = dr.fd_directions(dgx, dgv, k=4, h=1e-6, frozen=False)
+    dr.close()
+    a = np.concatenate([gx.ravel(), gv.ravel()])
+    bb = np.concatenate([dgx.ravel(), dgv.ravel()])
+    n, T = e["n"], e["substeps"]
+    value = n * T / (t_fwd + t_bwd)
+    return {
+        "metric": "adjoint body-substeps/s (forward + backward, Barnes-Hut, FP64)",
+        "value": value, "unit": UNIT, "n_gpus": 1, "steps": T, "warmup": args.warmup,
+        "ms_per_step": 1e3 * (t_fwd + t_bwd) / T, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"adjoint10k: {e['desc']}", "n_bodies": n, "theta": e["theta"],
+                   "softening": e["eps"], "dt": e["dt"], "substeps": T,
+                   "checkpoint_every": e["checkpoint_every"], "sph": False,
+                   "timing": "host wall clock of the blocking C-ABI calls"},
+        "times_s": {"forward": t_fwd, "backward_with_recompute": t_bwd,
+                    "direct_sum_forward_backward": t_direct},
+        "memory_bytes": {"checkpointed": mem_ckpt, "all_lists_recorded": st["device_bytes"]},
+        "interactions_per_run": st["interactions"],
+        "loss": loss,
+        "grad_orbital": {"pericentre": float(gp[0]), "inclination_deg": float(gp[1]),
+                         "approach_speed": float(gp[2])},
+        "checks": {
+            "fd_h1e-6_32dirs": {"median_rel": float(np.median(r6)), "max_rel": float(max(r6)),
+                                "n_within_1e-4": int(sum(x <= 1e-4 for x in r6)),
+                                "max_rel_floored_1e-3_grad": float(max(f6))},
+            "fd_h1e-5_32dirs": {"median_rel": float(np.median(r5)), "max_rel": float(max(r5))},
+            "fd_orbital_params_h1e-6": [float(x) for x in rp],
+            "direct_adjoint_vs_tree_adjoint": {
+                "rel_l2": float(np.linalg.norm(a - bb) / np.linalg.norm(bb)),
+                "cosine": float(a @ bb / (np.linalg.norm(a) * np.linalg.norm(bb))),
+                "orbital_rel": [float(abs(x - y) / abs(y)) for x, y in zip(gp, dgp)]},
+            "direct_adjoint_fd_h1e-6_4dirs_max_rel_floored": float(max(
+                floored_errors(dfd, float(np.sqrt((dgx ** 2).sum() + (dgv ** 2).sum())))))},
+        "gpu_launches": launches,
+    }
+
+
 def cpu_reference(cfg, steps, seed=SEED, time_budget=None):
     """The reference's CPU algorithm (oracle port, OpenMP on every host core)."""
     from cosmosim_gb300 import lib
@@ -494,19 +584,32 @@ def main():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="cuda", choices=["cuda", "reference"])
-    ap.add_argument("--config", default="merger100k", choices=sorted(CONFIGS) + ["ensemble64"])
+    ap.add_argument("--config", default="merger100k",
+                    choices=sorted(CONFIGS) + ["ensemble64", "adjoint10k"])
     ap.add_argument("--fp64-divisor", type=int, default=8,
                     help="FP64 run times steps/divisor substeps")
     ap.add_argument("--e2e-divisor", type=int, default=8)
     ap.add_argument("--cpu-budget", type=float, default=20.0,
                     help="seconds of CPU work for the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--profile", default=None, choices=["fp32", "fp64"],
+    ap.add_argument("--profile", default=None, choices=["fp32", "fp64", "both"],
                     help="only run warm-up + --steps substeps at this precision (for ncu)")
+    ap.add_argument("--n", type=int, default=None,
+                    help="--profile only: body count of a smaller case of the workload")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     rank, world, local = dist_env()
+    if args.config == "adjoint10k":
+        if rank == 0 and args.impl == "cuda":
+            import torch
+
+            torch.cuda.set_device(local)
+            print(json.dumps(adjoint_line(args)))
+        elif rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "the reference has no adjoint (forward CPU runs: --config merger100k)"}))
+        return
     if args.config == "ensemble64":
         if args.impl == "reference":
             if rank == 0:
@@ -568,15 +671,20 @@ def main():
 
     lib.load()
     if args.profile:
-        prec = lib.PREC_FP32_MIXED if args.profile == "fp32" else lib.PREC_FP64
-        b = lib.generate_ics(cfg["kind"], cfg["n"], SEED)
-        sim = lib.Sim.from_bodies(b, softening=cfg["eps"], theta=cfg["theta"], dt=cfg["dt"],
-                                  sph=cfg["sph"], precision=prec)
-        sim.set_stream(work_stream.cuda_stream)
-        sim.substeps_async(args.warmup + args.steps)
-        sim.sync()
-        print(json.dumps({"profile": args.profile, "config": args.config,
-                          "substeps": args.warmup + args.steps, "launches": sim.launch_count()}))
+        n = args.n or cfg["n"]
+        b = lib.generate_ics(cfg["kind"], n, SEED)
+        precs = {"fp32": [lib.PREC_FP32_MIXED], "fp64": [lib.PREC_FP64],
+                 "both": [lib.PREC_FP32_MIXED, lib.PREC_FP64]}[args.profile]
+        for prec in precs:
+            sim = lib.Sim.from_bodies(b, softening=cfg["eps"], theta=cfg["theta"], dt=cfg["dt"],
+                                      sph=cfg["sph"], precision=prec)
+            sim.set_stream(work_stream.cuda_stream)
+            sim.substeps_async(args.warmup + args.steps)
+            sim.sync()
+            print(json.dumps({"profile": prec, "config": args.config, "n": n,
+                              "substeps": args.warmup + args.steps,
+                              "launches": sim.launch_count()}))
+            sim.close()
         return
     fp32_peak, fp64_peak = lib.measure_fp_peaks()
     r = run_cuda(args, torch, lib, cfg, rank, world)

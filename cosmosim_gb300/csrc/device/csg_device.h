@@ -72,6 +72,13 @@ int csgd_build_tree(csgd_t *d, int geometry);
 int csgd_gravity(csgd_t *d, const csgd_force_params *p);
 int csgd_gravity_ex(csgd_t *d, const csgd_force_params *p, int exact);
 
+/* Interaction lists of the current tree (built here): with fill = 0 writes
+   counts[i] (cells body i interacts with; untouched for dead bodies); with
+   fill = 1 writes the cell ids, in the reference's depth-first order, to
+   ids[offs[i] ..], at most cap entries in all. Device pointers. */
+int csgd_walk_lists(csgd_t *d, const csgd_force_params *p, int *counts, const int *offs,
+                    int *ids, int cap, int fill);
+
 /* SPH on the current tree (needs geometry). */
 int csgd_sph_density(csgd_t *d);
 int csgd_sph_forces(csgd_t *d);

@@ -61,6 +61,15 @@ __device__ __forceinline__ int take_tasks(const WalkArgs &a)
 // registers a thread) for one-warp-per-task launches, 24 (up to 85) for
 // persistent ones, whose task loop state would otherwise spill.
 constexpr int persist_min_blocks(int warps, bool persist) { return (persist ? 24 : 32) / warps; }
+// The queued FP64 walk is bound by the FP64 pipe, not by latency: it is sized
+// for fewer resident warps so that its queue state stays in registers.
+#ifndef CSG_W64Q_RESIDENT_WARPS
+#define CSG_W64Q_RESIDENT_WARPS 32
+#endif
+constexpr int w64q_min_blocks(int warps, bool persist)
+{
+    return (persist ? 24 : CSG_W64Q_RESIDENT_WARPS) / warps;
+}
 
 // Validated task: bodies [pos0, pos0+count) and the system's cells [root, end).
 struct TaskRange {
@@ -227,18 +236,23 @@ __global__ void __launch_bounds__(8 * CSG_WARP) k_walk64(WalkArgs a)
         add_hits(a, hits);
 }
 
-// 1/r^3 for the queued FP64 walk: FP32 rsqrt seed y0 (rel. error < 2^-21),
-// e = 1 - r2*y0^2 exactly enough in FP64, then y = y0 (1 + e/2 + 3e^2/8)
-// (the Taylor series of (1-e)^-1/2 to second order; residual < 2^-60).
-__device__ __forceinline__ double inv_r3_q(double r2)
+// m/r^3 for the queued FP64 walk, with few FP64 operations (the FP64 pipe
+// is the walk's bottleneck on this GPU): y0 = FP32 rsqrt seed (rel. error
+// < 2^-21), y0^2 exact in FP64, e = 1 - r2*y0^2 by one fused multiply-add,
+// then m/r^3 = m*y0^3 * (1-e)^-3/2 = m*y0^3 * (1 + e(3/2 + 15/8 e)) (the
+// series to second order; the next term is < 2^-60). Range check on the FP32
+// value; outside it the plain expression.
+__device__ __forceinline__ double m_inv_r3_q(double m, double r2)
 {
-    if (r2 >= 1e-30 && r2 <= 1e30) {
-        const double y0 = (double)rsqrtf((float)r2);
-        const double e = fma(-r2 * y0, y0, 1.0);
-        const double y = fma(y0 * e, fma(0.375, e, 0.5), y0);
-        return y * y * y;
+    const float r2f = (float)r2;
+    if (r2f >= 1e-30f && r2f <= 1e30f) {
+        const double y0 = (double)rsqrtf(r2f);
+        const double y0sq = y0 * y0;
+        const double e = fma(-r2, y0sq, 1.0);
+        const double mz = m * (y0sq * y0);
+        return mz * fma(e, fma(1.875, e, 1.5), 1.0);
     }
-    return 1.0 / (r2 * sqrt(r2));
+    return m / (r2 * sqrt(r2));
 }
 
 // ---- shared FP32 traversal -------------------------------------------------
@@ -502,7 +516,7 @@ __device__ __forceinline__ void q64_eval(const WalkArgs &a, const int *q, int la
             const double2 c23 = __ldg((const double2 *)&a.w64[node] + 1); // cz, m
             const double dx = c01.x - px, dy = c01.y - py, dz = c23.x - pz;
             const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, a.eps2)));
-            const double f = c23.y * inv_r3_q(r2);
+            const double f = m_inv_r3_q(c23.y, r2);
             sx = fma(f, dx, sx);
             sy = fma(f, dy, sy);
             sz = fma(f, dz, sz);
@@ -549,7 +563,7 @@ __device__ __forceinline__ void walk64q_task(const WalkArgs &a, NodeW32 *win, in
 }
 
 template <bool STATS, bool EMPTY, int WARPS, bool PERSIST>
-__global__ void __launch_bounds__(WARPS * CSG_WARP, persist_min_blocks(WARPS, PERSIST)) k_walk64q(WalkArgs a)
+__global__ void __launch_bounds__(WARPS * CSG_WARP, w64q_min_blocks(WARPS, PERSIST)) k_walk64q(WalkArgs a)
 {
     __shared__ int q_all[WARPS][Q64 * CSG_WARP];
     __shared__ NodeW32 win_all[WARPS][CSG_WARP];
@@ -578,6 +592,38 @@ __global__ void k_zero_acc(const double *__restrict__ m, double *ax, double *ay,
         ay[i] = 0.0;
         az[i] = 0.0;
     }
+}
+
+// Interaction lists: the cells each alive body interacts with, in the
+// reference's depth-first order (the FP64 walk's interaction set), written
+// per caller index: ids[offs[i] .. offs[i] + counts[i]). FILL = false counts,
+// FILL = true writes (offs from an exclusive scan of the counts).
+template <bool FILL>
+__global__ void __launch_bounds__(8 * CSG_WARP) k_walk_lists(WalkArgs a, int *counts,
+                                                             const int *offs, int *ids, int cap)
+{
+    __shared__ NodeW32 win_all[8][CSG_WARP];
+    NodeW32 *win = win_all[threadIdx.x >> 5];
+    for_each_task<8, false>(a, [&](const TaskRange &tr) {
+        const int lane = threadIdx.x & 31;
+        const bool valid = lane < tr.count;
+        const int me = valid ? a.perm[tr.pos0 + lane] : -1;
+        const BodyPos b = body_pos(a, me, valid);
+        int k = 0;
+        const int base = (FILL && valid) ? offs[me] : 0;
+        const int lim = (FILL && valid) ? min(counts[me], cap - base) : 0;
+        walk_cells<false>(a, win, tr.root, tr.end, me, valid, b,
+            [&](bool take, const Cell &, float, float, float, float, int cur) {
+                if (take) {
+                    if (FILL && k < lim)
+                        ids[base + k] = cur;
+                    k++;
+                }
+            },
+            [&](int) {});
+        if (!FILL && valid)
+            counts[me] = k;
+    });
 }
 
 } // namespace
@@ -703,6 +749,27 @@ extern "C" int csgd_gravity_ex(csgd_t *d, const csgd_force_params *p, int exact)
 extern "C" int csgd_gravity(csgd_t *d, const csgd_force_params *p)
 {
     return csgd_gravity_ex(d, p, 0);
+}
+
+extern "C" int csgd_walk_lists(csgd_t *d, const csgd_force_params *p, int *counts,
+                               const int *offs, int *ids, int cap, int fill)
+{
+    const int n = d->n;
+    if (n <= 0)
+        return CSG_OK;
+    if (d->imported) { // lists are defined on trees built here
+        csgd_set_err(d, CSG_ERR_UNSUPPORTED);
+        return CSG_ERR_UNSUPPORTED;
+    }
+    WalkArgs a = walk_args(d, p);
+    a.group = 0;
+    const long long tasks = (long long)n / CSG_WARP + d->n_gal + 1;
+    const int grid = (int)((tasks + 7) / 8);
+    if (fill)
+        { k_walk_lists<true><<<grid, 8 * CSG_WARP, 0, d->stream>>>(a, counts, offs, ids, cap); d->launches++; }
+    else
+        { k_walk_lists<false><<<grid, 8 * CSG_WARP, 0, d->stream>>>(a, counts, offs, ids, cap); d->launches++; }
+    return csgd_check(d, cudaGetLastError());
 }
 
 // ---- launch shape and its autotuner ------------------------------------------

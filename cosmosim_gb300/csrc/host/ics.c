@@ -10,7 +10,7 @@
  *   csg_ref_spiral / csg_ref_merger: the reference's own galaxy recipe
  *     (src/initial_conditions.c:40-144), used by cosmosim_create when the
  *     application does not link the reference's generators;
- *   csg_generate_ics kinds 0-4: the benchmark configurations (exponential
+ *   csg_generate_ics kinds 0-6: the benchmark configurations (exponential
  *     disks with the given scale lengths and masses, a Plummer bulge drawn by
  *     the Aarseth-Henon-Wielen (1974) rejection method, a tilted merger).
  */
@@ -300,6 +300,16 @@ int csg_generate_ics_impl(int kind, int n, uint64_t seed, Body *out)
     case 4:
         merger(out, n, 0.0, &r);
         break;
+    case 5: { /* the merger's first disk alone, stars only, in its own frame */
+        DiskSpec s = {1.0, 1.0, 0.1, 0.005 * 1.0, 0.0, 0.0, 0.0};
+        disk(out, n, &s, &r);
+        break;
+    }
+    case 6: { /* the merger's second disk alone (untilted), stars only, own frame */
+        DiskSpec s = {1.2, 1.3, 0.13, 0.005 * 1.2, 0.0, 0.0, 0.0};
+        disk(out, n, &s, &r);
+        break;
+    }
     default:
         return -1;
     }

@@ -17,6 +17,8 @@ LIB_PATH = os.path.join(HERE, "libcosmosim_gb300.so")
 
 PREC_FP64 = 0
 PREC_FP32_MIXED = 1
+ADJ_TREE = 0
+ADJ_DIRECT = 1
 
 _vp = ctypes.c_void_p
 _d = ctypes.c_double
@@ -90,6 +92,13 @@ _SIGS = {
     "cosmosim_get_walk_shape": ([_vp, ctypes.POINTER(CsgWalkShape)], _i),
     "cosmosim_autotune_walk": ([_vp, _i, ctypes.POINTER(CsgWalkShape),
                                 ctypes.POINTER(CsgWalkShape), _i, _ip], _i),
+    "csg_adjoint_create": ([_i, ctypes.POINTER(CsgSimParams), _i, _i], _vp),
+    "csg_adjoint_destroy": ([_vp], None),
+    "csg_adjoint_forward": ([_vp, _vp, _vp, _i, ctypes.POINTER(_d), _vp], _i),
+    "csg_adjoint_backward": ([_vp, _vp, _vp], _i),
+    "csg_adjoint_forward_frozen": ([_vp, _vp, _vp, ctypes.POINTER(_d)], _i),
+    "csg_adjoint_stats": ([_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                           ctypes.POINTER(ctypes.c_int64)], _i),
 }
 
 _lib = None
@@ -202,7 +211,7 @@ def measure_fp_peaks():
 
 
 def generate_ics(kind, n, seed):
-    """Seeded initial conditions of benchmark configuration `kind` (0-4)."""
+    """Seeded initial conditions of benchmark configuration `kind` (0-6)."""
     lib = load()
     out = np.zeros(n, dtype=BODY_DTYPE)
     if lib.csg_generate_ics(kind, n, seed, ptr(out)) != n:
@@ -358,6 +367,74 @@ class Sim:
     def close(self):
         if self.h:
             self.lib.cosmosim_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---- adjoint of the leapfrog (csg_adjoint_*) ----
+
+class Adjoint:
+    """Reverse-mode gradient of a T-substep FP64 leapfrog run w.r.t. the
+    initial positions and velocities, loss = mean |x_T - target|^2 over alive
+    bodies. mode ADJ_TREE: Barnes-Hut with frozen interaction lists;
+    ADJ_DIRECT: FP64 direct sum."""
+
+    def __init__(self, n, G=1.0, softening=0.01, theta=0.5, dt=2e-3, substeps=200,
+                 checkpoint_every=20, mode=ADJ_TREE):
+        self.lib = load()
+        p = CsgSimParams(G, softening, theta, dt, substeps, 0, PREC_FP64)
+        h = self.lib.csg_adjoint_create(n, ctypes.byref(p), checkpoint_every, mode)
+        if not h:
+            rc = self.lib.csg_last_error()
+            raise CudaError(f"csg_adjoint_create: {self.lib.csg_error_string(rc).decode()}")
+        self.h = ctypes.c_void_p(h)
+        self.n = n
+
+    def _rc(self, rc, what):
+        if rc:
+            raise CudaError(f"{what}: {self.lib.csg_error_string(rc).decode()} (code {rc})")
+
+    @staticmethod
+    def _target(target):
+        t = np.ascontiguousarray(target, dtype=np.float64).reshape(-1, 3)
+        return t
+
+    def forward(self, bodies, target, record=False, final=False):
+        t = self._target(target)
+        loss = ctypes.c_double(0)
+        out = np.zeros(len(bodies), dtype=BODY_DTYPE) if final else None
+        self._rc(self.lib.csg_adjoint_forward(self.h, ptr(bodies), ptr(t), int(record),
+                                              ctypes.byref(loss),
+                                              ptr(out) if final else None), "adjoint forward")
+        return (loss.value, out) if final else loss.value
+
+    def forward_frozen(self, bodies, target):
+        t = self._target(target)
+        loss = ctypes.c_double(0)
+        self._rc(self.lib.csg_adjoint_forward_frozen(self.h, ptr(bodies), ptr(t),
+                                                     ctypes.byref(loss)), "adjoint frozen")
+        return loss.value
+
+    def backward(self):
+        gx = np.zeros((self.n, 3))
+        gv = np.zeros((self.n, 3))
+        self._rc(self.lib.csg_adjoint_backward(self.h, ptr(gx), ptr(gv)), "adjoint backward")
+        return gx, gv
+
+    def stats(self):
+        b, i, k = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int64(0)
+        self._rc(self.lib.csg_adjoint_stats(self.h, ctypes.byref(b), ctypes.byref(i),
+                                            ctypes.byref(k)), "stats")
+        return {"device_bytes": b.value, "interactions": i.value, "launches": k.value}
+
+    def close(self):
+        if self.h:
+            self.lib.csg_adjoint_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -179,6 +179,52 @@ CSG_EXPORT int csg_direct_forces_noalloc(const double *x, const double *y, const
                                          const double *mass, int n, const int *idx, int m,
                                          double G, double softening, double *out, void *stream);
 
+/* ---- Adjoint of the kick-drift-kick leapfrog -------------------------------
+   No counterpart in the reference. Differentiates a T-substep FP64 run
+   (src/integrator.c:4-57: initial forces, then kick/drift/forces/kick) with
+   respect to the initial positions and velocities, for the loss
+   L = mean over alive bodies of |x_T - target|^2.
+     CSG_ADJ_TREE    Barnes-Hut forces; each substep's interaction lists (the
+                     reference walk's cells, depth-first order) are frozen:
+                     the gradient is that of the run with those lists fixed;
+     CSG_ADJ_DIRECT  FP64 direct-sum forces (every pair).
+   The backward pass contracts the softened tidal tensor with the adjoint
+   vector over the lists; memory is bounded by keeping positions and
+   velocities every checkpoint_every substeps and recomputing each segment
+   (bit-identically) before reversing it. */
+typedef struct csg_adjoint csg_adjoint;
+#define CSG_ADJ_TREE 0
+#define CSG_ADJ_DIRECT 1
+
+/* params: G, softening, theta, dt and substeps (= T) are used; sph must be 0.
+   NULL on failure (csg_last_error). */
+CSG_EXPORT csg_adjoint *csg_adjoint_create(int n, const CsgSimParams *params,
+                                           int checkpoint_every, int mode);
+CSG_EXPORT void csg_adjoint_destroy(csg_adjoint *adj);
+
+/* Runs T substeps from bodies (their accelerations are recomputed), returns
+   the loss against target (3n doubles, x y z per body) and, if final_out is
+   not NULL, the final bodies. record = 1 also keeps every substep's tree and
+   lists (T+1 sets) for csg_adjoint_forward_frozen. Blocking. */
+CSG_EXPORT int csg_adjoint_forward(csg_adjoint *adj, const Body *bodies, const double *target,
+                                   int record, double *loss, Body *final_out);
+
+/* dL/dx_0 and dL/dv_0 of the last csg_adjoint_forward (3n doubles each, x y z
+   per body). Blocking. */
+CSG_EXPORT int csg_adjoint_backward(csg_adjoint *adj, double *grad_x, double *grad_v);
+
+/* The loss of a run from other initial positions/velocities (same masses)
+   with the recorded run's trees and interaction lists — the map whose
+   gradient csg_adjoint_backward returns (for finite-difference checks).
+   Needs a forward with record = 1; does not change what backward refers to. */
+CSG_EXPORT int csg_adjoint_forward_frozen(csg_adjoint *adj, const Body *bodies,
+                                          const double *target, double *loss);
+
+/* Device memory held, the list entries (interactions) of the last forward,
+   and the kernels launched so far. */
+CSG_EXPORT int csg_adjoint_stats(csg_adjoint *adj, int64_t *device_bytes, int64_t *interactions,
+                                 int64_t *launches);
+
 /* Free-function parity mode: gravity with the reference's exact operation
    sequence (no fused multiply-add, 1/(r2*sqrt(r2))). Same signature as
    octree_compute_forces. */
@@ -193,6 +239,9 @@ CSG_EXPORT void csg_octree_compute_forces_exact(const OctreeNode *pool, int root
      kind 2: Plummer bulge (30%, a = 0.5) + exponential disk (70%), total mass 1
      kind 3: one ensemble galaxy (scale length, SMBH fraction from seed)
      kind 4: two-disk merger, stars only
+     kind 5: the merger's first disk alone (mass 1, R_d 1, SMBH 0.005), own frame
+     kind 6: the merger's second disk alone (mass 1.2, R_d 1.3, SMBH 0.006),
+             untilted, own frame (kinds 5 and 6 let a caller set the orbit)
    Returns the number of bodies written (n). */
 CSG_EXPORT int csg_generate_ics(int kind, int n, uint64_t seed, Body *out);
 

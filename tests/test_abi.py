@@ -101,6 +101,20 @@ def test_ensemble_arguments_are_checked_before_any_device_work(lib):
     assert L.csg_last_error() == 4
 
 
+def test_adjoint_arguments_are_checked_before_any_device_work(lib):
+    L = lib.load()
+    p = lib.CsgSimParams(1.0, 0.01, 0.5, 2e-3, 10, 0, 0)
+    assert not L.csg_adjoint_create(0, ctypes.byref(p), 5, 0)
+    assert L.csg_last_error() == 4
+    assert not L.csg_adjoint_create(100, ctypes.byref(p), 0, 0)
+    assert L.csg_last_error() == 4
+    assert not L.csg_adjoint_create(100, ctypes.byref(p), 5, 7)
+    assert L.csg_last_error() == 4
+    p.sph = 1
+    assert not L.csg_adjoint_create(100, ctypes.byref(p), 5, 0)
+    assert L.csg_last_error() == 4
+
+
 def test_missing_library_raises(tmp_path):
     from cosmosim_gb300 import lib as libmod
 
