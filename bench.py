@@ -191,10 +191,11 @@ def run_cuda(args, torch, lib, cfg, rank, world):
         sim.sync()
         sim.enable_stats(True)
         sim.gravity_async()
-        inter = sim.interactions()
+        inter, wsteps, wactive = sim.walk_stats()
         sim.enable_stats(False)
         out[name] = dict(secs=secs, steps=k, launches=launches, build_s=build_s, walk_s=walk_s,
-                         interactions=inter, state=sim.bodies() if name == "fp32_mixed" else None)
+                         interactions=inter, warp_steps=wsteps, active_lane_steps=wactive,
+                         state=sim.bodies() if name == "fp32_mixed" else None)
         sim.close()
     # precision and algorithmic error on the FP32 run's final state
     st = out["fp32_mixed"]["state"]
@@ -552,6 +553,72 @@ def adjoint_line(args):
     }
 
 
+def theta_sweep(args, torch, lib, cfg, thetas, flush):
+    """Per opening angle: FP32-mixed and FP64 ms/substep, walk times, and the
+    force errors (FP32 vs FP64 walk; both vs FP64 direct sum on 4096 bodies)."""
+    stream = torch.cuda.current_stream()
+    bodies = lib.generate_ics(cfg["kind"], cfg["n"], SEED)
+    alive = bodies["mass"] > 0
+    n_alive = int(alive.sum())
+    rng = np.random.default_rng(1)
+    sample = rng.choice(np.nonzero(alive)[0], size=min(4096, n_alive), replace=False)
+    out = {}
+    for th in thetas:
+        row = {}
+        accs = {}
+        for prec, name in ((lib.PREC_FP32_MIXED, "fp32_mixed"), (lib.PREC_FP64, "fp64")):
+            sim = lib.Sim.from_bodies(bodies, softening=cfg["eps"], theta=th, dt=cfg["dt"],
+                                      sph=cfg["sph"], precision=prec)
+            sim.set_stream(stream.cuda_stream)
+            accs[name] = acc(sim.bodies())
+            for _ in range(3):
+                sim.substeps_async(1)
+            k = max(3, args.steps // (4 if name == "fp32_mixed" else 4 * args.fp64_divisor))
+            secs = time_substeps(torch, sim, k, flush)
+            walk_s = time_phase(torch, sim.gravity_async, 3, flush)
+            sim.enable_stats(True)
+            sim.gravity_async()
+            inter = sim.interactions()
+            sim.close()
+            row[name] = {"body_substeps_per_s": n_alive * k / secs, "ms_per_substep": 1e3 * secs / k,
+                         "walk_ms": 1e3 * walk_s,
+                         "interactions_per_body": inter / n_alive}
+        g = lib.Sim.from_bodies(bodies, softening=cfg["eps"], theta=th)
+        direct = g.direct_forces(sample)
+        g.close()
+        row["fp32_mixed_speedup"] = (row["fp32_mixed"]["body_substeps_per_s"] /
+                                     row["fp64"]["body_substeps_per_s"])
+        row["errors"] = {"fp32_vs_fp64_walk": rel_err_stats(accs["fp32_mixed"][alive],
+                                                           accs["fp64"][alive]),
+                         "fp64_walk_vs_direct": rel_err_stats(accs["fp64"][sample], direct),
+                         "fp32_walk_vs_direct": rel_err_stats(accs["fp32_mixed"][sample], direct)}
+        out[str(th)] = row
+    return out
+
+
+def energy_drift(torch, lib, cfg, k, flush):
+    """|E(k substeps) - E(0)| / |E(0)| (FP64 kinetic + softened potential, all
+    pairs) of FP32-mixed and FP64 runs from the same initial conditions."""
+    bodies = lib.generate_ics(cfg["kind"], cfg["n"], SEED)
+    out = {"substeps": k, "dt": cfg["dt"]}
+    e0 = None
+    for prec, name in ((lib.PREC_FP32_MIXED, "fp32_mixed"), (lib.PREC_FP64, "fp64")):
+        sim = lib.Sim.from_bodies(bodies, softening=cfg["eps"], theta=cfg["theta"], dt=cfg["dt"],
+                                  sph=cfg["sph"], precision=prec)
+        if e0 is None:
+            ke, pe = sim.energy()
+            e0 = ke + pe
+            out["e0"] = e0
+        t0 = time.perf_counter()
+        sim.substeps_async(k)
+        sim.sync()
+        secs = time.perf_counter() - t0
+        ke, pe = sim.energy()
+        out[name] = {"rel_drift": abs(ke + pe - e0) / abs(e0), "run_s": secs}
+        sim.close()
+    return out
+
+
 def cpu_reference(cfg, steps, seed=SEED, time_budget=None):
     """The reference's CPU algorithm (oracle port, OpenMP on every host core)."""
     from cosmosim_gb300 import lib
@@ -596,6 +663,10 @@ def main():
                     help="only run warm-up + --steps substeps at this precision (for ncu)")
     ap.add_argument("--n", type=int, default=None,
                     help="--profile only: body count of a smaller case of the workload")
+    ap.add_argument("--thetas", default=None,
+                    help="comma-separated opening angles: add a per-theta speed/error study")
+    ap.add_argument("--drift", type=int, default=0,
+                    help="add the energy drift over this many substeps (FP32-mixed and FP64)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -716,6 +787,9 @@ def main():
         "phases_ms": {"build": 1e3 * f32["build_s"], "walk_fp32": 1e3 * f32["walk_s"],
                       "walk_fp64": 1e3 * f64["walk_s"]},
         "interactions_per_substep": f32["interactions"],
+        "walk_traversal": {"warp_steps": f32["warp_steps"],
+                           "lane_utilisation": f32["active_lane_steps"] / max(32 * f32["warp_steps"], 1),
+                           "interactions_per_lane_step": f32["interactions"] / max(32 * f32["warp_steps"], 1)},
         "roofline": {"bound": "fp32-pipe", "kernel": "k_walk32 (gravity walk)",
                      "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": None,
@@ -729,6 +803,12 @@ def main():
         "gpu_launches": f32["launches"],
         "clocks": r["clocks"],
     }
+    if rank == 0 and args.thetas:
+        line["theta_sweep"] = theta_sweep(args, torch, lib, cfg,
+                                          [float(t) for t in args.thetas.split(",")],
+                                          flush_buffer(torch))
+    if rank == 0 and args.drift > 0:
+        line["energy_drift"] = energy_drift(torch, lib, cfg, args.drift, flush_buffer(torch))
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = cpu_reference(cfg, 10**9, time_budget=args.cpu_budget)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}

@@ -37,6 +37,10 @@ void csgd_destroy(csgd_t *d);
 void csgd_set_stream(csgd_t *d, void *stream);
 void *csgd_stream(csgd_t *d);
 
+/* Tree builds also record what a reference-order pool export needs (on for
+   states that export after most builds; export works either way). */
+void csgd_set_export_order(csgd_t *d, int on);
+
 /* Makes room for n bodies (grow-only). */
 int csgd_reserve(csgd_t *d, int n);
 int csgd_count(const csgd_t *d);
@@ -122,6 +126,9 @@ int csgd_node_count(csgd_t *d, int *n_nodes);
 void csgd_enable_stats(csgd_t *d, int on);
 int csgd_reset_stats(csgd_t *d);
 int csgd_interactions(csgd_t *d, int64_t *total);
+/* ... with the walks' warp steps and the lane-steps of lanes still walking. */
+int csgd_walk_stats(csgd_t *d, int64_t *interactions, int64_t *warp_steps,
+                    int64_t *active_lane_steps);
 
 /* Alive bodies (mass > 0 or NaN, as the reference's mass <= 0 test). Blocks. */
 int csgd_alive_count(csgd_t *d, int *count);

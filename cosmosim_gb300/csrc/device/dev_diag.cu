@@ -81,6 +81,20 @@ __global__ void k_direct_sum(const double *__restrict__ part, int ns, double *__
         out[3 * (size_t)k + d] = a[d];
 }
 
+// 1/r in FP64 with few FP64 operations: FP32 rsqrt seed y0 (rel. error
+// < 2^-21), e = 1 - r2*y0^2 by one fused multiply-add (y0^2 exact), then
+// y0 (1 + e/2 + 3e^2/8) (the series of (1-e)^-1/2; the next term is < 2^-60).
+__device__ __forceinline__ double inv_r(double r2)
+{
+    const float r2f = (float)r2;
+    if (r2f >= 1e-30f && r2f <= 1e30f) {
+        const double y0 = (double)rsqrtf(r2f);
+        const double e = fma(-r2, y0 * y0, 1.0);
+        return fma(y0 * e, fma(0.375, e, 0.5), y0);
+    }
+    return 1.0 / sqrt(r2);
+}
+
 // Potential energy: row i against columns j > i, rows split over blocks;
 // each thread writes its row sum, reduced afterwards.
 __global__ void __launch_bounds__(DT) k_potential_rows(const double *__restrict__ x,
@@ -115,14 +129,14 @@ __global__ void __launch_bounds__(DT) k_potential_rows(const double *__restrict_
             for (int q = 0; q < cnt; q++) {
                 if (t + q <= i || sg[q] != gi)
                     continue;
-                double dx = sx[q] - xi, dy = sy[q] - yi, dz = sz[q] - zi;
-                double r = sqrt(dx * dx + dy * dy + dz * dz + eps2);
-                pe -= G * mi * sm[q] / r;
+                const double dx = sx[q] - xi, dy = sy[q] - yi, dz = sz[q] - zi;
+                const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, eps2)));
+                pe = fma(-sm[q], inv_r(r2), pe);
             }
         }
     }
     if (i < n)
-        row[i] = pe;
+        row[i] = G * mi * pe;
 }
 
 __global__ void k_energy_reduce(const double *__restrict__ row, const double *__restrict__ m,

@@ -68,8 +68,9 @@ struct DevRoot {
     unsigned long long omin[3], omax[3]; // order-preserving bbox encodings
     double c0[3];                        // root centre
     double hs0;                          // root half size
-    double key_scale;                    // 2^20 / hs0 (fast key path)
-    double key_tol;                      // fast-path guard, in key grid units
+    double key_scale;                    // 2^52 / hs0: key grid units x 2^32 (fast key path)
+    double key_off[3];                   // (2^20 - c0 * 2^20 / hs0) x 2^32
+    long long key_tol;                   // fast-path guard, in units of 2^-32 grid cells
     int fast_keys;                       // 1 when the fast key path is safe
     int n_alive;                         // alive bodies of this system
     int first;                           // their first sorted position
@@ -94,6 +95,8 @@ struct DevScalars {
     int n_gas;
     int pad0;
     unsigned long long interactions;     // walk statistics (when enabled)
+    unsigned long long walk_steps;       // warp traversal steps
+    unsigned long long walk_active;      // lane-steps of lanes still walking
     unsigned long long key_slow;         // bodies that took the exact key path
     int alive_count;                     // csgd_alive_count result
 };
@@ -128,6 +131,8 @@ struct csgd {
     // and, for the persistent form, blocks per SM
     int walk_warps, walk_group, walk_bps;
     int num_sms;
+    int export_order; // builds also keep what pool export needs (two lowest indices per cell)
+    int minidx_valid; // the current tree has them
 
     // keys and sort
     unsigned long long *key, *key_alt;
@@ -177,6 +182,8 @@ struct csgd {
 // ---- helpers shared by the .cu files ----
 int csgd_check(csgd_t *d, cudaError_t e);
 void csgd_drop_graph(csgd_t *d); // destroys the captured substep (after a sync)
+// allocates the cell geometry (geo, s32) and/or the pool staging on first use
+extern "C" int csgd_ensure_tree_extras(csgd_t *d, int geometry, int pool);
 void csgd_set_err(csgd_t *d, int code);
 int csgd_grid(long long n, int block);
 

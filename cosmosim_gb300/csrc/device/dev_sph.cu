@@ -469,6 +469,9 @@ int gas_list(csgd_t *d)
 // allocated on first SPH use.
 static int ensure_lists(csgd_t *d)
 {
+    int rc = csgd_ensure_tree_extras(d, 1, 0); // SPH walks the cell geometry
+    if (rc)
+        return rc;
     if (d->nb && d->nb_cap >= d->cap)
         return CSG_OK;
     if (d->nb)

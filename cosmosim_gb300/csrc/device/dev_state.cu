@@ -295,6 +295,8 @@ extern "C" void csgd_destroy(csgd_t *d)
     free(d);
 }
 
+extern "C" void csgd_set_export_order(csgd_t *d, int on) { d->export_order = on ? 1 : 0; }
+
 extern "C" void csgd_set_stream(csgd_t *d, void *stream)
 {
     d->stream = stream ? (cudaStream_t)stream : d->own_stream;
@@ -379,8 +381,6 @@ extern "C" int csgd_reserve(csgd_t *d, int n)
     ok &= dalloc(&d->w64, ncap) == cudaSuccess;
     ok &= dalloc(&d->w32, ncap) == cudaSuccess;
     ok &= dalloc(&d->link, ncap) == cudaSuccess;
-    ok &= dalloc(&d->geo, ncap) == cudaSuccess;
-    ok &= dalloc(&d->s32, ncap) == cudaSuccess;
     ok &= dalloc(&d->child, 8 * ncap) == cudaSuccess;
     ok &= dalloc(&d->nchild, ncap) == cudaSuccess;
     ok &= dalloc(&d->ticket, ncap) == cudaSuccess;
@@ -390,7 +390,6 @@ extern "C" int csgd_reserve(csgd_t *d, int n)
     ok &= dalloc(&d->ord_id, ncap) == cudaSuccess;
     ok &= dalloc(&d->ord_id_alt, ncap) == cudaSuccess;
     ok &= dalloc(&d->rank, ncap) == cudaSuccess;
-    ok &= dalloc(&d->pool, ncap) == cudaSuccess;
     ok &= dalloc(&d->gid, cap) == cudaSuccess;
     ok &= dalloc(&d->sgid, cap) == cudaSuccess;
     const size_t tcap = cap / CSG_WARP + (size_t)d->gal_cap + 2; // >= tasks of any layout
@@ -411,6 +410,28 @@ extern "C" int csgd_reserve(csgd_t *d, int n)
     // the tree stays empty-but-valid until the first build
     cudaMemsetAsync(d->sc, 0, sizeof(DevScalars), d->stream);
     return csgd_check(d, cudaGetLastError());
+}
+
+// Cell geometry (SPH, pool export/import) and the reference-layout pool
+// staging are allocated on first use: a gravity-only state never holds them
+// (184 of the ~370 bytes a node would otherwise take). Not inside a stream
+// capture: csgd_prepare_sph allocates them before a substep is captured.
+extern "C" int csgd_ensure_tree_extras(csgd_t *d, int geometry, int pool)
+{
+    const size_t ncap = (size_t)(d->node_cap > 0 ? d->node_cap : 64);
+    bool ok = true;
+    if (geometry && !d->geo)
+        ok &= dalloc(&d->geo, ncap) == cudaSuccess;
+    if (geometry && !d->s32)
+        ok &= dalloc(&d->s32, ncap) == cudaSuccess;
+    if (pool && !d->pool)
+        ok &= dalloc(&d->pool, ncap) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        csgd_set_err(d, CSG_ERR_NOMEM);
+        return CSG_ERR_NOMEM;
+    }
+    return CSG_OK;
 }
 
 // ---- forests ---------------------------------------------------------------
@@ -604,8 +625,19 @@ extern "C" int csgd_interactions(csgd_t *d, int64_t *total)
 
 extern "C" int csgd_reset_stats(csgd_t *d)
 {
-    cudaMemsetAsync(&d->sc->interactions, 0, sizeof(unsigned long long), d->stream);
+    // interactions, walk_steps, walk_active are adjacent
+    cudaMemsetAsync(&d->sc->interactions, 0, 3 * sizeof(unsigned long long), d->stream);
     return csgd_check(d, cudaGetLastError());
+}
+
+extern "C" int csgd_walk_stats(csgd_t *d, int64_t *interactions, int64_t *warp_steps,
+                               int64_t *active_lane_steps)
+{
+    int rc = csgd_sync(d);
+    *interactions = (int64_t)d->sc_host->interactions;
+    *warp_steps = (int64_t)d->sc_host->walk_steps;
+    *active_lane_steps = (int64_t)d->sc_host->walk_active;
+    return rc;
 }
 
 extern "C" int csgd_alive_count(csgd_t *d, int *count)

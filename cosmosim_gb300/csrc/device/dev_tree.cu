@@ -163,59 +163,83 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
 
 // Alive-body bbox (src/octree.c:118-139). NaN coordinates never win a
 // comparison in the reference, so they are left out here too.
-// One pass over the bodies; each warp reduces its lanes' boxes and counts
-// when its bodies belong to one system (the usual case: a system's bodies are
-// contiguous) and falls back to per-lane atomics at system boundaries.
+// Grid-stride pass; each warp keeps a running box and count for the system
+// its bodies belong to (a system's bodies are contiguous) and flushes it with
+// one set of atomics when the system changes or at the end, so a single
+// system costs one flush per warp, not one per 32 bodies. Lanes of a warp
+// that straddles a system boundary fall back to per-lane atomics.
+__device__ __forceinline__ void bbox_flush(DevRoot *roots, int g, unsigned long long lo[3],
+                                           unsigned long long hi[3], int &cnt)
+{
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        lo[a] = warp_min_u64(lo[a]);
+        hi[a] = warp_max_u64(hi[a]);
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0 && g >= 0) {
+        for (int a = 0; a < 3; a++) {
+            if (lo[a] != ~0ull)
+                atomicMin(&roots[g].omin[a], lo[a]);
+            if (hi[a] != 0ull)
+                atomicMax(&roots[g].omax[a], hi[a]);
+        }
+        if (cnt)
+            atomicAdd(&roots[g].n_alive, cnt);
+    }
+    for (int a = 0; a < 3; a++) {
+        lo[a] = ~0ull;
+        hi[a] = 0ull;
+    }
+    cnt = 0;
+}
+
 __global__ void k_bbox(const double *__restrict__ x, const double *__restrict__ y,
                        const double *__restrict__ z, const double *__restrict__ m,
                        const int *__restrict__ gid, int n, DevRoot *roots)
 {
+    unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
+    int cnt = 0;
+    int cur_g = -1; // warp-uniform: the system the running box belongs to
     for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
          base += (long long)gridDim.x * blockDim.x) {
         const long long i = base + threadIdx.x;
-        unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
-        int cnt = 0;
         const int g = (i < n) ? gid[i] : -1;
-        if (i < n && is_alive(m[i])) {
-            cnt = 1;
-            double p[3] = {x[i], y[i], z[i]};
+        const int g0 = __shfl_sync(0xffffffffu, g, 0);
+        if (!__all_sync(0xffffffffu, g == g0 || g < 0)) { // straddles systems
+            if (g >= 0 && is_alive(m[i])) {
+                const double p[3] = {x[i], y[i], z[i]};
+                for (int a = 0; a < 3; a++) {
+                    if (p[a] != p[a])
+                        continue;
+                    atomicMin(&roots[g].omin[a], ord_enc(p[a]));
+                    atomicMax(&roots[g].omax[a], ord_enc(p[a]));
+                }
+                atomicAdd(&roots[g].n_alive, 1);
+            }
+            continue;
+        }
+        if (g0 != cur_g) {
+            if (cur_g >= 0)
+                bbox_flush(roots, cur_g, lo, hi, cnt);
+            cur_g = g0;
+        }
+        if (g >= 0 && is_alive(m[i])) {
+            cnt++;
+            const double p[3] = {x[i], y[i], z[i]};
 #pragma unroll
             for (int a = 0; a < 3; a++) {
                 if (p[a] != p[a])
                     continue;
-                lo[a] = hi[a] = ord_enc(p[a]);
+                const unsigned long long e = ord_enc(p[a]);
+                lo[a] = e < lo[a] ? e : lo[a];
+                hi[a] = e > hi[a] ? e : hi[a];
             }
-        }
-        const int g0 = __shfl_sync(0xffffffffu, g, 0);
-        if (__all_sync(0xffffffffu, g == g0 || g < 0)) {
-#pragma unroll
-            for (int a = 0; a < 3; a++) {
-                lo[a] = warp_min_u64(lo[a]);
-                hi[a] = warp_max_u64(hi[a]);
-            }
-            for (int o = 16; o > 0; o >>= 1)
-                cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-            if ((threadIdx.x & 31) == 0 && g0 >= 0) {
-                for (int a = 0; a < 3; a++) {
-                    if (lo[a] != ~0ull)
-                        atomicMin(&roots[g0].omin[a], lo[a]);
-                    if (hi[a] != 0ull)
-                        atomicMax(&roots[g0].omax[a], hi[a]);
-                }
-                if (cnt)
-                    atomicAdd(&roots[g0].n_alive, cnt);
-            }
-        } else if (g >= 0) {
-            for (int a = 0; a < 3; a++) {
-                if (lo[a] != ~0ull)
-                    atomicMin(&roots[g].omin[a], lo[a]);
-                if (hi[a] != 0ull)
-                    atomicMax(&roots[g].omax[a], hi[a]);
-            }
-            if (cnt)
-                atomicAdd(&roots[g].n_alive, cnt);
         }
     }
+    if (cur_g >= 0)
+        bbox_flush(roots, cur_g, lo, hi, cnt);
 }
 
 // Root cube, reference src/octree.c:141-159, plus the fast-key parameters.
@@ -226,7 +250,8 @@ __device__ void root_cube(DevRoot *sc)
         sc->hs0 = 1.0;
         sc->fast_keys = 0;
         sc->key_scale = 0.0;
-        sc->key_tol = 1.0;
+        sc->key_off[0] = sc->key_off[1] = sc->key_off[2] = 0.0;
+        sc->key_tol = 1ll << 32;
         return;
     }
     double lo[3], hi[3];
@@ -245,16 +270,22 @@ __device__ void root_cube(DevRoot *sc)
     if (hs < 1e-10)
         hs = 1.0;
     sc->hs0 = hs;
-    // Fast keys: t = (p - c0) * 2^20/hs + 2^20 lies within R*2^-31 grid units
-    // of the exact descent, R = 1 + max|c0|/hs; bodies within the guard of
-    // a split point take the exact descent.
+    // Fast keys: t = p * 2^20/hs + (2^20 - c0 * 2^20/hs), one fused
+    // multiply-add per axis, lies within ~2 R 2^-32 grid units of the exact
+    // descent, R = 1 + max|c0|/hs (the roundings of 2^20/hs, of c0 * 2^20/hs
+    // and of the sums, each <= R 2^-33 or 2^-32). Bodies within the guard
+    // (64 R 2^-32) of a split point take the exact descent. All values are
+    // kept x 2^32 (exact) so that floor and fraction come from one int64.
     double r = fmax(fabs(sc->c0[0]), fmax(fabs(sc->c0[1]), fabs(sc->c0[2]))) / hs + 1.0;
     double tol = 64.0 * r * 0x1p-32;
     bool finite = isfinite(sc->c0[0]) && isfinite(sc->c0[1]) && isfinite(sc->c0[2]) &&
                   isfinite(hs) && hs > 0.0;
-    sc->key_tol = tol;
     sc->fast_keys = (finite && tol < 0.25) ? 1 : 0;
-    sc->key_scale = finite ? 1048576.0 / hs : 0.0;
+    const double scale = finite ? 1048576.0 / hs : 0.0;
+    sc->key_scale = scale * 0x1p32;
+    for (int a = 0; a < 3; a++)
+        sc->key_off[a] = finite ? (1048576.0 - sc->c0[a] * scale) * 0x1p32 : 0.0;
+    sc->key_tol = sc->fast_keys ? (long long)(64.0 * r) + 1 : (1ll << 32);
 }
 
 // Root cube of every system, then where each system's alive bodies start in
@@ -277,15 +308,20 @@ __global__ void k_root(DevScalars *sc, DevRoot *roots, int n_gal)
 
 // ---- 2. keys -----------------------------------------------------------
 
-__device__ __forceinline__ bool fast_coord(double p, double c, double scale, double tol, int &i)
+// Key grid index of one coordinate when it is clear of every split point by
+// the guard; t32 = grid position x 2^32 (one FP64 fused multiply-add), its
+// integer part >> 32 is the index, its low 32 bits the fraction.
+__device__ __forceinline__ bool fast_coord(double p, double scale, double off, long long tol,
+                                           int &i)
 {
-    double t = (p - c) * scale + 1048576.0;
-    if (!(t >= tol && t <= 2097152.0 - tol))
+    const double t32 = fma(p, scale, off);
+    if (!(t32 >= 0.0 && t32 < 0x1p53)) // also NaN
         return false;
-    double f = floor(t);
-    if (t - f < tol || (f + 1.0) - t < tol)
+    const long long v = __double2ll_rz(t32);
+    const long long frac = v & 0xFFFFFFFFll;
+    if (v < tol || v > (1ll << 53) - tol || frac < tol || frac > (1ll << 32) - tol)
         return false;
-    i = (int)f;
+    i = (int)(v >> 32);
     return true;
 }
 
@@ -306,9 +342,9 @@ __global__ void k_keys(const double *__restrict__ x, const double *__restrict__ 
     const DevRoot *sc = &roots[gid[i]];
     const double px = x[i], py = y[i], pz = z[i];
     int ix, iy, iz;
-    if (sc->fast_keys && fast_coord(px, sc->c0[0], sc->key_scale, sc->key_tol, ix) &&
-        fast_coord(py, sc->c0[1], sc->key_scale, sc->key_tol, iy) &&
-        fast_coord(pz, sc->c0[2], sc->key_scale, sc->key_tol, iz)) {
+    if (sc->fast_keys && fast_coord(px, sc->key_scale, sc->key_off[0], sc->key_tol, ix) &&
+        fast_coord(py, sc->key_scale, sc->key_off[1], sc->key_tol, iy) &&
+        fast_coord(pz, sc->key_scale, sc->key_off[2], sc->key_tol, iz)) {
         // east = upper x half; south = lower y half; bottom = lower z half
         unsigned long long sx = (unsigned long long)ix;
         unsigned long long sy = (unsigned long long)(~iy & KEY_MASK21);
@@ -493,21 +529,14 @@ __device__ __forceinline__ void write_cell(csgd_t dd, DevScalars *sc, double hs0
     double hs = ldexp(hs0, -L);
     double s = 2.0 * hs;
     double s2 = s * s;
-    NodeW64 w;
-    w.cx = w.cy = w.cz = w.m = 0.0;
+    // the structural fields only: k_moments writes every cell's centre of
+    // mass and mass
+    NodeW64 &w = dd.w64[id];
     w.s2 = s2;
-    w.next = next;
-    w.body = body;
-    dd.w64[id] = w;
-    NodeW32 v;
-    v.cx = v.cy = v.cz = v.m = 0.0f;
-    v.lx = v.ly = v.lz = 0.0f;
-    v.next = next;
-    v.body = body;
+    *(int2 *)&w.next = make_int2(next, body);
+    NodeW32 &v = dd.w32[id];
     v.s2 = (float)s2;
-    v.s = (float)s;
-    v.pad = 0.0f;
-    dd.w32[id] = v;
+    *(int4 *)&v.next = make_int4(next, body, __float_as_int((float)s), 0);
     dd.link[id] = NodeLink{parent, L, first, count};
     int4 *c = (int4 *)(dd.child + 8 * (size_t)id);
     c[0] = make_int4(-1, -1, -1, -1);
@@ -516,11 +545,13 @@ __device__ __forceinline__ void write_cell(csgd_t dd, DevScalars *sc, double hs0
     dd.ticket[id] = 0;
 }
 
+// leaf_of[p]: the leaf cell that starts at sorted position p, or -1 (a
+// position inside a depth-64 multi-body leaf).
 __global__ void k_nodes(csgd_t dd, DevScalars *sc, const DevRoot *__restrict__ roots,
                         const unsigned long long *__restrict__ key,
                         const unsigned long long *__restrict__ ext, const int *__restrict__ sgid,
                         const signed char *__restrict__ lcp, const int *__restrict__ base,
-                        const int *__restrict__ perm)
+                        const int *__restrict__ perm, int *__restrict__ leaf_of)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const int na = sc->n_alive;
@@ -531,6 +562,12 @@ __global__ void k_nodes(csgd_t dd, DevScalars *sc, const DevRoot *__restrict__ r
             dev_fail(sc, CSG_ERR_NODE_CAPACITY);
         if (na == 0) { // empty root, reference src/octree.c:141-144
             write_cell(dd, sc, 1.0, 0, -1, 0, 0, 0, 1, -1);
+            double2 *w = (double2 *)&dd.w64[0];
+            w[0] = w[1] = make_double2(0.0, 0.0);
+            float4 *v = (float4 *)&dd.w32[0];
+            v[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+            v[1] = make_float4(0.f, 0.f, 0.f, dd.w32[0].s2);
+            dd.minidx[0] = make_int2(INT_MAX, INT_MAX);
             return;
         }
     }
@@ -551,6 +588,9 @@ __global__ void k_nodes(csgd_t dd, DevScalars *sc, const DevRoot *__restrict__ r
         int hi = (Q == CSG_MAX_LEVEL) ? search_hi(key, ext, sgid, na, p, CSG_MAX_LEVEL) : p;
         int parent = parent_id(key, ext, sgid, lcp, base, p, P, L, id);
         write_cell(dd, sc, hs0, id, parent, L, p, hi - p + 1, id + 1, perm[p]);
+        leaf_of[p] = id;
+    } else {
+        leaf_of[p] = -1;
     }
 }
 
@@ -618,27 +658,47 @@ __global__ void k_link(csgd_t dd, DevScalars *sc, const unsigned long long *__re
     atomicAdd(&dd.nchild[l.parent], 1);
 }
 
-// Bottom-up moments: the last child to finish computes its parent, summing the
-// children in octant order so the result does not depend on scheduling.
+// Bottom-up moments: one thread per leaf (sorted positions that start one);
+// the last child to finish computes its parent, summing the children in
+// octant order so the result does not depend on scheduling. Only the centre
+// of mass and mass fields are written (write_cell set the rest). EXPORT also
+// keeps the two lowest body indices below each cell (the pool export order).
+__device__ __forceinline__ void put_moments(const csgd_t &dd, int node, double sx, double sy,
+                                            double sz, double M)
+{
+    double2 *w = (double2 *)&dd.w64[node];
+    w[0] = make_double2(sx, sy);
+    w[1] = make_double2(sz, M);
+    float4 hi = make_float4((float)sx, (float)sy, (float)sz, (float)M);
+    float *v = (float *)&dd.w32[node];
+    *(float4 *)v = hi;
+    v[4] = (float)(sx - (double)hi.x);
+    v[5] = (float)(sy - (double)hi.y);
+    v[6] = (float)(sz - (double)hi.z);
+}
+
+template <bool EXPORT>
 __global__ void k_moments(csgd_t dd, DevScalars *sc, const double *__restrict__ x,
                           const double *__restrict__ y, const double *__restrict__ z,
-                          const double *__restrict__ m, const int *__restrict__ perm)
+                          const double *__restrict__ m, const int *__restrict__ perm,
+                          const int *__restrict__ leaf_of)
 {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= min(sc->n_nodes, dd.node_cap) || sc->n_nodes > dd.node_cap)
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= sc->n_alive || sc->n_nodes > dd.node_cap)
         return;
-    if (dd.w64[id].body < 0)
+    const int id = leaf_of[p];
+    if (id < 0 || id >= dd.node_cap)
         return;
     NodeLink l = dd.link[id];
     double M, sx, sy, sz;
-    int2 mi;
+    int2 mi = make_int2(INT_MAX, INT_MAX);
     if (l.count == 1) {
         int b = perm[l.first];
         M = m[b];
         sx = x[b];
         sy = y[b];
         sz = z[b];
-        mi = make_int2(b, INT_MAX);
+        mi.x = b;
     } else { // bodies that coincide to depth 64 share one leaf
         M = 0.0;
         double ax = 0.0, ay = 0.0, az = 0.0;
@@ -649,29 +709,17 @@ __global__ void k_moments(csgd_t dd, DevScalars *sc, const double *__restrict__ 
             ay += m[b] * y[b];
             az += m[b] * z[b];
         }
-        sx = ax / M;
-        sy = ay / M;
-        sz = az / M;
+        const double inv = 1.0 / M;
+        sx = ax * inv;
+        sy = ay * inv;
+        sz = az * inv;
         mi = make_int2(perm[l.first], perm[l.first + 1]);
     }
     int node = id;
     while (true) {
-        NodeW64 w = dd.w64[node];
-        w.cx = sx;
-        w.cy = sy;
-        w.cz = sz;
-        w.m = M;
-        dd.w64[node] = w;
-        NodeW32 v = dd.w32[node];
-        v.cx = (float)sx;
-        v.cy = (float)sy;
-        v.cz = (float)sz;
-        v.lx = (float)(sx - (double)v.cx);
-        v.ly = (float)(sy - (double)v.cy);
-        v.lz = (float)(sz - (double)v.cz);
-        v.m = (float)M;
-        dd.w32[node] = v;
-        dd.minidx[node] = mi;
+        put_moments(dd, node, sx, sy, sz, M);
+        if (EXPORT)
+            dd.minidx[node] = mi;
         int parent = dd.link[node].parent;
         if (parent < 0 || parent >= node)
             break; // preorder: a parent always precedes its children
@@ -683,30 +731,37 @@ __global__ void k_moments(csgd_t dd, DevScalars *sc, const double *__restrict__ 
         M = 0.0;
         double ax = 0.0, ay = 0.0, az = 0.0;
         int m1 = INT_MAX, m2 = INT_MAX;
+        const int4 *cp = (const int4 *)(dd.child + 8 * (size_t)parent);
+        const int4 c03 = __ldcg(cp), c47 = __ldcg(cp + 1);
+        const int ch[8] = {c03.x, c03.y, c03.z, c03.w, c47.x, c47.y, c47.z, c47.w};
         for (int q = 0; q < 8; q++) {
-            int c = __ldcg(&dd.child[8 * (size_t)parent + q]);
+            const int c = ch[q];
             if (c < 0)
                 continue;
-            double cm = __ldcg(&dd.w64[c].m);
-            M += cm;
-            ax += cm * __ldcg(&dd.w64[c].cx);
-            ay += cm * __ldcg(&dd.w64[c].cy);
-            az += cm * __ldcg(&dd.w64[c].cz);
-            int2 cmi = __ldcg(&dd.minidx[c]);
-            int cand[2] = {cmi.x, cmi.y};
-            for (int j = 0; j < 2; j++) {
-                int v2 = cand[j];
-                if (v2 < m1) {
-                    m2 = m1;
-                    m1 = v2;
-                } else if (v2 < m2) {
-                    m2 = v2;
+            const double2 *cw = (const double2 *)&dd.w64[c];
+            const double2 xy = __ldcg(cw), zm = __ldcg(cw + 1);
+            M += zm.y;
+            ax += zm.y * xy.x;
+            ay += zm.y * xy.y;
+            az += zm.y * zm.x;
+            if (EXPORT) {
+                int2 cmi = __ldcg(&dd.minidx[c]);
+                int cand[2] = {cmi.x, cmi.y};
+                for (int j = 0; j < 2; j++) {
+                    int v2 = cand[j];
+                    if (v2 < m1) {
+                        m2 = m1;
+                        m1 = v2;
+                    } else if (v2 < m2) {
+                        m2 = v2;
+                    }
                 }
             }
         }
-        sx = ax / M;
-        sy = ay / M;
-        sz = az / M;
+        const double inv = 1.0 / M;
+        sx = ax * inv;
+        sy = ay * inv;
+        sz = az * inv;
         mi = make_int2(m1, m2);
         node = parent;
     }
@@ -1030,7 +1085,9 @@ extern "C" int csgd_build_tree(csgd_t *d, int geometry)
     cudaStream_t s = d->stream;
     DevScalars *sc = d->sc;
     const int B = 256;
-    int rc = order_bodies(d);
+    int rc = geometry ? csgd_ensure_tree_extras(d, 1, 0) : CSG_OK;
+    if (!rc)
+        rc = order_bodies(d);
     if (rc)
         return rc;
     const int g = csgd_grid(n > 0 ? n : 1, B);
@@ -1040,11 +1097,16 @@ extern "C" int csgd_build_tree(csgd_t *d, int geometry)
     rc = csg_scan_exclusive(d, d->cnt, d->base, n, &sc->n_alive);
     if (rc)
         return rc;
-    { k_nodes<<<g, B, 0, s>>>(*d, sc, d->roots, d->key, d->ext, d->sgid, d->lcp, d->base, d->perm); d->launches++; }
+    // d->cnt (the counts, consumed by the scan) now holds each position's leaf
+    { k_nodes<<<g, B, 0, s>>>(*d, sc, d->roots, d->key, d->ext, d->sgid, d->lcp, d->base, d->perm, d->cnt); d->launches++; }
     const int gn = csgd_grid(d->node_cap, B);
     // nodes beyond n_nodes exit at once; the grid covers the capacity
     { k_link<<<gn, B, 0, s>>>(*d, sc, d->key, d->ext); d->launches++; }
-    { k_moments<<<gn, B, 0, s>>>(*d, sc, d->x, d->y, d->z, d->m, d->perm); d->launches++; }
+    if (d->export_order)
+        { k_moments<true><<<g, B, 0, s>>>(*d, sc, d->x, d->y, d->z, d->m, d->perm, d->cnt); d->launches++; }
+    else
+        { k_moments<false><<<g, B, 0, s>>>(*d, sc, d->x, d->y, d->z, d->m, d->perm, d->cnt); d->launches++; }
+    d->minidx_valid = d->export_order;
     { k_tasks<<<min(d->n_gal, 152), 256, 0, s>>>(sc, d->roots, d->n_gal, d->base, d->tasks, d->task_cap, 0); d->launches++; }
     d->geometry_valid = 0;
     d->imported = 0;
@@ -1065,6 +1127,17 @@ extern "C" int csgd_export_pool(csgd_t *d, OctreeNode *pool, int capacity, int *
     cudaStream_t s = d->stream;
     DevScalars *sc = d->sc;
     const int B = 256;
+    int erc = csgd_ensure_tree_extras(d, 1, 1);
+    if (erc)
+        return erc;
+    if (!d->minidx_valid) { // built without the export order: rebuild (same tree) with it
+        const int saved = d->export_order;
+        d->export_order = 1;
+        erc = csgd_build_tree(d, 1);
+        d->export_order = saved;
+        if (erc)
+            return erc;
+    }
     if (!d->geometry_valid) {
         const int gn = csgd_grid(d->node_cap, B);
         { k_geometry<<<gn, B, 0, s>>>(*d, sc, d->roots, d->key, d->ext, d->sgid); d->launches++; }
@@ -1102,6 +1175,9 @@ extern "C" int csgd_import_pool(csgd_t *d, const OctreeNode *pool, int n_nodes, 
     cudaStream_t s = d->stream;
     DevScalars *sc = d->sc;
     const int B = 256;
+    int erc = csgd_ensure_tree_extras(d, 1, 1);
+    if (erc)
+        return erc;
     // The walks take bodies in key order (neighbours share a warp): order the
     // alive bodies as a build would, then replace the cells by the pool's.
     int rc = order_bodies(d);
@@ -1120,5 +1196,6 @@ extern "C" int csgd_import_pool(csgd_t *d, const OctreeNode *pool, int n_nodes, 
     d->geometry_valid = 1;
     d->imported = 1;
     d->gas_valid = 0;
+    d->minidx_valid = 0;
     return csgd_check(d, cudaGetLastError());
 }

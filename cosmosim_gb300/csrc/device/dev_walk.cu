@@ -64,12 +64,18 @@ constexpr int persist_min_blocks(int warps, bool persist) { return (persist ? 24
 // The queued FP64 walk is bound by the FP64 pipe, not by latency: it is sized
 // for fewer resident warps so that its queue state stays in registers.
 #ifndef CSG_W64Q_RESIDENT_WARPS
-#define CSG_W64Q_RESIDENT_WARPS 32
+#define CSG_W64Q_RESIDENT_WARPS 24
 #endif
 constexpr int w64q_min_blocks(int warps, bool persist)
 {
     return (persist ? 24 : CSG_W64Q_RESIDENT_WARPS) / warps;
 }
+
+// Walk statistics: interactions, warp steps and lane-steps of lanes that
+// had not finished (lane utilisation = active / (32 steps)).
+struct WalkStats {
+    unsigned long long hits = 0, steps = 0, active = 0;
+};
 
 // Validated task: bodies [pos0, pos0+count) and the system's cells [root, end).
 struct TaskRange {
@@ -137,7 +143,7 @@ __device__ __forceinline__ double inv_r3_fast(double r2)
 
 template <bool EXACT, bool STATS>
 __device__ __forceinline__ void walk64_task(const WalkArgs &a, NodeW64 *win, const TaskRange &tr,
-                                            unsigned long long &hits)
+                                            WalkStats &st)
 {
     const int lane = threadIdx.x & 31;
     const int nn = tr.end;
@@ -158,6 +164,10 @@ __device__ __forceinline__ void walk64_task(const WalkArgs &a, NodeW64 *win, con
         }
         const NodeW64 c = win[cur - wbase];
         bool open = false;
+        if (STATS) {
+            st.steps++;
+            st.active += (cur >= skip);
+        }
         if (cur >= skip) {
             if (c.m == 0.0) { // empty cell: reference returns at once (src/octree.c:181-182)
                 skip = c.next;
@@ -200,7 +210,7 @@ __device__ __forceinline__ void walk64_task(const WalkArgs &a, NodeW64 *win, con
                         sz = fma(f, dz, sz);
                     }
                     if (STATS)
-                        hits++;
+                        st.hits++;
                 }
             }
         }
@@ -218,11 +228,16 @@ __device__ __forceinline__ void walk64_task(const WalkArgs &a, NodeW64 *win, con
     }
 }
 
-__device__ __forceinline__ void add_hits(const WalkArgs &a, unsigned long long hits)
+__device__ __forceinline__ void add_hits(const WalkArgs &a, const WalkStats &w)
 {
-    unsigned int h = __reduce_add_sync(0xffffffffu, (unsigned int)hits);
-    if ((threadIdx.x & 31) == 0 && h)
-        atomicAdd(&a.sc->interactions, (unsigned long long)h);
+    unsigned int h = __reduce_add_sync(0xffffffffu, (unsigned int)w.hits);
+    unsigned int ac = __reduce_add_sync(0xffffffffu, (unsigned int)w.active);
+    if ((threadIdx.x & 31) == 0) {
+        if (h)
+            atomicAdd(&a.sc->interactions, (unsigned long long)h);
+        atomicAdd(&a.sc->walk_steps, w.steps);
+        atomicAdd(&a.sc->walk_active, (unsigned long long)ac);
+    }
 }
 
 template <bool EXACT, bool STATS>
@@ -230,10 +245,10 @@ __global__ void __launch_bounds__(8 * CSG_WARP) k_walk64(WalkArgs a)
 {
     __shared__ NodeW64 win_all[8][CSG_WARP];
     NodeW64 *win = win_all[threadIdx.x >> 5];
-    unsigned long long hits = 0;
-    for_each_task<8, false>(a, [&](const TaskRange &tr) { walk64_task<EXACT, STATS>(a, win, tr, hits); });
+    WalkStats st;
+    for_each_task<8, false>(a, [&](const TaskRange &tr) { walk64_task<EXACT, STATS>(a, win, tr, st); });
     if (STATS)
-        add_hits(a, hits);
+        add_hits(a, st);
 }
 
 // m/r^3 for the queued FP64 walk, with few FP64 operations (the FP64 pipe
@@ -241,7 +256,8 @@ __global__ void __launch_bounds__(8 * CSG_WARP) k_walk64(WalkArgs a)
 // < 2^-21), y0^2 exact in FP64, e = 1 - r2*y0^2 by one fused multiply-add,
 // then m/r^3 = m*y0^3 * (1-e)^-3/2 = m*y0^3 * (1 + e(3/2 + 15/8 e)) (the
 // series to second order; the next term is < 2^-60). Range check on the FP32
-// value; outside it the plain expression.
+// value; outside it the plain expression. (Forming 15/8 e^2 in FP32 instead
+// saves one FP64 operation but its two conversions cost more on this GPU.)
 __device__ __forceinline__ double m_inv_r3_q(double m, double r2)
 {
     const float r2f = (float)r2;
@@ -321,8 +337,8 @@ __device__ __forceinline__ Cell load_cell(const WalkArgs &a, NodeW32 *win, int &
 
 // Visits the preorder tree for the warp's 32 bodies; calls take(cell, dx, dy,
 // dz, d2, cur) (under a warp-uniform "some lane takes" branch) for every cell
-// the lane interacts with, in the reference's depth-first order; after(cur)
-// runs once per step for the whole warp. EMPTY: cells of zero mass may occur
+// the lane interacts with, in the reference's depth-first order; after(cur,
+// active) runs once per step for the whole warp. EMPTY: cells of zero mass may occur
 // (caller pools); the reference skips them with everything below.
 template <bool EMPTY, typename Take, typename After>
 __device__ __forceinline__ void walk_cells(const WalkArgs &a, NodeW32 *win, int root, int nn,
@@ -339,7 +355,7 @@ __device__ __forceinline__ void walk_cells(const WalkArgs &a, NodeW32 *win, int 
             if (a.w64[cur].m == 0.0) { // empty cell (src/octree.c:181-182)
                 if (active)
                     skip = c.next;
-                after_fn(cur);
+                after_fn(cur, active);
                 if (c.next <= cur) {
                     dev_fail(a.sc, CSG_ERR_WALK_LIMIT);
                     break;
@@ -352,8 +368,17 @@ __device__ __forceinline__ void walk_cells(const WalkArgs &a, NodeW32 *win, int 
         const float dy = (c.A.y - b.hy) + (c.B.y - b.ly);
         const float dz = (c.A.z - b.hz) + (c.B.z - b.lz);
         const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        if (c.body >= 0) { // leaf (warp-uniform)
+        if (c.body >= 0) { // leaf (warp-uniform): no lane can open it, no vote
             take = active && c.body != me;
+            if (__any_sync(0xffffffffu, take))
+                take_fn(take, c, dx, dy, dz, d2, cur);
+            after_fn(cur, active);
+            if (c.next <= cur) {
+                dev_fail(a.sc, CSG_ERR_WALK_LIMIT);
+                break;
+            }
+            cur = c.next;
+            continue;
         } else {
             const float lhs = a.theta2f * d2;
             const float band = c.B.w * a.guard_rel;
@@ -370,7 +395,7 @@ __device__ __forceinline__ void walk_cells(const WalkArgs &a, NodeW32 *win, int 
         }
         if (__any_sync(0xffffffffu, take))
             take_fn(take, c, dx, dy, dz, d2, cur);
-        after_fn(cur);
+        after_fn(cur, active);
         const int nxt = __any_sync(0xffffffffu, open) ? cur + 1 : c.next;
         if (nxt <= cur) { // a malformed tree must not loop
             dev_fail(a.sc, CSG_ERR_WALK_LIMIT);
@@ -393,7 +418,7 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v)
 // compensation (per-body compensated FP32 summation); G applied once.
 template <bool STATS, bool EMPTY>
 __device__ __forceinline__ void walk32_task(const WalkArgs &a, NodeW32 *win, const TaskRange &tr,
-                                            unsigned long long &hits)
+                                            WalkStats &st)
 {
     const int lane = threadIdx.x & 31;
     const int nn = tr.end;
@@ -409,6 +434,22 @@ __device__ __forceinline__ void walk32_task(const WalkArgs &a, NodeW32 *win, con
     int nblk = 0;
     int skip = valid ? 0 : INT_MAX;
     int cur = tr.root, wbase = INT_MIN / 2;
+    auto interact = [&](const NodeW32 &c, float dx, float dy, float dz, float d2) {
+        const float y = rsqrtf(d2 + a.eps2f);
+        const float f = c.m * (y * y * y);
+        bx = fmaf(f, dx, bx);
+        by = fmaf(f, dy, by);
+        bz = fmaf(f, dz, bz);
+        if (++nblk == 8) { // compensated add of the block
+            kahan_add(sx, cx, bx);
+            kahan_add(sy, cy, by);
+            kahan_add(sz, cz, bz);
+            bx = by = bz = 0.f;
+            nblk = 0;
+        }
+        if (STATS)
+            st.hits++;
+    };
     while (cur < nn) {
         if (cur - wbase >= CSG_WARP) {
             wbase = cur;
@@ -418,6 +459,26 @@ __device__ __forceinline__ void walk32_task(const WalkArgs &a, NodeW32 *win, con
             __syncwarp();
         }
         const NodeW32 c = win[cur - wbase];
+        if (STATS) {
+            st.steps++;
+            st.active += (cur >= skip);
+        }
+        if (c.body >= 0) {
+            // a leaf (warp-uniform): nothing below it to open, so no vote;
+            // every lane still walking takes it unless it is its own body
+            if (cur >= skip && c.body != me && !(EMPTY && c.m == 0.0f && a.w64[cur].m == 0.0)) {
+                const float dx = (c.cx - hx) + (c.lx - lx);
+                const float dy = (c.cy - hy) + (c.ly - ly);
+                const float dz = (c.cz - hz) + (c.lz - lz);
+                interact(c, dx, dy, dz, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
+            }
+            if (c.next <= cur) {
+                dev_fail(a.sc, CSG_ERR_WALK_LIMIT);
+                break;
+            }
+            cur = c.next;
+            continue;
+        }
         bool open = false;
         if (cur >= skip) {
             if (EMPTY && c.m == 0.0f && a.w64[cur].m == 0.0) {
@@ -427,40 +488,22 @@ __device__ __forceinline__ void walk32_task(const WalkArgs &a, NodeW32 *win, con
                 const float dy = (c.cy - hy) + (c.ly - ly);
                 const float dz = (c.cz - hz) + (c.lz - lz);
                 const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                // |theta^2 d^2 - s^2| inside the FP32 error band -> decide in FP64
+                const float lhs = a.theta2f * d2;
+                const float band = c.s2 * a.guard_rel;
                 bool take;
-                if (c.body >= 0) {
-                    take = (c.body != me);
-                } else {
-                    // |theta^2 d^2 - s^2| inside the FP32 error band -> decide in FP64
-                    const float lhs = a.theta2f * d2;
-                    const float band = c.s * a.guard_abs + c.s2 * a.guard_rel;
-                    if (c.s2 < lhs - band && d2 > 0.f) {
-                        take = true;
-                    } else if (c.s2 > lhs + band) {
-                        take = false;
-                    } else { // rare: decided by the reference's FP64 test, out of line
-                        take = decide64(a, cur, px, py, pz);
-                    }
-                    if (take)
-                        skip = c.next;
-                    else
-                        open = true;
+                if (c.s2 < lhs - band && d2 > 0.f) {
+                    take = true;
+                } else if (c.s2 > lhs + band) {
+                    take = false;
+                } else { // rare: decided by the reference's FP64 test, out of line
+                    take = decide64(a, cur, px, py, pz);
                 }
                 if (take) {
-                    const float y = rsqrtf(d2 + a.eps2f);
-                    const float f = c.m * (y * y * y);
-                    bx = fmaf(f, dx, bx);
-                    by = fmaf(f, dy, by);
-                    bz = fmaf(f, dz, bz);
-                    if (++nblk == 8) { // compensated add of the block
-                        kahan_add(sx, cx, bx);
-                        kahan_add(sy, cy, by);
-                        kahan_add(sz, cz, bz);
-                        bx = by = bz = 0.f;
-                        nblk = 0;
-                    }
-                    if (STATS)
-                        hits++;
+                    skip = c.next;
+                    interact(c, dx, dy, dz, d2);
+                } else {
+                    open = true;
                 }
             }
         }
@@ -486,10 +529,10 @@ __global__ void __launch_bounds__(WARPS * CSG_WARP, persist_min_blocks(WARPS, PE
 {
     __shared__ NodeW32 win_all[WARPS][CSG_WARP];
     NodeW32 *win = win_all[threadIdx.x >> 5];
-    unsigned long long hits = 0;
-    for_each_task<WARPS, PERSIST>(a, [&](const TaskRange &tr) { walk32_task<STATS, EMPTY>(a, win, tr, hits); });
+    WalkStats st;
+    for_each_task<WARPS, PERSIST>(a, [&](const TaskRange &tr) { walk32_task<STATS, EMPTY>(a, win, tr, st); });
     if (STATS)
-        add_hits(a, hits);
+        add_hits(a, st);
 }
 
 // FP64 walk with dense evaluation. The traversal is walk_cells (decisions
@@ -527,7 +570,7 @@ __device__ __forceinline__ void q64_eval(const WalkArgs &a, const int *q, int la
 
 template <bool STATS, bool EMPTY>
 __device__ __forceinline__ void walk64q_task(const WalkArgs &a, NodeW32 *win, int *q,
-                                             const TaskRange &tr, unsigned long long &hits)
+                                             const TaskRange &tr, WalkStats &st)
 {
     const int lane = threadIdx.x & 31;
     const bool valid = lane < tr.count;
@@ -541,10 +584,14 @@ __device__ __forceinline__ void walk64q_task(const WalkArgs &a, NodeW32 *win, in
                 q[(tail & (Q64 - 1)) * CSG_WARP + lane] = cur;
                 tail++;
                 if (STATS)
-                    hits++;
+                    st.hits++;
             }
         },
-        [&](int) {
+        [&](int, bool active) {
+            if (STATS) {
+                st.steps++;
+                st.active += active;
+            }
             const int cnt = tail - head; // 0..Q64-1; always 0 for a lane without a body
             const int cmin = (int)__reduce_min_sync(0xffffffffu, (unsigned)(valid ? cnt : INT_MAX));
             const int cmax = (int)__reduce_max_sync(0xffffffffu, (unsigned)cnt);
@@ -570,10 +617,10 @@ __global__ void __launch_bounds__(WARPS * CSG_WARP, w64q_min_blocks(WARPS, PERSI
     const int warp = threadIdx.x >> 5;
     int *q = q_all[warp];
     NodeW32 *win = win_all[warp];
-    unsigned long long hits = 0;
-    for_each_task<WARPS, PERSIST>(a, [&](const TaskRange &tr) { walk64q_task<STATS, EMPTY>(a, win, q, tr, hits); });
+    WalkStats st;
+    for_each_task<WARPS, PERSIST>(a, [&](const TaskRange &tr) { walk64q_task<STATS, EMPTY>(a, win, q, tr, st); });
     if (STATS)
-        add_hits(a, hits);
+        add_hits(a, st);
 }
 
 // Dead bodies get a = 0 (src/octree.c:226-230); alive ones are overwritten by
@@ -620,7 +667,7 @@ __global__ void __launch_bounds__(8 * CSG_WARP) k_walk_lists(WalkArgs a, int *co
                     k++;
                 }
             },
-            [&](int) {});
+            [&](int, bool) {});
         if (!FILL && valid)
             counts[me] = k;
     });

@@ -15,6 +15,8 @@ csgd_t *csg_thread_dev(void)
 {
     if (!tl_dev) {
         tl_dev = csgd_create();
+        if (tl_dev) /* the free functions export the tree into the caller's pool */
+            csgd_set_export_order(tl_dev, 1);
         if (!tl_dev)
             tl_error = CSG_ERR_NO_DEVICE;
     }

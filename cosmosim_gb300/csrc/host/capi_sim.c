@@ -530,6 +530,15 @@ CSG_EXPORT int cosmosim_interactions(SimHandle handle, int64_t *total)
     return set_err(s, csgd_interactions(s->dev, total));
 }
 
+CSG_EXPORT int cosmosim_walk_stats(SimHandle handle, int64_t *interactions, int64_t *warp_steps,
+                                   int64_t *active_lane_steps)
+{
+    if (!handle || !interactions || !warp_steps || !active_lane_steps)
+        return CSG_ERR_BAD_ARG;
+    SimState *s = (SimState *)handle;
+    return set_err(s, csgd_walk_stats(s->dev, interactions, warp_steps, active_lane_steps));
+}
+
 CSG_EXPORT int cosmosim_node_count(SimHandle handle, int *n_nodes)
 {
     if (!handle || !n_nodes)

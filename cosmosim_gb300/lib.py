@@ -75,6 +75,8 @@ _SIGS = {
     "cosmosim_enable_stats": ([_vp, _i], _i),
     "cosmosim_interactions": ([_vp, ctypes.POINTER(ctypes.c_int64)], _i),
     "cosmosim_node_count": ([_vp, _ip], _i),
+    "cosmosim_walk_stats": ([_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                             ctypes.POINTER(ctypes.c_int64)], _i),
     "cosmosim_set_precision": ([_vp, _i], _i),
     "csg_last_error": ([], _i),
     "csg_error_string": ([_i], ctypes.c_char_p),
@@ -313,6 +315,12 @@ class Sim:
         v = ctypes.c_int64(0)
         self._rc(self.lib.cosmosim_interactions(self.h, ctypes.byref(v)), "interactions")
         return v.value
+
+    def walk_stats(self):
+        """(interactions, warp steps, active lane-steps) since enable_stats."""
+        v = [ctypes.c_int64(0) for _ in range(3)]
+        self._rc(self.lib.cosmosim_walk_stats(self.h, *[ctypes.byref(x) for x in v]), "walk_stats")
+        return tuple(x.value for x in v)
 
     def node_count(self):
         v = ctypes.c_int(0)

@@ -146,6 +146,11 @@ CSG_EXPORT int cosmosim_gravity_async(SimHandle handle);
 /* Interaction counting (accepted cells + leaves, the reference walk's unit). */
 CSG_EXPORT int cosmosim_enable_stats(SimHandle handle, int on);
 CSG_EXPORT int cosmosim_interactions(SimHandle handle, int64_t *total);
+/* The same counters with the walks' warp steps (one cell visited by a warp)
+   and the lane-steps of lanes that had not finished: active / (32 steps) is
+   the walk's lane utilisation. */
+CSG_EXPORT int cosmosim_walk_stats(SimHandle handle, int64_t *interactions, int64_t *warp_steps,
+                                   int64_t *active_lane_steps);
 CSG_EXPORT int cosmosim_node_count(SimHandle handle, int *n_nodes);
 CSG_EXPORT int cosmosim_set_precision(SimHandle handle, int precision);
 
