@@ -66,6 +66,18 @@ int csgd_autotune_walk(csgd_t *d, const csgd_force_params *p, int reps, CsgWalkS
 /* Body array-of-structs <-> device SoA (host buffers may be pageable). */
 int csgd_upload_bodies(csgd_t *d, const Body *host, int n);
 int csgd_download_bodies(csgd_t *d, Body *host, int n);
+/* Refreshes the device Body staging from the SoA fields (no copy to the host). */
+int csgd_pack_aos(csgd_t *d);
+
+/* Alive bodies (mass <= 0 skipped) as packed float records, in index order,
+   at most max_bodies: CSG_SNAPSHOT_UE (16 floats) or CSG_SNAPSHOT_RENDER (10).
+   out is a device pointer when out_is_device, else host memory. Blocks. */
+int csgd_snapshot_f32(csgd_t *d, int format, float *out, int out_is_device, int max_bodies,
+                      int *count_out);
+
+/* Drops bodies whose mass is not > 0, keeping the order of the rest
+   (reference src/quasar.c:511-523); *new_n is the new count. Blocks. */
+int csgd_compact(csgd_t *d, int *new_n);
 
 /* Tree build over the current positions/masses. With geometry != 0 it also
    computes every cell's geometric centre (needed by SPH and pool export). */

@@ -167,6 +167,7 @@ struct csgd {
 
     DevScalars *sc;      // device
     DevScalars *sc_host; // pinned mirror
+    int *h_int;          // pinned scratch for single values read back (4 ints)
     int geometry_valid;
     // captured substep (cosmosim_substeps_async path)
     cudaGraphExec_t graph;

@@ -37,12 +37,13 @@ __global__ void k_unpack(const Body *__restrict__ b, int n, double *x, double *y
     h[i] = q.smoothing_h;
 }
 
-// Writes back the fields the hot path changes; mass, type and the quasar
-// fields keep the values that were uploaded.
+// Writes back the fields kept in SoA; the quasar fields (spin, accretion
+// rate, luminosity, lifetime) keep the values the staging copy holds.
 __global__ void k_pack(Body *__restrict__ b, int n, const double *x, const double *y,
                        const double *z, const double *vx, const double *vy, const double *vz,
                        const double *ax, const double *ay, const double *az, const double *rho,
-                       const double *P, const double *u, const double *h)
+                       const double *P, const double *u, const double *h, const double *m,
+                       const int *type)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
@@ -61,6 +62,8 @@ __global__ void k_pack(Body *__restrict__ b, int n, const double *x, const doubl
     q.pressure = P[i];
     q.internal_energy = u[i];
     q.smoothing_h = h[i];
+    q.mass = m[i];
+    q.type = (BodyType)type[i];
 }
 
 // Half kick and drift, src/integrator.c:22-31.
@@ -255,9 +258,12 @@ extern "C" csgd_t *csgd_create(void)
         return nullptr;
     }
     if (cudaMalloc((void **)&d->sc, sizeof(DevScalars)) != cudaSuccess ||
-        cudaMallocHost((void **)&d->sc_host, sizeof(DevScalars)) != cudaSuccess) {
+        cudaMallocHost((void **)&d->sc_host, sizeof(DevScalars)) != cudaSuccess ||
+        cudaMallocHost((void **)&d->h_int, 4 * sizeof(int)) != cudaSuccess) {
         if (d->sc)
             cudaFree(d->sc);
+        if (d->sc_host)
+            cudaFreeHost(d->sc_host);
         cudaFree(d->roots);
         cudaStreamDestroy(d->own_stream);
         free(d);
@@ -290,6 +296,8 @@ extern "C" void csgd_destroy(csgd_t *d)
         cudaFree(d->roots);
     if (d->sc_host)
         cudaFreeHost(d->sc_host);
+    if (d->h_int)
+        cudaFreeHost(d->h_int);
     if (d->own_stream)
         cudaStreamDestroy(d->own_stream);
     free(d);
@@ -520,6 +528,17 @@ extern "C" int csgd_upload_bodies(csgd_t *d, const Body *host, int n)
     return csgd_check(d, cudaGetLastError());
 }
 
+extern "C" int csgd_pack_aos(csgd_t *d)
+{
+    const int n = d->n;
+    if (n <= 0)
+        return CSG_OK;
+    { k_pack<<<csgd_grid(n, 256), 256, 0, d->stream>>>(d->aos, n, d->x, d->y, d->z, d->vx, d->vy,
+                                                      d->vz, d->ax, d->ay, d->az, d->rho, d->P,
+                                                      d->u, d->h, d->m, d->type); d->launches++; }
+    return csgd_check(d, cudaGetLastError());
+}
+
 extern "C" int csgd_download_bodies(csgd_t *d, Body *host, int n)
 {
     if (n > d->n || n < 0) {
@@ -528,9 +547,9 @@ extern "C" int csgd_download_bodies(csgd_t *d, Body *host, int n)
     }
     if (n == 0)
         return CSG_OK;
-    { k_pack<<<csgd_grid(n, 256), 256, 0, d->stream>>>(d->aos, n, d->x, d->y, d->z, d->vx, d->vy,
-                                                      d->vz, d->ax, d->ay, d->az, d->rho, d->P,
-                                                      d->u, d->h); d->launches++; }
+    int rc = csgd_pack_aos(d);
+    if (rc)
+        return rc;
     cudaMemcpyAsync(host, d->aos, sizeof(Body) * (size_t)n, cudaMemcpyDeviceToHost, d->stream);
     return csgd_check(d, cudaGetLastError());
 }

@@ -29,7 +29,6 @@
 extern QuasarConfig quasar_default_config(void) __attribute__((weak));
 extern void quasar_step(Body *bodies, int *n, int n_alloc, QuasarConfig *cfg, double dt)
     __attribute__((weak));
-extern int quasar_compact(Body *bodies, int n) __attribute__((weak));
 extern void generate_spiral_galaxy(Body *bodies, int n, double cx, double cy, double galaxy_mass,
                                    double disk_radius, double vx_bulk, double vy_bulk)
     __attribute__((weak));
@@ -148,7 +147,7 @@ CSG_EXPORT SimHandle cosmosim_create_ex(CosmosimConfig config, double G, double 
     int n_dust = (config.merger && config.quasar) ? n / 5 : 0;
     int n_alloc = config.quasar ? n + n_dust + n / 4 : n;
     if (config.quasar &&
-        (!quasar_step || !quasar_default_config || !quasar_compact || !generate_quasar_galaxy ||
+        (!quasar_step || !quasar_default_config || !generate_quasar_galaxy ||
          !generate_quasar_merger || !generate_merger_dust)) {
         csg_thread_set_error(CSG_ERR_UNSUPPORTED); /* the CPU quasar step is not linked */
         return NULL;
@@ -380,13 +379,10 @@ CSG_EXPORT void cosmosim_step(SimHandle handle)
         }
     }
     if (!rc && s->quasar && ++s->compact_counter >= 60) { /* src/cosmosim_api.c:133-142 */
-        rc = csgd_download_bodies(s->dev, s->host, s->current_n);
+        int n = s->current_n; /* quasar_compact's semantics, on the device */
+        rc = csgd_compact(s->dev, &n);
         if (!rc)
-            rc = csgd_sync(s->dev);
-        if (!rc) {
-            s->current_n = quasar_compact(s->host, s->current_n);
-            rc = csgd_upload_bodies(s->dev, s->host, s->current_n);
-        }
+            s->current_n = n;
         s->compact_counter = 0;
     }
     if (!rc)
@@ -444,6 +440,35 @@ CSG_EXPORT int cosmosim_set_bodies(SimHandle handle, const Body *bodies, int n)
     int rc = csgd_upload_bodies(s->dev, bodies, n);
     s->host_stale = 1;
     return set_err(s, rc);
+}
+
+CSG_EXPORT int cosmosim_snapshot_f32(SimHandle handle, int format, float *out, int out_is_device,
+                                     int max_bodies)
+{
+    if (!handle)
+        return -1;
+    SimState *s = (SimState *)handle;
+    int count = 0;
+    int rc = csgd_snapshot_f32(s->dev, format, out, out_is_device, max_bodies, &count);
+    if (rc)
+        csgd_sync(s->dev); /* clears a recorded argument error */
+    set_err(s, rc);
+    return rc ? -1 : count;
+}
+
+CSG_EXPORT int cosmosim_compact(SimHandle handle)
+{
+    if (!handle)
+        return -1;
+    SimState *s = (SimState *)handle;
+    int n = s->current_n;
+    int rc = csgd_compact(s->dev, &n);
+    if (!rc) {
+        s->current_n = n;
+        s->host_stale = 1;
+    }
+    set_err(s, rc);
+    return rc ? -1 : n;
 }
 
 CSG_EXPORT int cosmosim_get_count(SimHandle handle)

@@ -70,6 +70,8 @@ _SIGS = {
     "cosmosim_set_stream": ([_vp, _vp], _i),
     "cosmosim_copy_bodies": ([_vp, _vp, _i], _i),
     "cosmosim_set_bodies": ([_vp, _vp, _i], _i),
+    "cosmosim_snapshot_f32": ([_vp, _i, _vp, _i, _i], _i),
+    "cosmosim_compact": ([_vp], _i),
     "cosmosim_build_tree_async": ([_vp], _i),
     "cosmosim_gravity_async": ([_vp], _i),
     "cosmosim_enable_stats": ([_vp, _i], _i),
@@ -349,6 +351,26 @@ class Sim:
         """Uploads bodies into the handle (cosmosim_set_bodies; asynchronous:
         keep `bodies` alive and unchanged until the next sync)."""
         self._rc(self.lib.cosmosim_set_bodies(self.h, ptr(bodies), len(bodies)), "set_bodies")
+
+    def snapshot(self, fmt=0, max_bodies=None, device_out=None):
+        """Alive bodies as float records (cosmosim_snapshot_f32): fmt 0 = 16
+        floats (FCosmosimBodyGPU), 1 = 10 floats (renderer). Into a new numpy
+        array, or into device_out (a device pointer) when given."""
+        stride = 16 if fmt == 0 else 10
+        cap = self.count if max_bodies is None else max_bodies
+        if device_out is not None:
+            k = self.lib.cosmosim_snapshot_f32(self.h, fmt, ctypes.c_void_p(device_out), 1, cap)
+            self._rc(0 if k >= 0 else self.lib.cosmosim_last_error(self.h), "snapshot")
+            return k
+        out = np.zeros((max(cap, 1), stride), dtype=np.float32)
+        k = self.lib.cosmosim_snapshot_f32(self.h, fmt, ptr(out), 0, cap)
+        self._rc(0 if k >= 0 else self.lib.cosmosim_last_error(self.h), "snapshot")
+        return out[:k].copy()
+
+    def compact(self):
+        k = self.lib.cosmosim_compact(self.h)
+        self._rc(0 if k >= 0 else self.lib.cosmosim_last_error(self.h), "compact")
+        return k
 
     def get_bodies_view(self):
         """The borrowed array cosmosim_get_bodies returns, copied into numpy."""

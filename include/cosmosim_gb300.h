@@ -128,6 +128,28 @@ CSG_EXPORT int cosmosim_enable_graphs(SimHandle handle, int on);
 /* Runs the handle's work on the given cudaStream_t (NULL: its own stream). */
 CSG_EXPORT int cosmosim_set_stream(SimHandle handle, void *cuda_stream);
 
+/* Snapshot of the alive bodies as packed float records, built on the GPU —
+   no counterpart in the reference, whose consumers convert the Body array
+   on the host:
+     CSG_SNAPSHOT_UE      16 floats per body, the Unreal plugin's
+                          FCosmosimBodyGPU (pos, mass, vel, type, internal
+                          energy, density, lifetime, luminosity, spin, 0);
+     CSG_SNAPSHOT_RENDER  10 floats per body, the renderer's vertex record
+                          (pos, mass, vel, type, internal energy, density).
+   Bodies with mass <= 0 are skipped; index order; at most max_bodies.
+   out_is_device: out is a device pointer (e.g. a graphics-interop buffer),
+   else host memory. Returns the number of records written, or -1 (see
+   cosmosim_last_error). Blocking. */
+#define CSG_SNAPSHOT_UE 0
+#define CSG_SNAPSHOT_RENDER 1
+CSG_EXPORT int cosmosim_snapshot_f32(SimHandle handle, int format, float *out, int out_is_device,
+                                     int max_bodies);
+
+/* Drops the dead bodies (mass not > 0) of a handle on the GPU, keeping the
+   order of the others (the reference's quasar_compact, src/quasar.c:511-523).
+   Returns the new count, or -1. Blocking. */
+CSG_EXPORT int cosmosim_compact(SimHandle handle);
+
 /* Copies the bodies out (n must equal cosmosim_get_count). */
 CSG_EXPORT int cosmosim_copy_bodies(SimHandle handle, Body *out, int n);
 
