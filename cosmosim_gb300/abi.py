@@ -56,6 +56,19 @@ class CosmosimConfig(ctypes.Structure):
 assert ctypes.sizeof(CosmosimConfig) == 72
 
 
+class QuasarConfig(ctypes.Structure):
+    """reference src/quasar.h:6-22 (104 bytes)."""
+
+    _fields_ = [(f, ctypes.c_double) for f in (
+        "accretion_radius", "swallow_radius", "isco_radius", "viscosity_alpha", "jet_speed",
+        "jet_mass", "jet_lifetime", "feedback_strength", "eta_eff", "eddington_k",
+        "accretion_smoothing")] + [(f, ctypes.c_int) for f in (
+            "jet_cap", "jet_count", "max_bodies", "jet_ring_count")]
+
+
+assert ctypes.sizeof(QuasarConfig) == 104
+
+
 def new_bodies(n):
     """Zeroed Body array (what calloc gives the reference's callers)."""
     return np.zeros(n, dtype=BODY_DTYPE)

@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-fvisibility=hidden", "--expt-relaxed-constexpr"]
 # Kernels that must round exactly like the reference's C (no fused multiply-add).
-NO_FMA = {"dev_state.cu", "dev_sph.cu"}
+NO_FMA = {"dev_state.cu", "dev_sph.cu", "dev_quasar.cu"}
 CC_FLAGS = ["-std=c11", "-O2", "-fPIC", "-fvisibility=hidden", "-Wall", "-Wextra",
             "-Wno-unused-parameter"]
 

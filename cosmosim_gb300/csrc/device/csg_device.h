@@ -75,6 +75,16 @@ int csgd_pack_aos(csgd_t *d);
 int csgd_snapshot_f32(csgd_t *d, int format, float *out, int out_is_device, int max_bodies,
                       int *count_out);
 
+/* Quasar step on the device (reference src/quasar.c:477-509): may append
+   bodies up to n_alloc (<= the reserved capacity); *jet_count is read and
+   updated (the reference's cfg->jet_count); *n_out gets the new body count.
+   The generator state and knot phase persist in the state between steps;
+   csgd_quasar_state sets them (defaults 1 and 0, as the reference starts).
+   Blocks (the host needs the new count). */
+int csgd_quasar_step(csgd_t *d, const QuasarConfig *cfg, int n_alloc, double dt,
+                     int *jet_count, int *n_out);
+int csgd_quasar_state(csgd_t *d, unsigned long long rng, int knot_phase);
+
 /* Drops bodies whose mass is not > 0, keeping the order of the rest
    (reference src/quasar.c:511-523); *new_n is the new count. Blocks. */
 int csgd_compact(csgd_t *d, int *new_n);

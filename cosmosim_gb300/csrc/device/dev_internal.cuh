@@ -101,6 +101,17 @@ struct DevScalars {
     int alive_count;                     // csgd_alive_count result
 };
 
+// Quasar step state kept on the device between steps (the reference keeps
+// the generator state and the knot phase in file statics, src/quasar.c:11
+// and :224; the live jet count in its QuasarConfig).
+struct QuasarState {
+    unsigned long long rng;
+    int knot_phase;
+    int jet_count;
+    int n;      // bodies in use (the step appends jets and lobes)
+    int n_smbh; // bodies of type SMBH found by the current step
+};
+
 struct csgd {
     cudaStream_t stream;
     cudaStream_t own_stream;
@@ -168,6 +179,7 @@ struct csgd {
     DevScalars *sc;      // device
     DevScalars *sc_host; // pinned mirror
     int *h_int;          // pinned scratch for single values read back (4 ints)
+    QuasarState *qs;     // device, allocated by the first quasar step
     int geometry_valid;
     // captured substep (cosmosim_substeps_async path)
     cudaGraphExec_t graph;

@@ -298,6 +298,8 @@ extern "C" void csgd_destroy(csgd_t *d)
         cudaFreeHost(d->sc_host);
     if (d->h_int)
         cudaFreeHost(d->h_int);
+    if (d->qs)
+        cudaFree(d->qs);
     if (d->own_stream)
         cudaStreamDestroy(d->own_stream);
     free(d);

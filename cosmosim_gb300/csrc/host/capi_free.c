@@ -225,3 +225,39 @@ CSG_EXPORT void sph_apply_cooling(Body *bodies, int n, double dt)
         rc = csgd_sync(d);
     csg_thread_set_error(rc);
 }
+
+/* ---- quasar step (reference src/quasar.c:477-509) on the GPU ---------------- */
+
+CSG_EXPORT void csg_quasar_step(Body *bodies, int *n, int n_alloc, QuasarConfig *cfg, double dt)
+{
+    csgd_t *d = csg_thread_dev();
+    if (!d)
+        return;
+    if (!bodies || !n || !cfg || *n < 0 || n_alloc < *n) {
+        csg_thread_set_error(CSG_ERR_BAD_ARG);
+        return;
+    }
+    int new_n = *n, jets = cfg->jet_count;
+    int rc = csgd_reserve(d, n_alloc > 0 ? n_alloc : 1); /* room for appended jets */
+    if (!rc)
+        rc = csgd_upload_bodies(d, bodies, *n);
+    if (!rc)
+        rc = csgd_quasar_step(d, cfg, n_alloc, dt, &jets, &new_n);
+    if (!rc)
+        rc = csgd_download_bodies(d, bodies, new_n);
+    if (!rc)
+        rc = csgd_sync(d);
+    if (!rc) {
+        *n = new_n;
+        cfg->jet_count = jets;
+    }
+    csg_thread_set_error(rc);
+}
+
+CSG_EXPORT void csg_quasar_seed(uint64_t rng_state, int knot_phase)
+{
+    csgd_t *d = csg_thread_dev();
+    if (!d)
+        return;
+    csg_thread_set_error(csgd_quasar_state(d, (unsigned long long)rng_state, knot_phase));
+}

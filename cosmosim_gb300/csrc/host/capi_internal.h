@@ -25,5 +25,15 @@ int csg_pool_extent(const OctreeNode *pool, int root, int *n_nodes);
 
 /* Seeded initial conditions (ics.c). */
 int csg_generate_ics_impl(int kind, int n, uint64_t seed, Body *out);
+void csg_ref_spiral(Body *bodies, int n, double cx, double cy, double galaxy_mass,
+                    double disk_radius, double vx_bulk, double vy_bulk, uint64_t seed);
+void csg_ref_merger(Body *bodies, int n, double separation, double approach_vel, uint64_t seed);
+void csg_ref_quasar_galaxy(Body *bodies, int n, double cx, double cy, double galaxy_mass,
+                           double disk_radius, double vx_bulk, double vy_bulk,
+                           double smbh_mass_frac, uint64_t seed);
+void csg_ref_quasar_merger(Body *bodies, int n, double separation, double approach_vel,
+                           double smbh_mass_frac, uint64_t seed);
+void csg_ref_merger_dust(Body *bodies, int start_idx, int n_dust, double separation,
+                         uint64_t seed);
 
 #endif

@@ -4,11 +4,12 @@
  *
  * A handle owns one device state (its own CUDA stream) and a host Body array
  * that cosmosim_get_bodies refreshes only when the device holds newer data.
- * Quasar mode keeps the reference's CPU quasar step (src/quasar.c): when the
- * application links it, the handle copies the bodies out, runs it after each
- * substep and copies them back (src/cosmosim_api.c:121-141). Initial
- * conditions come from the reference's generators when linked, else from this
- * library's seeded restatement of the same recipe.
+ * Quasar mode runs the quasar step (src/quasar.c:477-509) on the device after
+ * each substep and compacts dead bodies on the device every 60 steps
+ * (src/cosmosim_api.c:121-141): the bodies stay resident. Initial conditions
+ * and quasar defaults come from the reference's generators when the
+ * application links them, else from this library's seeded restatement of the
+ * same recipes.
  */
 #include "capi_internal.h"
 
@@ -27,8 +28,6 @@
 /* The reference's CPU-side translation units, when the application links
    them (they are not part of this library). */
 extern QuasarConfig quasar_default_config(void) __attribute__((weak));
-extern void quasar_step(Body *bodies, int *n, int n_alloc, QuasarConfig *cfg, double dt)
-    __attribute__((weak));
 extern void generate_spiral_galaxy(Body *bodies, int n, double cx, double cy, double galaxy_mass,
                                    double disk_radius, double vx_bulk, double vy_bulk)
     __attribute__((weak));
@@ -42,9 +41,6 @@ extern void generate_quasar_merger(Body *bodies, int n, double separation, doubl
 extern void generate_merger_dust(Body *bodies, int start_idx, int n_dust, double separation)
     __attribute__((weak));
 
-void csg_ref_spiral(Body *bodies, int n, double cx, double cy, double galaxy_mass,
-                    double disk_radius, double vx_bulk, double vy_bulk, uint64_t seed);
-void csg_ref_merger(Body *bodies, int n, double separation, double approach_vel, uint64_t seed);
 
 typedef struct {
     csgd_t *dev;
@@ -146,12 +142,6 @@ CSG_EXPORT SimHandle cosmosim_create_ex(CosmosimConfig config, double G, double 
     int n = config.n_bodies < 2 ? 2 : config.n_bodies; /* src/cosmosim_api.c:50-51 */
     int n_dust = (config.merger && config.quasar) ? n / 5 : 0;
     int n_alloc = config.quasar ? n + n_dust + n / 4 : n;
-    if (config.quasar &&
-        (!quasar_step || !quasar_default_config || !generate_quasar_galaxy ||
-         !generate_quasar_merger || !generate_merger_dust)) {
-        csg_thread_set_error(CSG_ERR_UNSUPPORTED); /* the CPU quasar step is not linked */
-        return NULL;
-    }
     SimState *s = (SimState *)calloc(1, sizeof(SimState));
     Body *bodies = (Body *)calloc((size_t)n_alloc, sizeof(Body));
     if (!s || !bodies) {
@@ -162,13 +152,26 @@ CSG_EXPORT SimHandle cosmosim_create_ex(CosmosimConfig config, double G, double 
     }
     if (config.quasar) { /* src/cosmosim_api.c:66-75 */
         if (config.merger) {
-            generate_quasar_merger(bodies, n, REF_SEPARATION, REF_APPROACH_VEL,
-                                   config.smbh_mass_frac);
-            if (n_dust > 0)
-                generate_merger_dust(bodies, n, n_dust, REF_SEPARATION);
+            if (generate_quasar_merger)
+                generate_quasar_merger(bodies, n, REF_SEPARATION, REF_APPROACH_VEL,
+                                       config.smbh_mass_frac);
+            else
+                csg_ref_quasar_merger(bodies, n, REF_SEPARATION, REF_APPROACH_VEL,
+                                      config.smbh_mass_frac, CSG_DEFAULT_SEED);
+            if (n_dust > 0) {
+                if (generate_merger_dust)
+                    generate_merger_dust(bodies, n, n_dust, REF_SEPARATION);
+                else
+                    csg_ref_merger_dust(bodies, n, n_dust, REF_SEPARATION,
+                                        CSG_DEFAULT_SEED + 99999ull);
+            }
         } else {
-            generate_quasar_galaxy(bodies, n, 0.0, 0.0, (double)n * 2.0, REF_DISK_RADIUS, 0.0,
-                                   0.0, config.smbh_mass_frac);
+            if (generate_quasar_galaxy)
+                generate_quasar_galaxy(bodies, n, 0.0, 0.0, (double)n * 2.0, REF_DISK_RADIUS,
+                                       0.0, 0.0, config.smbh_mass_frac);
+            else
+                csg_ref_quasar_galaxy(bodies, n, 0.0, 0.0, (double)n * 2.0, REF_DISK_RADIUS,
+                                      0.0, 0.0, config.smbh_mass_frac, CSG_DEFAULT_SEED);
         }
     } else if (config.merger) {
         if (generate_merger)
@@ -196,7 +199,7 @@ CSG_EXPORT SimHandle cosmosim_create_ex(CosmosimConfig config, double G, double 
     s->params.precision = precision;
     s->quasar = config.quasar ? 1 : 0;
     if (s->quasar) { /* src/cosmosim_api.c:87-94 */
-        s->qcfg = quasar_default_config();
+        s->qcfg = quasar_default_config ? quasar_default_config() : csg_quasar_default_config();
         s->qcfg.accretion_radius = config.accretion_radius;
         s->qcfg.jet_speed = config.jet_speed;
         s->qcfg.feedback_strength = config.feedback_strength;
@@ -339,16 +342,15 @@ CSG_EXPORT int cosmosim_autotune_walk(SimHandle handle, int reps, CsgWalkShape *
     return set_err(s, rc);
 }
 
-/* Runs the CPU quasar step between device substeps (src/cosmosim_api.c:130-132). */
+/* The quasar step between substeps (src/cosmosim_api.c:130-132), on the
+   device; it may append jets and lobes. */
 static int quasar_substep(SimState *s)
 {
-    int rc = csgd_download_bodies(s->dev, s->host, s->current_n);
+    int n = s->current_n;
+    int rc = csgd_quasar_step(s->dev, &s->qcfg, s->n_alloc, s->config.dt, &s->qcfg.jet_count, &n);
     if (!rc)
-        rc = csgd_sync(s->dev);
-    if (rc)
-        return rc;
-    quasar_step(s->host, &s->current_n, s->n_alloc, &s->qcfg, s->config.dt);
-    return csgd_upload_bodies(s->dev, s->host, s->current_n);
+        s->current_n = n;
+    return rc;
 }
 
 CSG_EXPORT int cosmosim_substeps_async(SimHandle handle, int k)

@@ -109,6 +109,160 @@ void csg_ref_merger(Body *bodies, int n, double separation, double approach_vel,
                    -approach_vel, -approach_vel * 0.3, seed + 12345);
 }
 
+/* The reference's quasar galaxy (src/initial_conditions.c:146-196): a spiral
+   whose central body becomes an SMBH of mass smbh_mass_frac x galaxy_mass,
+   spin (0, 0.7071, 0.7071), seeded accretion; the inner 20% of the disk
+   radius is gas with SPH fields. */
+void csg_ref_quasar_galaxy(Body *bodies, int n, double cx, double cy, double galaxy_mass,
+                           double disk_radius, double vx_bulk, double vy_bulk,
+                           double smbh_mass_frac, uint64_t seed)
+{
+    csg_ref_spiral(bodies, n, cx, cy, galaxy_mass, disk_radius, vx_bulk, vy_bulk, seed);
+    if (n < 1)
+        return;
+    bodies[0].mass = galaxy_mass * smbh_mass_frac;
+    bodies[0].type = BODY_SMBH;
+    bodies[0].spin_x = 0.0;
+    bodies[0].spin_y = 0.7071;
+    bodies[0].spin_z = 0.7071;
+    bodies[0].accretion_rate = galaxy_mass * 0.001;
+    bodies[0].luminosity = 0.1 * bodies[0].accretion_rate;
+    double inner_sq = (disk_radius * 0.2) * (disk_radius * 0.2);
+    double spacing = disk_radius / sqrt((double)n);
+    for (int i = 1; i < n; i++) {
+        double dx = bodies[i].x - cx, dy = bodies[i].y - cy;
+        if (dx * dx + dy * dy < inner_sq)
+            bodies[i].type = BODY_GAS;
+    }
+    for (int i = 1; i < n; i++) {
+        if (bodies[i].type != BODY_GAS)
+            continue;
+        double dx = bodies[i].x - cx, dy = bodies[i].y - cy;
+        double r = sqrt(dx * dx + dy * dy);
+        if (r < 1e-10)
+            r = 1e-10;
+        double m_enc = galaxy_mass * (1.0 - exp(-r / (disk_radius / 4.0)));
+        double vloc = sqrt(m_enc / r);
+        bodies[i].internal_energy = 0.5 * vloc * vloc / (CSG_SPH_GAMMA - 1.0);
+        bodies[i].smoothing_h = spacing * 2.0;
+    }
+}
+
+/* The reference's quasar merger (src/initial_conditions.c:268-348): two quasar
+   galaxies, masses 1 : 1.2, the second 30% larger and tilted 50 deg about x,
+   on a grazing orbit (tangential 0.2 v_circ, radial approach_vel). */
+void csg_ref_quasar_merger(Body *bodies, int n, double separation, double approach_vel,
+                           double smbh_mass_frac, uint64_t seed)
+{
+    int n1 = n / 2, n2 = n - n1;
+    double disk_radius = separation * 0.15;
+    double galaxy_mass = (double)n1 * 2.0;
+    double total_mass = galaxy_mass + galaxy_mass * 1.2;
+    double v_orbit = sqrt(total_mass / separation) * 0.2;
+    csg_ref_quasar_galaxy(bodies, n1, -separation * 0.5, 0.0, galaxy_mass, disk_radius,
+                          approach_vel, v_orbit, smbh_mass_frac, seed);
+    bodies[0].spin_x = 0.0;
+    bodies[0].spin_y = 0.7071;
+    bodies[0].spin_z = 0.7071;
+    csg_ref_quasar_galaxy(bodies + n1, n2, separation * 0.5, 0.0, galaxy_mass * 1.2,
+                          disk_radius * 1.3, -approach_vel, -v_orbit * 0.85, smbh_mass_frac,
+                          seed + 12345);
+    double t = 50.0 * CSG_PI / 180.0, ct = cos(t), st = sin(t);
+    for (int i = n1; i < n; i++) {
+        double y0 = bodies[i].y, z0 = bodies[i].z;
+        bodies[i].y = y0 * ct - z0 * st;
+        bodies[i].z = y0 * st + z0 * ct;
+        double vy0 = bodies[i].vy, vz0 = bodies[i].vz;
+        bodies[i].vy = vy0 * ct - vz0 * st;
+        bodies[i].vz = vy0 * st + vz0 * ct;
+    }
+    if (n2 > 0) {
+        double sy = 0.7071 * ct - 0.7071 * st, sz = 0.7071 * st + 0.7071 * ct;
+        double smag = sqrt(sy * sy + sz * sz);
+        bodies[n1].spin_x = 0.0;
+        bodies[n1].spin_y = sy / smag;
+        bodies[n1].spin_z = sz / smag;
+    }
+}
+
+/* The reference's merger dust (src/initial_conditions.c:198-266): a tidal
+   bridge between the two centres and an outer halo around each disk. */
+void csg_ref_merger_dust(Body *bodies, int start_idx, int n_dust, double separation,
+                         uint64_t seed)
+{
+    Rng r;
+    rng_seed(&r, seed);
+    double disk_radius = separation * 0.15;
+    double gm1 = (double)(start_idx / 2) * 2.0, gm2 = gm1 * 1.2;
+    double disk_r2 = disk_radius * 1.3;
+    double cx1 = -separation * 0.5, cx2 = separation * 0.5;
+    int n_tidal = n_dust / 3;
+    int n_halo1 = (n_dust - n_tidal) / 2;
+    int n_halo2 = n_dust - n_tidal - n_halo1;
+    for (int i = 0; i < n_tidal; i++) {
+        Body *b = &bodies[start_idx + i];
+        clear_body(b);
+        double t = rng_uniform(&r);
+        double bx = cx1 + t * (cx2 - cx1);
+        double by = rng_normal(&r) * separation * 0.06;
+        b->x = bx + rng_normal(&r) * separation * 0.04;
+        b->y = by;
+        b->z = rng_normal(&r) * separation * 0.015;
+        b->mass = 0.4 + rng_uniform(&r) * 0.6;
+        b->type = BODY_DUST;
+        double rr = sqrt(bx * bx + by * by);
+        if (rr < 1e-10)
+            rr = 1e-10;
+        double v_c = sqrt(gm1 / rr) * 0.25;
+        b->vx = -v_c * by / rr + rng_normal(&r) * 0.4;
+        b->vy = v_c * bx / rr + rng_normal(&r) * 0.4;
+        b->vz = rng_normal(&r) * 0.2;
+    }
+    for (int half = 0; half < 2; half++) {
+        int cnt = half ? n_halo2 : n_halo1;
+        int off = start_idx + n_tidal + (half ? n_halo1 : 0);
+        double rad0 = half ? disk_r2 : disk_radius, cx = half ? cx2 : cx1;
+        double gm = half ? gm2 : gm1;
+        for (int i = 0; i < cnt; i++) {
+            Body *b = &bodies[off + i];
+            clear_body(b);
+            double rr = rad0 * (0.7 + 0.9 * sqrt(rng_uniform(&r)));
+            double th = 2.0 * CSG_PI * rng_uniform(&r);
+            b->x = cx + rr * cos(th);
+            b->y = rr * sin(th);
+            b->z = rng_normal(&r) * rad0 * 0.08;
+            b->mass = 0.4 + rng_uniform(&r) * 0.6;
+            b->type = BODY_DUST;
+            double v_c = sqrt(gm / rr) * 0.75;
+            double disp = v_c * 0.08;
+            b->vx = -v_c * sin(th) + rng_normal(&r) * disp;
+            b->vy = v_c * cos(th) + rng_normal(&r) * disp;
+            b->vz = rng_normal(&r) * disp * 0.3;
+        }
+    }
+}
+
+/* The reference's quasar defaults (src/quasar.c:37-57). */
+CSG_EXPORT QuasarConfig csg_quasar_default_config(void)
+{
+    QuasarConfig c;
+    memset(&c, 0, sizeof(c));
+    c.accretion_radius = 3.0;
+    c.swallow_radius = 0.3;
+    c.isco_radius = 0.5;
+    c.viscosity_alpha = 0.05;
+    c.jet_speed = 20.0;
+    c.jet_mass = 0.5;
+    c.jet_lifetime = 5.0;
+    c.feedback_strength = 1.0;
+    c.eta_eff = 0.1;
+    c.eddington_k = 0.5;
+    c.accretion_smoothing = 0.95;
+    c.jet_cap = 2000;
+    c.jet_ring_count = 4;
+    return c;
+}
+
 /* ---- benchmark configurations --------------------------------------------- */
 
 typedef struct {

@@ -10,7 +10,7 @@ import os
 
 import numpy as np
 
-from .abi import BODY_DTYPE, NODE_DTYPE, CosmosimConfig, ptr
+from .abi import BODY_DTYPE, NODE_DTYPE, CosmosimConfig, QuasarConfig, ptr
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libcosmosim_gb300.so")
@@ -72,6 +72,9 @@ _SIGS = {
     "cosmosim_set_bodies": ([_vp, _vp, _i], _i),
     "cosmosim_snapshot_f32": ([_vp, _i, _vp, _i, _i], _i),
     "cosmosim_compact": ([_vp], _i),
+    "csg_quasar_step": ([_vp, _ip, _i, _vp, _d], None),
+    "csg_quasar_seed": ([ctypes.c_uint64, _i], None),
+    "csg_quasar_default_config": ([], QuasarConfig),
     "cosmosim_build_tree_async": ([_vp], _i),
     "cosmosim_gravity_async": ([_vp], _i),
     "cosmosim_enable_stats": ([_vp, _i], _i),
@@ -203,6 +206,22 @@ def sph_apply_cooling(bodies, dt):
     lib = load()
     lib.sph_apply_cooling(ptr(bodies), len(bodies), dt)
     _check(lib, "sph_apply_cooling")
+
+
+def quasar_step(bodies, n, cfg, dt):
+    """The GPU quasar step (csg_quasar_step) on bodies[:n] with room for
+    len(bodies); returns the new count (cfg.jet_count is updated in place)."""
+    lib = load()
+    nn = ctypes.c_int(n)
+    lib.csg_quasar_step(ptr(bodies), ctypes.byref(nn), len(bodies), ctypes.byref(cfg), dt)
+    _check(lib, "csg_quasar_step")
+    return nn.value
+
+
+def quasar_seed(rng_state=1, knot_phase=0):
+    lib = load()
+    lib.csg_quasar_seed(rng_state, knot_phase)
+    _check(lib, "csg_quasar_seed")
 
 
 def measure_fp_peaks():

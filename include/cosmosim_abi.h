@@ -169,6 +169,7 @@ CSG_EXPORT void cosmosim_destroy(SimHandle handle);
 static_assert(sizeof(Body) == 168, "Body must be 168 bytes");
 static_assert(sizeof(OctreeNode) == 104, "OctreeNode must be 104 bytes");
 static_assert(sizeof(CosmosimConfig) == 72, "CosmosimConfig must be 72 bytes");
+static_assert(sizeof(QuasarConfig) == 104, "QuasarConfig must be 104 bytes");
 #else
 _Static_assert(sizeof(Body) == 168, "Body must be 168 bytes");
 _Static_assert(sizeof(OctreeNode) == 104, "OctreeNode must be 104 bytes");

@@ -252,6 +252,22 @@ CSG_EXPORT int csg_adjoint_forward_frozen(csg_adjoint *adj, const Body *bodies,
 CSG_EXPORT int csg_adjoint_stats(csg_adjoint *adj, int64_t *device_bytes, int64_t *interactions,
                                  int64_t *launches);
 
+/* ---- Quasar step on the GPU ---------------------------------------------------
+   csg_quasar_step has the signature and semantics of the reference's
+   quasar_step (src/quasar.h:29-34, src/quasar.c:477-509): accretion onto
+   SMBHs, accretion rate / luminosity, radiation feedback, jet decay into
+   lobes, recycling of distant jets, jet spawning; bodies may be appended up to
+   n_alloc, *n and cfg->jet_count are updated. It runs on the calling thread's
+   GPU state. The random generator state and the jet knot phase persist
+   between calls as the reference's file statics do (src/quasar.c:11, :224);
+   csg_quasar_seed sets them (the reference starts at 1 and 0). Handles in
+   quasar mode run the same step on their resident bodies after every
+   substep. */
+CSG_EXPORT void csg_quasar_step(Body *bodies, int *n, int n_alloc, QuasarConfig *cfg, double dt);
+CSG_EXPORT void csg_quasar_seed(uint64_t rng_state, int knot_phase);
+/* The reference's defaults (src/quasar.c:37-57). */
+CSG_EXPORT QuasarConfig csg_quasar_default_config(void);
+
 /* Free-function parity mode: gravity with the reference's exact operation
    sequence (no fused multiply-add, 1/(r2*sqrt(r2))). Same signature as
    octree_compute_forces. */

@@ -12,6 +12,7 @@
 #include <float.h>
 #include <math.h>
 #include <stddef.h>
+#include <string.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -532,4 +533,342 @@ double orc_total_energy(const Body *bodies, int n, double G, double softening)
         }
     }
     return ke + pe;
+}
+
+/* ---- quasar step (reference src/quasar.c) ----------------------------------- */
+
+static uint64_t q_state = 1;  /* src/quasar.c:11 */
+static int q_knot_phase = 0; /* src/quasar.c:224 */
+
+void orc_quasar_seed(uint64_t rng_state, int knot_phase)
+{
+    q_state = rng_state ? rng_state : 1;
+    q_knot_phase = knot_phase;
+}
+
+static double q_uni(void) /* src/quasar.c:13-27: xorshift64 13/7/17, 53-bit uniform */
+{
+    uint64_t x = q_state;
+    x ^= x << 13;
+    x ^= x >> 7;
+    x ^= x << 17;
+    q_state = x;
+    return (double)(x >> 11) * (1.0 / 9007199254740992.0);
+}
+
+static double q_gauss(void) /* src/quasar.c:29-35: Box-Muller, first output */
+{
+    double u1 = q_uni(), u2 = q_uni();
+    if (u1 < 1e-15)
+        u1 = 1e-15;
+    return sqrt(-2.0 * log(u1)) * cos(2.0 * ORC_PI * u2);
+}
+
+static void q_kill(Body *b)
+{
+    b->mass = 0.0;
+    b->vx = b->vy = b->vz = 0.0;
+    b->ax = b->ay = b->az = 0.0;
+}
+
+/* src/quasar.c:63-101: momentum-conserving merge, spin nudged by the
+   victim's specific angular momentum direction. */
+static void q_swallow(Body *s, Body *v)
+{
+    double mt = s->mass + v->mass;
+    s->vx = (s->mass * s->vx + v->mass * v->vx) / mt;
+    s->vy = (s->mass * s->vy + v->mass * v->vy) / mt;
+    s->vz = (s->mass * s->vz + v->mass * v->vz) / mt;
+    double rx = v->x - s->x, ry = v->y - s->y, rz = v->z - s->z;
+    double ux = v->vx - s->vx, uy = v->vy - s->vy, uz = v->vz - s->vz;
+    double lx = ry * uz - rz * uy, ly = rz * ux - rx * uz, lz = rx * uy - ry * ux;
+    double lm = sqrt(lx * lx + ly * ly + lz * lz);
+    if (lm > 1e-15) {
+        double w = v->mass / mt * 0.01;
+        s->spin_x += w * lx / lm;
+        s->spin_y += w * ly / lm;
+        s->spin_z += w * lz / lm;
+        double sm = sqrt(s->spin_x * s->spin_x + s->spin_y * s->spin_y + s->spin_z * s->spin_z);
+        if (sm > 1e-15) {
+            s->spin_x /= sm;
+            s->spin_y /= sm;
+            s->spin_z /= sm;
+        }
+    }
+    s->mass = mt;
+    q_kill(v);
+}
+
+/* src/quasar.c:103-123: drag on the radial velocity component */
+static void q_drag(const Body *s, Body *g, double alpha)
+{
+    double rx = g->x - s->x, ry = g->y - s->y, rz = g->z - s->z;
+    double r = sqrt(rx * rx + ry * ry + rz * rz);
+    if (r < 1e-15)
+        return;
+    double ux = g->vx - s->vx, uy = g->vy - s->vy, uz = g->vz - s->vz;
+    double vr = (ux * rx + uy * ry + uz * rz) / r;
+    g->ax -= alpha * (vr * rx / r);
+    g->ay -= alpha * (vr * ry / r);
+    g->az -= alpha * (vr * rz / r);
+}
+
+/* src/quasar.c:125-190 */
+static double q_accrete(Body *b, int n, const QuasarConfig *c)
+{
+    double swallowed = 0.0;
+    double ra2 = c->accretion_radius * c->accretion_radius;
+    double rs2 = c->swallow_radius * c->swallow_radius;
+    for (int s = 0; s < n; s++) {
+        if (b[s].type != BODY_SMBH || b[s].mass <= 0.0)
+            continue;
+        Body *S = &b[s];
+        for (int i = 0; i < n; i++) {
+            if (i == s || b[i].mass <= 0.0 || b[i].type == BODY_SMBH)
+                continue;
+            double dx = b[i].x - S->x, dy = b[i].y - S->y, dz = b[i].z - S->z;
+            double d2 = dx * dx + dy * dy + dz * dz;
+            if (d2 > ra2)
+                continue;
+            if (d2 < rs2) {
+                swallowed += b[i].mass;
+                q_swallow(S, &b[i]);
+                continue;
+            }
+            double r = sqrt(d2);
+            double ux = b[i].vx - S->vx, uy = b[i].vy - S->vy, uz = b[i].vz - S->vz;
+            double lx = dy * uz - dz * uy, ly = dz * ux - dx * uz, lz = dx * uy - dy * ux;
+            double rc = (lx * lx + ly * ly + lz * lz) / (S->mass * r);
+            if (rc > c->isco_radius && b[i].type != BODY_GAS) {
+                b[i].type = BODY_GAS;
+                if (b[i].smoothing_h < 1e-10)
+                    b[i].smoothing_h = c->accretion_radius * 0.3;
+                if (b[i].internal_energy < 1e-10) {
+                    double v2 = b[i].vx * b[i].vx + b[i].vy * b[i].vy + b[i].vz * b[i].vz;
+                    b[i].internal_energy = 0.001 * v2 + 0.01;
+                }
+            }
+            if (b[i].type == BODY_GAS) {
+                q_drag(S, &b[i], c->viscosity_alpha);
+                if (r < c->isco_radius) {
+                    swallowed += b[i].mass;
+                    q_swallow(S, &b[i]);
+                }
+            }
+        }
+    }
+    return swallowed;
+}
+
+/* src/quasar.c:192-220 */
+static void q_feedback(Body *b, int n, const QuasarConfig *c)
+{
+    double rf2 = (c->accretion_radius * 3.0) * (c->accretion_radius * 3.0);
+    for (int s = 0; s < n; s++) {
+        if (b[s].type != BODY_SMBH || b[s].luminosity <= 0.0)
+            continue;
+        for (int i = 0; i < n; i++) {
+            if (i == s || b[i].mass <= 0.0 || b[i].type == BODY_SMBH)
+                continue;
+            double dx = b[i].x - b[s].x, dy = b[i].y - b[s].y, dz = b[i].z - b[s].z;
+            double d2 = dx * dx + dy * dy + dz * dz;
+            if (d2 > rf2 || d2 < 1e-10)
+                continue;
+            double r = sqrt(d2);
+            double f = c->feedback_strength * b[s].luminosity / (4.0 * ORC_PI * d2);
+            b[i].ax += f * dx / r;
+            b[i].ay += f * dy / r;
+            b[i].az += f * dz / r;
+        }
+    }
+}
+
+/* src/quasar.c:222-373: knots (speed/cone modulation), helical offset, rings */
+static void q_spawn(Body *b, int *n, int n_alloc, QuasarConfig *c)
+{
+    q_knot_phase++;
+    double ph1 = q_knot_phase * 0.10, ph2 = q_knot_phase * 0.057;
+    double speed_mod = 1.0 + 0.6 * sin(ph1);
+    if (speed_mod < 0.5)
+        speed_mod = 0.5;
+    double cone = 0.05 + 0.13 * (0.5 + 0.5 * sin(ph2));
+    double helix = q_knot_phase * 0.04;
+    for (int s = 0; s < *n; s++) {
+        if (b[s].type != BODY_SMBH || b[s].luminosity <= 0.0)
+            continue;
+        const Body *S = &b[s];
+        double e_jet = 0.5 * c->jet_mass * c->jet_speed * c->jet_speed;
+        if (e_jet < 1e-15)
+            continue;
+        int ns = (int)(S->luminosity / e_jet);
+        ns = ns < 2 ? 2 : (ns > 8 ? 8 : ns);
+        double px, py, pz;
+        if (fabs(S->spin_z) < 0.9) {
+            px = -S->spin_y;
+            py = S->spin_x;
+            pz = 0.0;
+        } else {
+            px = 0.0;
+            py = -S->spin_z;
+            pz = S->spin_y;
+        }
+        double pm = sqrt(px * px + py * py + pz * pz);
+        if (pm > 1e-15) {
+            px /= pm;
+            py /= pm;
+            pz /= pm;
+        }
+        double qx = S->spin_y * pz - S->spin_z * py;
+        double qy = S->spin_z * px - S->spin_x * pz;
+        double qz = S->spin_x * py - S->spin_y * px;
+        double qm = sqrt(qx * qx + qy * qy + qz * qz);
+        if (qm > 1e-15) {
+            qx /= qm;
+            qy /= qm;
+            qz /= qm;
+        }
+        double amp = c->swallow_radius * 0.35;
+        double hx = amp * (cos(helix) * px + sin(helix) * qx);
+        double hy = amp * (cos(helix) * py + sin(helix) * qy);
+        double hz = amp * (cos(helix) * pz + sin(helix) * qz);
+        double speed = c->jet_speed * speed_mod;
+        int total = ns + ((speed_mod > 1.35) ? 4 : 0);
+        for (int j = 0; j < total && c->jet_count < c->jet_cap; j++) {
+            if (*n >= n_alloc)
+                break;
+            int burst = j >= ns;
+            double sign = (j % 2 == 0) ? 1.0 : -1.0;
+            double jcone = burst ? 0.012 : cone;
+            double jspeed = burst ? speed * 1.28 : speed;
+            double jmass = burst ? c->jet_mass * 1.9 : c->jet_mass;
+            double jlife = burst ? c->jet_lifetime * 1.4 : c->jet_lifetime;
+            double fwd = burst ? c->swallow_radius * 0.6 : 0.0;
+            double angle = q_uni() * 2.0 * ORC_PI;
+            double offset = q_gauss() * jcone;
+            int ring = burst ? 1 : c->jet_ring_count;
+            for (int r = 0; r < ring; r++) {
+                if (*n >= n_alloc || c->jet_count >= c->jet_cap)
+                    break;
+                Body *J = &b[*n];
+                memset(J, 0, sizeof(Body));
+                J->type = BODY_JET;
+                J->lifetime = jlife;
+                double ra = (ring > 1) ? 2.0 * ORC_PI * r / ring + angle : angle;
+                double rr = (ring > 1) ? c->swallow_radius * 0.15 : 0.0;
+                double rx = rr * (cos(ra) * px + sin(ra) * qx);
+                double ry = rr * (cos(ra) * py + sin(ra) * qy);
+                double rz = rr * (cos(ra) * pz + sin(ra) * qz);
+                J->mass = (ring > 1) ? jmass * 0.6 : jmass;
+                J->x = S->x + sign * S->spin_x * (c->swallow_radius + fwd) +
+                       offset * (px * cos(angle)) + sign * hx + rx;
+                J->y = S->y + sign * S->spin_y * (c->swallow_radius + fwd) +
+                       offset * (py * cos(angle)) + sign * hy + ry;
+                J->z = S->z + sign * S->spin_z * (c->swallow_radius + fwd) +
+                       offset * (pz * sin(angle)) + sign * hz + rz;
+                double ev = jspeed * 0.04 * (1.0 + J->lifetime * 0.1);
+                J->vx = S->vx + sign * S->spin_x * jspeed + rx * ev / (rr + 1e-15);
+                J->vy = S->vy + sign * S->spin_y * jspeed + ry * ev / (rr + 1e-15);
+                J->vz = S->vz + sign * S->spin_z * jspeed + rz * ev / (rr + 1e-15);
+                (*n)++;
+                c->jet_count++;
+            }
+        }
+    }
+}
+
+/* src/quasar.c:375-420: jets count down and leave a lobe; lobes count down */
+static void q_decay(Body *b, int *n, int n_alloc, QuasarConfig *c, double dt)
+{
+    int n0 = *n;
+    for (int i = 0; i < n0; i++) {
+        if (b[i].type != BODY_JET || b[i].mass <= 0.0)
+            continue;
+        b[i].lifetime -= dt;
+        if (b[i].lifetime > 0.0)
+            continue;
+        if (*n < n_alloc && b[i].mass > 0.2) {
+            Body *L = &b[*n];
+            memset(L, 0, sizeof(Body));
+            L->type = BODY_LOBE;
+            L->mass = b[i].mass * 0.5;
+            L->x = b[i].x;
+            L->y = b[i].y;
+            L->z = b[i].z;
+            L->vx = b[i].vx * 0.15 + (q_uni() - 0.5) * 0.5;
+            L->vy = b[i].vy * 0.15 + (q_uni() - 0.5) * 0.5;
+            L->vz = b[i].vz * 0.15 + (q_uni() - 0.5) * 0.5;
+            L->lifetime = c->jet_lifetime * 3.0;
+            (*n)++;
+        }
+        q_kill(&b[i]);
+        c->jet_count--;
+    }
+    for (int i = 0; i < *n; i++) {
+        if (b[i].type != BODY_LOBE || b[i].mass <= 0.0)
+            continue;
+        b[i].lifetime -= dt;
+        if (b[i].lifetime <= 0.0)
+            q_kill(&b[i]);
+    }
+}
+
+/* src/quasar.c:422-475: jets beyond 10 accretion radii of the first SMBH
+   return as infalling gas on the accretion sphere */
+static void q_recycle(Body *b, int n, QuasarConfig *c)
+{
+    int s = -1;
+    for (int i = 0; i < n && s < 0; i++)
+        if (b[i].type == BODY_SMBH && b[i].mass > 0.0)
+            s = i;
+    if (s < 0)
+        return;
+    const Body *S = &b[s];
+    double R = c->accretion_radius * 10.0;
+    for (int i = 0; i < n; i++) {
+        if (b[i].type != BODY_JET || b[i].mass <= 0.0)
+            continue;
+        double dx = b[i].x - S->x, dy = b[i].y - S->y, dz = b[i].z - S->z;
+        if (dx * dx + dy * dy + dz * dz < R * R)
+            continue;
+        double angle = 2.0 * ORC_PI * q_uni();
+        double cp = 2.0 * q_uni() - 1.0;
+        double sp = sqrt(1.0 - cp * cp);
+        double rp = c->accretion_radius;
+        b[i].x = S->x + rp * sp * cos(angle);
+        b[i].y = S->y + rp * sp * sin(angle);
+        b[i].z = S->z + rp * cp;
+        double vin = 0.5 * sqrt(S->mass / rp);
+        double nx = (b[i].x - S->x) / rp, ny = (b[i].y - S->y) / rp, nz = (b[i].z - S->z) / rp;
+        b[i].vx = S->vx - vin * nx;
+        b[i].vy = S->vy - vin * ny;
+        b[i].vz = S->vz - vin * nz;
+        b[i].ax = b[i].ay = b[i].az = 0.0;
+        b[i].type = BODY_GAS;
+        b[i].lifetime = 0.0;
+        b[i].smoothing_h = c->accretion_radius * 0.3;
+        double v2 = b[i].vx * b[i].vx + b[i].vy * b[i].vy + b[i].vz * b[i].vz;
+        b[i].internal_energy = 0.001 * v2 + 0.01;
+        b[i].density = 0.0;
+        b[i].pressure = 0.0;
+        c->jet_count--;
+    }
+}
+
+void orc_quasar_step(Body *bodies, int *n, int n_alloc, QuasarConfig *cfg, double dt)
+{
+    double swallowed = q_accrete(bodies, *n, cfg);
+    for (int i = 0; i < *n; i++) { /* src/quasar.c:482-494 */
+        if (bodies[i].type != BODY_SMBH)
+            continue;
+        Body *S = &bodies[i];
+        S->accretion_rate = cfg->accretion_smoothing * S->accretion_rate +
+                            (1.0 - cfg->accretion_smoothing) * (swallowed / dt);
+        S->luminosity = cfg->eta_eff * S->accretion_rate;
+        if (S->luminosity > cfg->eddington_k * S->mass)
+            S->luminosity = cfg->eddington_k * S->mass;
+    }
+    q_feedback(bodies, *n, cfg);
+    q_decay(bodies, n, n_alloc, cfg, dt);
+    q_recycle(bodies, *n, cfg);
+    q_spawn(bodies, n, n_alloc, cfg);
 }

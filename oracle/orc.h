@@ -59,6 +59,12 @@ double orc_total_energy(const Body *bodies, int n, double G, double softening);
 /* Threads the OpenMP loops use (0 = runtime default). Returns the count in use. */
 int orc_set_threads(int nthreads);
 
+/* Quasar step, reference src/quasar.c:477-509 (single-threaded, as the
+   reference). The generator state and knot phase persist between calls
+   (src/quasar.c:11, :224); orc_quasar_seed sets them. */
+void orc_quasar_step(Body *bodies, int *n, int n_alloc, QuasarConfig *cfg, double dt);
+void orc_quasar_seed(uint64_t rng_state, int knot_phase);
+
 #ifdef __cplusplus
 }
 #endif

@@ -55,6 +55,9 @@ def _bind(lib, prefix):
     f = getattr(lib, prefix + "integrator_init_accelerations")
     f.argtypes = [_vp, _i, _d, _d, _d, _vp]
     f.restype = None
+    f = getattr(lib, prefix + "quasar_step")
+    f.argtypes = [_vp, _c_int_p, _i, _vp, _d]
+    f.restype = None
 
 
 class CpuPhysics:
@@ -101,6 +104,13 @@ class CpuPhysics:
         self._f("integrator_init_accelerations")(ptr(bodies), len(bodies), G, eps, theta,
                                                  ptr(pool))
 
+    def quasar_step(self, bodies, n, cfg, dt):
+        """Quasar step on bodies[:n] with room for len(bodies); returns the new
+        count (cfg, a QuasarConfig, is updated in place)."""
+        nn = ctypes.c_int(n)
+        self._f("quasar_step")(ptr(bodies), ctypes.byref(nn), len(bodies), ctypes.byref(cfg), dt)
+        return nn.value
+
 
 class Oracle(CpuPhysics):
     """The C restatement (orc.c) plus its check helpers."""
@@ -118,6 +128,11 @@ class Oracle(CpuPhysics):
         lib.orc_total_energy.restype = _d
         lib.orc_set_threads.argtypes = [_i]
         lib.orc_set_threads.restype = _i
+        lib.orc_quasar_seed.argtypes = [ctypes.c_uint64, _i]
+        lib.orc_quasar_seed.restype = None
+
+    def quasar_seed(self, rng_state=1, knot_phase=0):
+        self.lib.orc_quasar_seed(rng_state, knot_phase)
 
     def set_threads(self, n):
         return self.lib.orc_set_threads(n)

@@ -168,5 +168,101 @@ def main():
             print(f, os.path.getsize(os.path.join(HERE, f)))
 
 
+QUASAR_FIELDS = ["x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "mass", "type", "spin_x",
+                 "spin_y", "spin_z", "accretion_rate", "luminosity", "lifetime", "density",
+                 "pressure", "internal_energy", "smoothing_h"]
+
+
+def quasar_bodies(rng, n=3000, extra=600):
+    """Two SMBHs with stars and gas around them (some inside the swallow and
+    ISCO radii), jets about to expire or far enough to be recycled, lobes,
+    dust and dead bodies; room for `extra` appended bodies."""
+    from cosmosim_gb300.abi import BODY_DUST, BODY_JET, BODY_LOBE, BODY_SMBH
+
+    b = np.zeros(n + extra, dtype=BODY_DTYPE)
+    c = np.array([[0.0, 0.0, 0.0], [12.0, 0.0, 0.0]])
+    b["type"][:2] = BODY_SMBH
+    b["mass"][:2] = [5.0, 3.0]
+    b["x"][:2], b["y"][:2], b["z"][:2] = c[:, 0], c[:, 1], c[:, 2]
+    b["vx"][:2] = [0.05, -0.08]
+    b["spin_x"][:2], b["spin_y"][:2], b["spin_z"][:2] = [0.0, 0.1], [0.7071, 0.1], [0.7071, 0.99]
+    b["accretion_rate"][:2] = [2.0, 0.5]
+    b["luminosity"][:2] = [5.0, 1.0]
+    m = n - 2 - 40 - 10 - 20
+    host = rng.integers(0, 2, m)
+    r = rng.exponential(1.6, m)
+    th = rng.uniform(0, 2 * np.pi, m)
+    k = slice(2, 2 + m)
+    b["x"][k] = c[host, 0] + r * np.cos(th)
+    b["y"][k] = c[host, 1] + r * np.sin(th)
+    b["z"][k] = rng.normal(0, 0.2, m)
+    vc = np.sqrt(np.where(host == 0, 5.0, 3.0) / np.maximum(r, 0.05)) * rng.uniform(0.2, 1.2, m)
+    b["vx"][k] = -vc * np.sin(th) + rng.normal(0, 0.1, m)
+    b["vy"][k] = vc * np.cos(th) + rng.normal(0, 0.1, m)
+    b["vz"][k] = rng.normal(0, 0.05, m)
+    b["mass"][k] = rng.uniform(0.001, 0.01, m)
+    gas = rng.random(m) < 0.3
+    b["type"][k] = np.where(gas, BODY_GAS, 0)
+    b["internal_energy"][k] = np.where(gas & (rng.random(m) < 0.8), rng.uniform(0.1, 1.0, m), 0.0)
+    b["smoothing_h"][k] = np.where(gas & (rng.random(m) < 0.8), 0.2, 0.0)
+    b["mass"][k][rng.random(m) < 0.02] = 0.0
+    j = slice(2 + m, 2 + m + 40)
+    b["type"][j] = BODY_JET
+    b["mass"][j] = rng.choice([0.5, 0.3, 0.15], 40)
+    b["lifetime"][j] = rng.uniform(-0.01, 0.1, 40)
+    far = rng.random(40) < 0.3
+    rj = np.where(far, rng.uniform(31.0, 40.0, 40), rng.uniform(0.5, 20.0, 40))
+    pj = rng.normal(0, 1, (40, 3))
+    pj /= np.linalg.norm(pj, axis=1)[:, None]
+    b["x"][j], b["y"][j], b["z"][j] = (rj[:, None] * pj).T
+    b["vx"][j], b["vy"][j], b["vz"][j] = rng.normal(0, 5.0, (3, 40))
+    lo = slice(2 + m + 40, 2 + m + 50)
+    b["type"][lo] = BODY_LOBE
+    b["mass"][lo] = 0.25
+    b["lifetime"][lo] = rng.uniform(-0.01, 0.08, 10)
+    b["x"][lo] = rng.uniform(-20, 20, 10)
+    du = slice(2 + m + 50, n)
+    b["type"][du] = BODY_DUST
+    b["mass"][du] = rng.uniform(0.4, 1.0, n - (2 + m + 50))
+    b["x"][du] = rng.uniform(-5, 15, n - (2 + m + 50))
+    b["y"][du] = rng.uniform(-3, 3, n - (2 + m + 50))
+    return b, n
+
+
+def quasar_golden():
+    """Runs in a fresh process: the reference's quasar_step keeps its random
+    generator and knot phase in file statics that start at 1 and 0."""
+    import ctypes
+
+    from cosmosim_gb300.abi import QuasarConfig
+
+    orc.build()
+    ref = orc.reference()
+    ref.lib.quasar_default_config.restype = QuasarConfig
+    rng = np.random.default_rng(21)
+    b0, n0 = quasar_bodies(rng)
+    cfg = ref.lib.quasar_default_config()
+    cfg.jet_count = 40
+    cfg.max_bodies = len(b0)
+    s, n = b0.copy(), n0
+    steps, counts = [], []
+    for _ in range(6):
+        n = ref.quasar_step(s, n, cfg, 0.02)
+        steps.append(fields(s, QUASAR_FIELDS))
+        counts.append((n, cfg.jet_count))
+    keep = [0, 5]  # states after steps 1 and 6 (bodies in use at the end)
+    save("quasar_3000.npz", bodies=b0, n0=n0, dt=0.02,
+         steps=np.array([steps[k][:n] for k in keep]), step_numbers=np.array(keep) + 1,
+         counts=np.array(counts), out_fields=np.array(QUASAR_FIELDS),
+         cfg=np.frombuffer(bytes(ref.lib.quasar_default_config()), dtype=np.uint8))
+    del ctypes
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["--quasar"]:
+        quasar_golden()
+    else:
+        main()
+        import subprocess
+
+        subprocess.run([sys.executable, __file__, "--quasar"], check=True)

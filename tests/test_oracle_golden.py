@@ -97,3 +97,29 @@ def test_interaction_count_matches_walk(orc):
     # theta = 0 opens every cell: each alive body meets every other alive leaf
     assert np.all(per[alive] == alive.sum() - 1)
     assert total == per.sum()
+
+
+def quasar_cfg(g):
+    from cosmosim_gb300.abi import QuasarConfig
+
+    cfg = QuasarConfig.from_buffer_copy(g["cfg"].tobytes())
+    cfg.jet_count = 40
+    cfg.max_bodies = len(g["bodies"])
+    return cfg
+
+
+def test_quasar_step(orc):
+    """Six quasar steps (accretion, feedback, jet decay into lobes, recycling,
+    spawning with the reference's random stream) equal the reference's."""
+    g = golden("quasar_3000.npz")
+    names = [str(x) for x in g["out_fields"]]
+    b = g["bodies"].copy()
+    cfg = quasar_cfg(g)
+    orc.quasar_seed(1, 0)
+    n = int(g["n0"])
+    want = dict(zip(g["step_numbers"].tolist(), g["steps"]))
+    for step in range(1, 7):
+        n = orc.quasar_step(b, n, cfg, float(g["dt"]))
+        assert (n, cfg.jet_count) == tuple(g["counts"][step - 1])
+        if step in want:
+            np.testing.assert_array_equal(fields(b[:n], names), want[step][:n])
