@@ -161,6 +161,7 @@ struct csgd {
     int *nb;           // SPH neighbour lists, 128 slots x cap (slot-major)
     int *nb_count;
     double *pr2, *cs; // SPH per-body force terms
+    double *sph_term; // SPH pair terms, 3 x 128 x cap (slot-major)
     int nb_cap;
 
     // nodes

@@ -66,6 +66,7 @@ struct SphArgs {
     int *nb;       // neighbour lists, slot-major
     int *nb_count; // neighbours per gas body
     double *pr2, *cs; // per-body force terms (k_sph_body_terms)
+    double *term;     // pair terms, 3 planes of 128 slots x stride (slot-major)
     int n, node_cap, stride;
 };
 
@@ -215,29 +216,54 @@ __global__ void __launch_bounds__(SPH_THREADS) k_sph_lists(SphArgs a)
         list_one(a, k, lane);
 }
 
-// Density, adaptive h and pressure over the recorded list, src/sph.c:45-97.
-// Lanes walk their own lists in lockstep: no work is repeated for lanes that
-// found no neighbour at a given step.
-__global__ void __launch_bounds__(SPH_THREADS) k_sph_density_pairs(SphArgs a)
+// Pair kernels. Each pass runs in two kernels so that the FP64 pair
+// arithmetic (sqrt, divisions) keeps every SM busy even when gas bodies are
+// few: one thread per (list slot, gas body) writes the pair's term, then one
+// thread per gas body adds its terms in list order — the reference's order,
+// with the same operations, so the sums are the reference's bit for bit
+// (a skipped pair stores 0, and x - 0 == x for every x).
+__device__ __forceinline__ bool pair_slot(const SphArgs &a, long long t, int n_gas, int &s,
+                                          int &k)
+{
+    s = (int)(t / n_gas);
+    k = (int)(t - (long long)s * n_gas);
+    return s < a.nb_count[k];
+}
+
+// Density terms m_j W(r, h_i), src/sph.c:53-63.
+__global__ void __launch_bounds__(SPH_THREADS) k_sph_density_terms(SphArgs a)
+{
+    const int n_gas = a.sc->n_gas;
+    const long long total = (long long)CSG_SPH_MAX_NEIGHBORS * n_gas;
+    const size_t stride = (size_t)a.stride;
+    for (long long t = (long long)blockIdx.x * SPH_THREADS + threadIdx.x; t < total;
+         t += (long long)gridDim.x * SPH_THREADS) {
+        int s, k;
+        if (!pair_slot(a, t, n_gas, s, k))
+            continue;
+        const int i = a.gas[k];
+        const int j = a.nb[stride * s + k];
+        double dx = a.x[i] - a.x[j];
+        double dy = a.y[i] - a.y[j];
+        double dz = a.z[i] - a.z[j];
+        double r = sqrt(dx * dx + dy * dy + dz * dz);
+        a.term[stride * s + k] = a.m[j] * kernel_W(r, a.h[i]);
+    }
+}
+
+// Density, adaptive h and pressure, src/sph.c:45-97.
+__global__ void __launch_bounds__(SPH_THREADS) k_sph_density_sums(SphArgs a)
 {
     const int k = blockIdx.x * SPH_THREADS + threadIdx.x;
     if (k >= a.sc->n_gas)
         return;
     const int i = a.gas[k];
-    const double qx = a.x[i], qy = a.y[i], qz = a.z[i];
     const double h = a.h[i];
     const int nn = a.nb_count[k];
-    const int *lst = a.nb + k;
     const size_t stride = (size_t)a.stride;
     double rho = 0.0;
-    for (int s = 0; s < nn; s++) {
-        const int j = lst[stride * s];
-        double dx = qx - a.x[j];
-        double dy = qy - a.y[j];
-        double dz = qz - a.z[j];
-        double r = sqrt(dx * dx + dy * dy + dz * dz);
-        rho += a.m[j] * kernel_W(r, h);
-    }
+    for (int s = 0; s < nn; s++)
+        rho += a.term[stride * s + k];
     if (nn < 20 && h < 50.0)
         a.h[i] = h * 1.2;
     else if (nn > 48 && h > 0.1)
@@ -253,7 +279,7 @@ __global__ void __launch_bounds__(SPH_THREADS) k_sph_density_pairs(SphArgs a)
 
 // Per-body terms of the force pass: P/(rho^2 + 1e-15) and the sound speed
 // sqrt(gamma P/(rho + 1e-15)) (src/sph.c:112, :153-154, :170-171). The pair
-// loop needs them for both bodies of every pair; computing them once per body
+// terms need them for both bodies of every pair; computing them once per body
 // gives the same values as the reference's per-pair evaluation.
 __global__ void __launch_bounds__(SPH_THREADS) k_sph_body_terms(SphArgs a)
 {
@@ -266,55 +292,74 @@ __global__ void __launch_bounds__(SPH_THREADS) k_sph_body_terms(SphArgs a)
     a.cs[j] = sqrt(GAMMA * P / (rho + 1e-15));
 }
 
-// Pressure gradient + Monaghan viscosity over the recorded list,
-// src/sph.c:101-196.
-__global__ void __launch_bounds__(SPH_THREADS) k_sph_forces_pairs(SphArgs a)
+// Pressure gradient + Monaghan viscosity terms, src/sph.c:126-186.
+__global__ void __launch_bounds__(SPH_THREADS) k_sph_force_terms(SphArgs a)
+{
+    const int n_gas = a.sc->n_gas;
+    const long long total = (long long)CSG_SPH_MAX_NEIGHBORS * n_gas;
+    const size_t stride = (size_t)a.stride;
+    const size_t plane = stride * CSG_SPH_MAX_NEIGHBORS;
+    for (long long t = (long long)blockIdx.x * SPH_THREADS + threadIdx.x; t < total;
+         t += (long long)gridDim.x * SPH_THREADS) {
+        int s, k;
+        if (!pair_slot(a, t, n_gas, s, k))
+            continue;
+        const size_t o = stride * s + k;
+        const int i = a.gas[k];
+        const int j = a.nb[o];
+        double tx = 0.0, ty = 0.0, tz = 0.0;
+        if (j != i && a.type[j] == BODY_GAS) {
+            double dx = a.x[i] - a.x[j];
+            double dy = a.y[i] - a.y[j];
+            double dz = a.z[i] - a.z[j];
+            double r = sqrt(dx * dx + dy * dy + dz * dz);
+            if (!(r < 1e-15)) {
+                const double h_i = a.h[i], rho_i = a.rho[i];
+                double h_avg = 0.5 * (h_i + a.h[j]);
+                double rho_j = a.rho[j];
+                double dvx = a.vx[i] - a.vx[j];
+                double dvy = a.vy[i] - a.vy[j];
+                double dvz = a.vz[i] - a.vz[j];
+                double vr = dvx * dx + dvy * dy + dvz * dz;
+                double visc = 0.0;
+                if (vr < 0.0) {
+                    double mu = h_avg * vr / (r * r + 0.01 * h_avg * h_avg);
+                    double c_avg = 0.5 * (a.cs[i] + a.cs[j]);
+                    double rho_avg = 0.5 * (rho_i + rho_j);
+                    visc = (-1.0 * c_avg * mu + 2.0 * mu * mu) / (rho_avg + 1e-15);
+                }
+                double g = kernel_dWdr(r, h_avg);
+                double gx = g * dx / r;
+                double gy = g * dy / r;
+                double gz = g * dz / r;
+                double f = a.m[j] * (a.pr2[i] + a.pr2[j] + visc);
+                tx = f * gx;
+                ty = f * gy;
+                tz = f * gz;
+            }
+        }
+        a.term[o] = tx;
+        a.term[plane + o] = ty;
+        a.term[2 * plane + o] = tz;
+    }
+}
+
+// Sums of the force terms in list order, src/sph.c:187-196.
+__global__ void __launch_bounds__(SPH_THREADS) k_sph_force_sums(SphArgs a)
 {
     const int k = blockIdx.x * SPH_THREADS + threadIdx.x;
     if (k >= a.sc->n_gas)
         return;
     const int i = a.gas[k];
-    const double qx = a.x[i], qy = a.y[i], qz = a.z[i];
-    const double h_i = a.h[i];
-    const double rho_i = a.rho[i];
-    const double c_i = a.cs[i];
-    const double pr2_i = a.pr2[i];
-    const double vxi = a.vx[i], vyi = a.vy[i], vzi = a.vz[i];
     const int nn = a.nb_count[k];
-    const int *lst = a.nb + k;
     const size_t stride = (size_t)a.stride;
+    const size_t plane = stride * CSG_SPH_MAX_NEIGHBORS;
     double sx = 0.0, sy = 0.0, sz = 0.0;
     for (int s = 0; s < nn; s++) {
-        const int j = lst[stride * s];
-        if (j == i || a.type[j] != BODY_GAS)
-            continue;
-        double dx = qx - a.x[j];
-        double dy = qy - a.y[j];
-        double dz = qz - a.z[j];
-        double r = sqrt(dx * dx + dy * dy + dz * dz);
-        if (r < 1e-15)
-            continue;
-        double h_avg = 0.5 * (h_i + a.h[j]);
-        double rho_j = a.rho[j];
-        double dvx = vxi - a.vx[j];
-        double dvy = vyi - a.vy[j];
-        double dvz = vzi - a.vz[j];
-        double vr = dvx * dx + dvy * dy + dvz * dz;
-        double visc = 0.0;
-        if (vr < 0.0) {
-            double mu = h_avg * vr / (r * r + 0.01 * h_avg * h_avg);
-            double c_avg = 0.5 * (c_i + a.cs[j]);
-            double rho_avg = 0.5 * (rho_i + rho_j);
-            visc = (-1.0 * c_avg * mu + 2.0 * mu * mu) / (rho_avg + 1e-15);
-        }
-        double g = kernel_dWdr(r, h_avg);
-        double gx = g * dx / r;
-        double gy = g * dy / r;
-        double gz = g * dz / r;
-        double f = a.m[j] * (pr2_i + a.pr2[j] + visc);
-        sx -= f * gx;
-        sy -= f * gy;
-        sz -= f * gz;
+        const size_t o = stride * s + k;
+        sx -= a.term[o];
+        sy -= a.term[plane + o];
+        sz -= a.term[2 * plane + o];
     }
     if (isnan(sx))
         sx = 0.0;
@@ -414,6 +459,7 @@ SphArgs make_args(csgd_t *d)
     a.nb_count = d->nb_count;
     a.pr2 = d->pr2;
     a.cs = d->cs;
+    a.term = d->sph_term;
     a.n = d->n;
     a.node_cap = d->node_cap;
     a.stride = d->cap;
@@ -482,14 +528,18 @@ static int ensure_lists(csgd_t *d)
         cudaFree(d->pr2);
     if (d->cs)
         cudaFree(d->cs);
+    if (d->sph_term)
+        cudaFree(d->sph_term);
     d->nb = nullptr;
     d->nb_count = nullptr;
-    d->pr2 = d->cs = nullptr;
+    d->pr2 = d->cs = d->sph_term = nullptr;
     size_t c = (size_t)(d->cap > 0 ? d->cap : 1);
     if (cudaMalloc((void **)&d->nb, sizeof(int) * CSG_SPH_MAX_NEIGHBORS * c) != cudaSuccess ||
         cudaMalloc((void **)&d->nb_count, sizeof(int) * c) != cudaSuccess ||
         cudaMalloc((void **)&d->pr2, sizeof(double) * c) != cudaSuccess ||
-        cudaMalloc((void **)&d->cs, sizeof(double) * c) != cudaSuccess) {
+        cudaMalloc((void **)&d->cs, sizeof(double) * c) != cudaSuccess ||
+        cudaMalloc((void **)&d->sph_term, sizeof(double) * 3 * CSG_SPH_MAX_NEIGHBORS * c) !=
+            cudaSuccess) {
         cudaGetLastError();
         csgd_set_err(d, CSG_ERR_NOMEM);
         return CSG_ERR_NOMEM;
@@ -522,12 +572,17 @@ static int sph_pass(csgd_t *d, int forces)
     if (gl > 152 * 16)
         gl = 152 * 16;
     { k_sph_lists<<<gl, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
+    // pair terms: a grid-stride pass over (slot, gas body), sized for 32 warps
+    // per SM (the gas count is known on the device only)
+    const int gp = d->num_sms * (2048 / SPH_THREADS);
     if (forces) {
         { k_sph_body_terms<<<g, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
-        { k_sph_forces_pairs<<<g, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
+        { k_sph_force_terms<<<gp, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
+        { k_sph_force_sums<<<g, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
+    } else {
+        { k_sph_density_terms<<<gp, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
+        { k_sph_density_sums<<<g, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
     }
-    else
-        { k_sph_density_pairs<<<g, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
     return csgd_check(d, cudaGetLastError());
 }
 

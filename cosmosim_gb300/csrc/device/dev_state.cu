@@ -290,6 +290,8 @@ extern "C" void csgd_destroy(csgd_t *d)
         cudaFree(d->pr2);
     if (d->cs)
         cudaFree(d->cs);
+    if (d->sph_term)
+        cudaFree(d->sph_term);
     if (d->sc)
         cudaFree(d->sc);
     if (d->roots)
