@@ -1,7 +1,8 @@
 // dev_sort.cu — exclusive scan and stable LSD radix sort used by the tree build.
 //
 // Radix sort: 8-bit digits, three kernels per digit (tile histogram, scan of
-// the digit-major histogram, stable scatter). Stability inside a tile comes
+// the digit-major histogram, stable scatter); tiles of 1024 keys below 2M keys,
+// 4096 above. Stability inside a tile comes
 // from giving each warp a contiguous slice of the tile and ranking equal
 // digits with __match_any_sync in input order; across tiles from the
 // digit-major exclusive scan. Stability matters: keys that tie keep caller
@@ -17,9 +18,9 @@ constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
 constexpr int SORT_THREADS = 256;
 constexpr int SORT_WARPS = SORT_THREADS / CSG_WARP;
-constexpr int SORT_ITEMS_PER_LANE = 16;
-constexpr int SORT_WARP_ITEMS = CSG_WARP * SORT_ITEMS_PER_LANE; // 512
-constexpr int SORT_TILE = SORT_WARPS * SORT_WARP_ITEMS;          // 4096
+// Items per lane: 16 (tiles of 4096 keys) for large sorts, 4 (tiles of 1024)
+// below 2M keys, so that a 100k-key sort still spreads over ~100 blocks.
+constexpr int sort_tile(int ipl) { return SORT_WARPS * CSG_WARP * ipl; }
 constexpr int RADIX = 256;
 
 __device__ __forceinline__ int warp_incl_scan(int v)
@@ -86,6 +87,7 @@ __global__ void k_scan_total(int *__restrict__ out, int n, const int *__restrict
 
 // ---- radix sort kernels ----
 
+template <int IPL>
 __global__ void k_radix_hist(const unsigned long long *__restrict__ key, int n, int shift,
                              unsigned int *__restrict__ hist, int nblocks)
 {
@@ -93,8 +95,8 @@ __global__ void k_radix_hist(const unsigned long long *__restrict__ key, int n, 
     for (int i = threadIdx.x; i < RADIX; i += blockDim.x)
         h[i] = 0;
     __syncthreads();
-    const long long t0 = (long long)blockIdx.x * SORT_TILE;
-    for (int k = threadIdx.x; k < SORT_TILE; k += blockDim.x) {
+    const long long t0 = (long long)blockIdx.x * sort_tile(IPL);
+    for (int k = threadIdx.x; k < sort_tile(IPL); k += blockDim.x) {
         long long i = t0 + k;
         if (i < n)
             atomicAdd(&h[(unsigned)(key[i] >> shift) & (RADIX - 1)], 1u);
@@ -104,6 +106,7 @@ __global__ void k_radix_hist(const unsigned long long *__restrict__ key, int n, 
         hist[(size_t)i * nblocks + blockIdx.x] = h[i];
 }
 
+template <int IPL>
 __global__ void k_radix_scatter(const unsigned long long *__restrict__ key_in,
                                 const int *__restrict__ val_in,
                                 unsigned long long *__restrict__ key_out,
@@ -115,10 +118,11 @@ __global__ void k_radix_scatter(const unsigned long long *__restrict__ key_in,
     for (int i = threadIdx.x; i < SORT_WARPS * RADIX; i += blockDim.x)
         (&wcount[0][0])[i] = 0;
     __syncthreads();
-    const long long w0 = (long long)blockIdx.x * SORT_TILE + (long long)warp * SORT_WARP_ITEMS;
+    const long long w0 =
+        (long long)blockIdx.x * sort_tile(IPL) + (long long)warp * (CSG_WARP * IPL);
     const unsigned lt = (1u << lane) - 1u;
     // pass 1: per-warp digit counts
-    for (int c = 0; c < SORT_ITEMS_PER_LANE; c++) {
+    for (int c = 0; c < IPL; c++) {
         long long i = w0 + c * CSG_WARP + lane;
         int dg = (i < n) ? (int)((key_in[i] >> shift) & (RADIX - 1)) : RADIX;
         unsigned peers = __match_any_sync(0xffffffffu, dg);
@@ -138,7 +142,7 @@ __global__ void k_radix_scatter(const unsigned long long *__restrict__ key_in,
     }
     __syncthreads();
     // pass 2: stable placement in input order
-    for (int c = 0; c < SORT_ITEMS_PER_LANE; c++) {
+    for (int c = 0; c < IPL; c++) {
         long long i = w0 + c * CSG_WARP + lane;
         unsigned long long k = 0;
         int v = 0;
@@ -208,7 +212,9 @@ int csg_radix_sort(csgd_t *d, unsigned long long *key, int *val, unsigned long l
 {
     if (n <= 1)
         return CSG_OK;
-    const int nblocks = (n + SORT_TILE - 1) / SORT_TILE;
+    const bool small = n < (2 << 20);
+    const int tile = small ? sort_tile(4) : sort_tile(16);
+    const int nblocks = (n + tile - 1) / tile;
     const int hn = RADIX * nblocks;
     if (2 * hn + 1 > d->sort_hist_cap) {
         csgd_set_err(d, CSG_ERR_NOMEM);
@@ -221,12 +227,17 @@ int csg_radix_sort(csgd_t *d, unsigned long long *key, int *val, unsigned long l
     const int passes = (bits + 7) / 8;
     for (int p = 0; p < passes; p++) {
         const int shift = 8 * p;
-        { k_radix_hist<<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, n, shift, hist, nblocks); d->launches++; }
+        if (small)
+            { k_radix_hist<4><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, n, shift, hist, nblocks); d->launches++; }
+        else
+            { k_radix_hist<16><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, n, shift, hist, nblocks); d->launches++; }
         int rc = csg_scan_exclusive(d, (const int *)hist, offs, hn, nullptr);
         if (rc)
             return rc;
-        { k_radix_scatter<<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, offs,
-                                                                  nblocks); d->launches++; }
+        if (small)
+            { k_radix_scatter<4><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, offs, nblocks); d->launches++; }
+        else
+            { k_radix_scatter<16><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, offs, nblocks); d->launches++; }
         unsigned long long *tk = ki;
         ki = ko;
         ko = tk;

@@ -379,8 +379,10 @@ extern "C" int csgd_reserve(csgd_t *d, int n)
     ok &= dalloc(&d->perm, cap) == cudaSuccess;
     ok &= dalloc(&d->perm_alt, cap) == cudaSuccess;
     ok &= dalloc(&d->ext, 3 * cap) == cudaSuccess;
+    // digit-major tile histograms: tiles of 1024 keys below 2M keys, else 4096
     const size_t sort_items = ncap;
-    const size_t hist = 256 * ((sort_items + 4095) / 4096);
+    const size_t hist = 256 * (sort_items < (2u << 20) ? (sort_items + 1023) / 1024
+                                                       : (sort_items + 4095) / 4096);
     d->sort_hist_cap = (int)(2 * hist + 1);
     ok &= dalloc(&d->sort_hist, (size_t)d->sort_hist_cap) == cudaSuccess;
     ok &= dalloc(&d->lcp, cap) == cudaSuccess;
