@@ -73,6 +73,46 @@ __global__ void k_scan_tile(const int *__restrict__ in, int *__restrict__ out, i
         sums[blockIdx.x] = run;
 }
 
+// Exclusive scan of up to SCAN_SMALL items by one block: each thread sums a
+// contiguous chunk, the block scans the chunk sums, each thread rescans its
+// chunk. One launch instead of the tile/recursion/add/total sequence for the
+// small scans a substep does; writes out[n] = total.
+constexpr int SCAN_SMALL = 16 * SCAN_TILE;
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_small(const int *__restrict__ in,
+                                                             int *__restrict__ out, int n,
+                                                             const int *__restrict__ limit)
+{
+    __shared__ int warp_tot[SCAN_THREADS / 32];
+    __shared__ int total_s;
+    const int lim = limit ? min(n, *limit) : n;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int chunk = (n + SCAN_THREADS - 1) / SCAN_THREADS;
+    const int b0 = min(n, threadIdx.x * chunk), b1 = min(n, b0 + chunk);
+    int local = 0;
+    for (int i = b0; i < b1; i++)
+        local += (i < lim) ? in[i] : 0;
+    const int incl = warp_incl_scan(local);
+    if (lane == 31)
+        warp_tot[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const int t = warp_tot[lane];
+        const int ti = warp_incl_scan(t);
+        warp_tot[lane] = ti - t;
+        if (lane == 31)
+            total_s = ti;
+    }
+    __syncthreads();
+    int run = warp_tot[warp] + incl - local;
+    for (int i = b0; i < b1; i++) {
+        out[i] = run;
+        run += (i < lim) ? in[i] : 0;
+    }
+    if (threadIdx.x == 0)
+        out[n] = total_s;
+}
+
 __global__ void k_scan_add(int *__restrict__ out, int n, const int *__restrict__ offs)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -172,6 +212,10 @@ int csg_scan_exclusive(csgd_t *d, const int *in, int *out, int n, const int *cou
 {
     if (n <= 0) {
         cudaMemsetAsync(out, 0, sizeof(int), d->stream);
+        return csgd_check(d, cudaGetLastError());
+    }
+    if (n <= SCAN_SMALL) {
+        { k_scan_small<<<1, SCAN_THREADS, 0, d->stream>>>(in, out, n, count_limit); d->launches++; }
         return csgd_check(d, cudaGetLastError());
     }
     // level sizes: n -> ceil(n/T) -> ... -> 1
