@@ -384,10 +384,8 @@ __device__ __forceinline__ void walk_cells(const WalkArgs &a, NodeW32 *win, int 
             const float band = c.B.w * a.guard_rel;
             bool acc = (c.B.w < lhs - band) && d2 > 0.f;
             const bool amb = active && !acc && !(c.B.w > lhs + band);
-            if (__any_sync(0xffffffffu, amb)) {
-                if (amb)
-                    acc = decide64(a, cur, b.px, b.py, b.pz);
-            }
+            if (amb) // rare
+                acc = decide64(a, cur, b.px, b.py, b.pz);
             take = active && acc;
             open = active && !acc;
             if (take)
@@ -414,8 +412,12 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v)
 }
 
 // FP32-mixed walk: pair terms in FP32 from ~48-bit position differences,
-// summed per lane in blocks of up to 8 terms that are added with Kahan
-// compensation (per-body compensated FP32 summation); G applied once.
+// summed per lane in blocks (one term per warp step at most, flushed every 8
+// steps for the whole warp) that are added with Kahan compensation
+// (per-body compensated FP32 summation); G applied once. The step is
+// branch-light: every lane computes the pair term and lanes that do not take
+// the cell add zero, so the warp never splits on "take".
+
 template <bool STATS, bool EMPTY>
 __device__ __forceinline__ void walk32_task(const WalkArgs &a, NodeW32 *win, const TaskRange &tr,
                                             WalkStats &st)
@@ -430,93 +432,76 @@ __device__ __forceinline__ void walk32_task(const WalkArgs &a, NodeW32 *win, con
     const float lx = (float)(px - (double)hx), ly = (float)(py - (double)hy),
                 lz = (float)(pz - (double)hz);
     float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-    float bx = 0.f, by = 0.f, bz = 0.f; // current block of up to 8 terms
-    int nblk = 0;
     int skip = valid ? 0 : INT_MAX;
     int cur = tr.root, wbase = INT_MIN / 2;
-    auto interact = [&](const NodeW32 &c, float dx, float dy, float dz, float d2) {
-        const float y = rsqrtf(d2 + a.eps2f);
-        const float f = c.m * (y * y * y);
-        bx = fmaf(f, dx, bx);
-        by = fmaf(f, dy, by);
-        bz = fmaf(f, dz, bz);
-        if (++nblk == 8) { // compensated add of the block
-            kahan_add(sx, cx, bx);
-            kahan_add(sy, cy, by);
-            kahan_add(sz, cz, bz);
-            bx = by = bz = 0.f;
-            nblk = 0;
-        }
-        if (STATS)
-            st.hits++;
-    };
     while (cur < nn) {
-        if (cur - wbase >= CSG_WARP) {
-            wbase = cur;
-            __syncwarp();
-            if (wbase + lane < nn)
-                win[lane] = a.w32[wbase + lane];
-            __syncwarp();
-        }
-        const NodeW32 c = win[cur - wbase];
-        if (STATS) {
-            st.steps++;
-            st.active += (cur >= skip);
-        }
-        if (c.body >= 0) {
-            // a leaf (warp-uniform): nothing below it to open, so no vote;
-            // every lane still walking takes it unless it is its own body
-            if (cur >= skip && c.body != me && !(EMPTY && c.m == 0.0f && a.w64[cur].m == 0.0)) {
-                const float dx = (c.cx - hx) + (c.lx - lx);
-                const float dy = (c.cy - hy) + (c.ly - ly);
-                const float dz = (c.cz - hz) + (c.lz - lz);
-                interact(c, dx, dy, dz, fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-            }
-            if (c.next <= cur) {
-                dev_fail(a.sc, CSG_ERR_WALK_LIMIT);
+        // a block of up to 8 steps: at most one term per lane per step, then
+        // one compensated add of the block (warp-uniform)
+        float bx = 0.f, by = 0.f, bz = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            if (cur >= nn)
                 break;
+            if (cur - wbase >= CSG_WARP) {
+                wbase = cur;
+                __syncwarp();
+                if (wbase + lane < nn)
+                    win[lane] = a.w32[wbase + lane];
+                __syncwarp();
             }
-            cur = c.next;
-            continue;
-        }
-        bool open = false;
-        if (cur >= skip) {
-            if (EMPTY && c.m == 0.0f && a.w64[cur].m == 0.0) {
-                skip = c.next; // empty cell of a caller pool (src/octree.c:181-182)
-            } else {
-                const float dx = (c.cx - hx) + (c.lx - lx);
-                const float dy = (c.cy - hy) + (c.ly - ly);
-                const float dz = (c.cz - hz) + (c.lz - lz);
-                const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                // |theta^2 d^2 - s^2| inside the FP32 error band -> decide in FP64
-                const float lhs = a.theta2f * d2;
-                const float band = c.s2 * a.guard_rel;
-                bool take;
-                if (c.s2 < lhs - band && d2 > 0.f) {
-                    take = true;
-                } else if (c.s2 > lhs + band) {
+            const NodeW32 c = win[cur - wbase];
+            const bool active = cur >= skip;
+            if (STATS) {
+                st.steps++;
+                st.active += active;
+            }
+            const float dx = (c.cx - hx) + (c.lx - lx);
+            const float dy = (c.cy - hy) + (c.ly - ly);
+            const float dz = (c.cz - hz) + (c.lz - lz);
+            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            bool take;
+            int nxt;
+            if (c.body >= 0) { // leaf (warp-uniform): nothing to open, no vote
+                take = active && c.body != me;
+                if (EMPTY && take && c.m == 0.0f && a.w64[cur].m == 0.0)
                     take = false;
-                } else { // rare: decided by the reference's FP64 test, out of line
-                    take = decide64(a, cur, px, py, pz);
-                }
-                if (take) {
-                    skip = c.next;
-                    interact(c, dx, dy, dz, d2);
+                nxt = c.next;
+            } else {
+                bool acc, open;
+                if (EMPTY && c.m == 0.0f && a.w64[cur].m == 0.0) { // empty cell of a caller pool
+                    acc = false;
+                    open = false;
+                    if (active)
+                        skip = c.next;
                 } else {
-                    open = true;
+                    // |theta^2 d^2 - s^2| inside the FP32 error band -> decide in FP64
+                    const float lhs = a.theta2f * d2;
+                    const float band = c.s2 * a.guard_rel;
+                    acc = (c.s2 < lhs - band) && d2 > 0.f;
+                    const bool amb = active && !acc && !(c.s2 > lhs + band);
+                    if (amb) // rare
+                        acc = decide64(a, cur, px, py, pz);
+                    open = active && !acc;
                 }
+                take = active && acc;
+                skip = take ? c.next : skip;
+                nxt = __any_sync(0xffffffffu, open) ? cur + 1 : c.next;
             }
+            const float y = rsqrtf(d2 + a.eps2f);
+            const float f = take ? c.m * (y * y * y) : 0.0f;
+            bx = fmaf(f, dx, bx);
+            by = fmaf(f, dy, by);
+            bz = fmaf(f, dz, bz);
+            if (STATS)
+                st.hits += take;
+            // every tree built or imported here has next > id; the max keeps
+            // the walk finite on any other
+            cur = max(nxt, cur + 1);
         }
-        const int nxt = __any_sync(0xffffffffu, open) ? cur + 1 : c.next;
-        if (nxt <= cur) {
-            dev_fail(a.sc, CSG_ERR_WALK_LIMIT);
-            break;
-        }
-        cur = nxt;
+        kahan_add(sx, cx, bx);
+        kahan_add(sy, cy, by);
+        kahan_add(sz, cz, bz);
     }
-    kahan_add(sx, cx, bx);
-    kahan_add(sy, cy, by);
-    kahan_add(sz, cz, bz);
     if (valid) {
         a.ax[me] = a.G * ((double)sx - (double)cx);
         a.ay[me] = a.G * ((double)sy - (double)cy);
