@@ -273,9 +273,17 @@ def run_ensemble(args, torch, lib, rank, world):
     dev = torch.cuda.current_device()
     stream = torch.cuda.current_stream()
     flush = flush_buffer(torch)
+    t0 = time.perf_counter()
     allb, parts = ensemble_bodies(lib, rank)
+    t_host_ics = time.perf_counter() - t0
     sizes = [len(p) for p in parts]
     n_total = len(allb)
+    # the same 64 systems generated on the GPU straight into a handle
+    t0 = time.perf_counter()
+    dev_ens = lib.Sim.ensemble_ics(3, sizes, SEED + 1000 * rank, softening=e["eps"],
+                                   theta=e["theta"], dt=e["dt"], precision=lib.PREC_FP32_MIXED)
+    t_dev_ics = time.perf_counter() - t0
+    dev_ens.close()
     common = dict(softening=e["eps"], theta=e["theta"], dt=e["dt"])
     res = {}
     # the batched handle, FP32-mixed: autotune the walk shape, then time substeps
@@ -374,7 +382,9 @@ def run_ensemble(args, torch, lib, rank, world):
         "fp64_walk_vs_direct": rel_err_stats(a64[sample], direct),
         "direct_sample": int(len(sample))}
     return dict(n_total=n_total, sizes=sizes, runs=res, best=best, candidates=cands,
-                errors=errors, clocks=clocks, e2e_s=e2e_s, e2e_steps=ke)
+                errors=errors, clocks=clocks, e2e_s=e2e_s, e2e_steps=ke,
+                ic_s={"host_generator_64_galaxies": t_host_ics,
+                      "device_generated_handle_incl_first_forces": t_dev_ics})
 
 
 def ensemble_line(args, torch, lib, rank, world, fp32_peak):
@@ -406,6 +416,7 @@ def ensemble_line(args, torch, lib, rank, world, fp32_peak):
                    "l2": "512 MB flush between timed substeps",
                    "parallelism": f"replicas x{world}"},
         "walk_shape": {"autotuned": r["best"], "candidates": r["candidates"]},
+        "initial_conditions_s": r["ic_s"],
         "baselines": {
             "ensemble_fp64_plain": rate(runs["fp64"]),
             "sequential_64_handles_fp64_plain": rate(runs["seq_fp64"]),

@@ -25,9 +25,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-fvisibility=hidden", "--expt-relaxed-constexpr"]
 # Kernels that must round exactly like the reference's C (no fused multiply-add).
-NO_FMA = {"dev_state.cu", "dev_sph.cu", "dev_quasar.cu"}
-CC_FLAGS = ["-std=c11", "-O2", "-fPIC", "-fvisibility=hidden", "-Wall", "-Wextra",
-            "-Wno-unused-parameter"]
+NO_FMA = {"dev_state.cu", "dev_sph.cu", "dev_quasar.cu", "dev_ics.cu"}
+# -ffp-contract=off: the host layer (initial conditions) rounds the same on
+# x86_64 and aarch64, and as the device generators do.
+CC_FLAGS = ["-std=c11", "-O2", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", "-Wall",
+            "-Wextra", "-Wno-unused-parameter"]
 
 
 def _nvcc():

@@ -36,6 +36,8 @@ void csgd_destroy(csgd_t *d);
 /* Uses the given cudaStream_t (NULL = the state's own stream). */
 void csgd_set_stream(csgd_t *d, void *stream);
 void *csgd_stream(csgd_t *d);
+/* The device Body staging array (capacity >= the reserved body count). */
+Body *csgd_aos(csgd_t *d);
 
 /* Tree builds also record what a reference-order pool export needs (on for
    states that export after most builds; export works either way). */
@@ -66,14 +68,31 @@ int csgd_autotune_walk(csgd_t *d, const csgd_force_params *p, int reps, CsgWalkS
 /* Body array-of-structs <-> device SoA (host buffers may be pageable). */
 int csgd_upload_bodies(csgd_t *d, const Body *host, int n);
 int csgd_download_bodies(csgd_t *d, Body *host, int n);
-/* Refreshes the device Body staging from the SoA fields (no copy to the host). */
+/* Refreshes the device Body staging from the SoA fields (no copy to the host),
+   and the SoA fields from the staging. */
 int csgd_pack_aos(csgd_t *d);
+int csgd_unpack_aos(csgd_t *d);
 
 /* Alive bodies (mass <= 0 skipped) as packed float records, in index order,
    at most max_bodies: CSG_SNAPSHOT_UE (16 floats) or CSG_SNAPSHOT_RENDER (10).
    out is a device pointer when out_is_device, else host memory. Blocks. */
 int csgd_snapshot_f32(csgd_t *d, int format, float *out, int out_is_device, int max_bodies,
                       int *count_out);
+
+/* Exponential-disk initial conditions generated on the device (the recipe of
+   csg_generate_ics kinds 0, 3, 5, 6): system g gets counts[g] bodies from
+   plans[g], written to out (device Body array) one system after another.
+   The seeded xorshift64 stream is jumped ahead per run of bodies, so body i
+   draws the same numbers as the host generator's body i. Blocks. */
+typedef struct {
+    double mass, rd, zh, smbh, gas_frac, bulge_mass, bulge_a;
+    uint64_t seed;   /* generator state before the disk's first draw */
+    int pad;
+} csgd_disk_plan;
+int csgd_generate_disks(void *stream, const csgd_disk_plan *plans, const int *counts, int n_sys,
+                        Body *out);
+/* Replaces the bodies by a device Body array of n bodies (D2D). */
+int csgd_upload_device_bodies(csgd_t *d, const Body *device_bodies, int n);
 
 /* Quasar step on the device (reference src/quasar.c:477-509): may append
    bodies up to n_alloc (<= the reserved capacity); *jet_count is read and

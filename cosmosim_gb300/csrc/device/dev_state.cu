@@ -316,6 +316,8 @@ extern "C" void csgd_set_stream(csgd_t *d, void *stream)
 
 extern "C" void *csgd_stream(csgd_t *d) { return (void *)d->stream; }
 
+extern "C" Body *csgd_aos(csgd_t *d) { return d->aos; }
+
 extern "C" int csgd_count(const csgd_t *d) { return d->n; }
 
 extern "C" void csgd_enable_stats(csgd_t *d, int on)
@@ -518,6 +520,19 @@ extern "C" int csgd_system_count(const csgd_t *d) { return d->n_gal; }
 
 // ---- host I/O --------------------------------------------------------------
 
+extern "C" int csgd_unpack_aos(csgd_t *d)
+{
+    const int n = d->n;
+    if (n <= 0)
+        return CSG_OK;
+    { k_unpack<<<csgd_grid(n, 256), 256, 0, d->stream>>>(d->aos, n, d->x, d->y, d->z, d->vx, d->vy,
+                                                        d->vz, d->ax, d->ay, d->az, d->m, d->type,
+                                                        d->rho, d->P, d->u, d->h); d->launches++; }
+    d->geometry_valid = 0;
+    d->gas_valid = 0;
+    return csgd_check(d, cudaGetLastError());
+}
+
 extern "C" int csgd_upload_bodies(csgd_t *d, const Body *host, int n)
 {
     int rc = csgd_reserve(d, n);
@@ -526,12 +541,7 @@ extern "C" int csgd_upload_bodies(csgd_t *d, const Body *host, int n)
     if (n == 0)
         return CSG_OK;
     cudaMemcpyAsync(d->aos, host, sizeof(Body) * (size_t)n, cudaMemcpyHostToDevice, d->stream);
-    { k_unpack<<<csgd_grid(n, 256), 256, 0, d->stream>>>(d->aos, n, d->x, d->y, d->z, d->vx, d->vy,
-                                                        d->vz, d->ax, d->ay, d->az, d->m, d->type,
-                                                        d->rho, d->P, d->u, d->h); d->launches++; }
-    d->geometry_valid = 0;
-    d->gas_valid = 0;
-    return csgd_check(d, cudaGetLastError());
+    return csgd_unpack_aos(d);
 }
 
 extern "C" int csgd_pack_aos(csgd_t *d)

@@ -35,5 +35,6 @@ void csg_ref_quasar_merger(Body *bodies, int n, double separation, double approa
                            double smbh_mass_frac, uint64_t seed);
 void csg_ref_merger_dust(Body *bodies, int start_idx, int n_dust, double separation,
                          uint64_t seed);
+int csg_disk_plan(int kind, uint64_t seed, csgd_disk_plan *plan);
 
 #endif

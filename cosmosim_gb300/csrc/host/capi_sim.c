@@ -287,6 +287,87 @@ CSG_EXPORT SimHandle cosmosim_create_ensemble(const Body *bodies, int n, int n_s
     return (SimHandle)start_systems(s, n_sys, counts);
 }
 
+CSG_EXPORT SimHandle cosmosim_create_ensemble_ics(int kind, int n_sys, const int *counts,
+                                                  uint64_t seed0, const CsgSimParams *params)
+{
+    if (n_sys < 1 || n_sys > CSG_MAX_SYSTEMS || !counts || !params) {
+        csg_thread_set_error(CSG_ERR_BAD_ARG);
+        return NULL;
+    }
+    if (params->sph) {
+        csg_thread_set_error(CSG_ERR_UNSUPPORTED);
+        return NULL;
+    }
+    long long total = 0;
+    csgd_disk_plan *plans = (csgd_disk_plan *)calloc((size_t)n_sys, sizeof(csgd_disk_plan));
+    if (!plans) {
+        csg_thread_set_error(CSG_ERR_NOMEM);
+        return NULL;
+    }
+    for (int g = 0; g < n_sys; g++) {
+        if (counts[g] < 0 || csg_disk_plan(kind, seed0 + (uint64_t)g, &plans[g])) {
+            free(plans);
+            csg_thread_set_error(CSG_ERR_BAD_ARG);
+            return NULL;
+        }
+        total += counts[g];
+    }
+    if (total < 1 || total > 0x7fffffff) {
+        free(plans);
+        csg_thread_set_error(CSG_ERR_BAD_ARG);
+        return NULL;
+    }
+    const int n = (int)total;
+    SimState *s = (SimState *)calloc(1, sizeof(SimState));
+    Body *host = (Body *)calloc((size_t)n, sizeof(Body));
+    csgd_t *d = csgd_create();
+    int rc = (!s || !host) ? CSG_ERR_NOMEM : (!d ? CSG_ERR_NO_DEVICE : CSG_OK);
+    if (!rc)
+        rc = csgd_reserve(d, n);
+    if (!rc) /* generated straight into the device Body staging */
+        rc = csgd_generate_disks(csgd_stream(d), plans, counts, n_sys, csgd_aos(d));
+    if (!rc)
+        rc = csgd_unpack_aos(d);
+    if (!rc)
+        rc = csgd_set_systems(d, n_sys, counts);
+    csgd_force_params p;
+    if (s)
+        s->params = *params;
+    if (!rc) {
+        p.G = params->G;
+        p.softening = params->softening;
+        p.theta = params->theta;
+        p.precision = params->precision;
+        rc = csgd_build_tree(d, 0);
+    }
+    if (!rc)
+        rc = csgd_gravity(d, &p);
+    if (!rc)
+        rc = csgd_download_bodies(d, host, n);
+    if (!rc)
+        rc = csgd_sync(d);
+    free(plans);
+    if (rc) {
+        if (d)
+            csgd_destroy(d);
+        free(host);
+        free(s);
+        csg_thread_set_error(rc);
+        return NULL;
+    }
+    s->dev = d;
+    s->host = host;
+    s->n_alloc = n;
+    s->current_n = n;
+    s->config = cosmosim_default_config();
+    s->config.n_bodies = n;
+    s->config.dt = params->dt;
+    s->config.theta = params->theta;
+    s->config.substeps = params->substeps;
+    csg_thread_set_error(CSG_OK);
+    return (SimHandle)s;
+}
+
 CSG_EXPORT int cosmosim_system_count(SimHandle handle)
 {
     if (!handle)

@@ -420,6 +420,46 @@ static void merger(Body *out, int n, double gas_frac, Rng *r)
     shift(out + n1, n2, sep * m1 / mt, 0.0, 0.0, -vrad * m1 / mt, -vtan * m1 / mt, 0.0);
 }
 
+/* The disk of kinds 0, 3, 5, 6 as a plan for the device generator: its
+   DiskSpec and the generator state before its first body's draws (kind 3
+   draws its scale length and SMBH fraction first). Returns 0, or -1 for a
+   kind that is not a single disk. */
+int csg_disk_plan(int kind, uint64_t seed, csgd_disk_plan *plan)
+{
+    Rng r;
+    rng_seed(&r, seed);
+    DiskSpec s;
+    switch (kind) {
+    case 0:
+        s = (DiskSpec){1.0, 1.0, 0.1, 0.01, 0.0, 0.0, 0.0};
+        break;
+    case 3: {
+        double rd = 0.5 + 1.5 * rng_uniform(&r);
+        double f = 0.001 + 0.019 * rng_uniform(&r);
+        s = (DiskSpec){1.0, rd, 0.1 * rd, f, 0.0, 0.0, 0.0};
+        break;
+    }
+    case 5:
+        s = (DiskSpec){1.0, 1.0, 0.1, 0.005 * 1.0, 0.0, 0.0, 0.0};
+        break;
+    case 6:
+        s = (DiskSpec){1.2, 1.3, 0.13, 0.005 * 1.2, 0.0, 0.0, 0.0};
+        break;
+    default:
+        return -1;
+    }
+    memset(plan, 0, sizeof(*plan));
+    plan->mass = s.mass;
+    plan->rd = s.rd;
+    plan->zh = s.zh;
+    plan->smbh = s.smbh;
+    plan->gas_frac = s.gas_frac;
+    plan->bulge_mass = s.bulge_mass;
+    plan->bulge_a = s.bulge_a;
+    plan->seed = r.s;
+    return 0;
+}
+
 int csg_generate_ics_impl(int kind, int n, uint64_t seed, Body *out)
 {
     if (n < 0 || (n > 0 && !out))
@@ -473,4 +513,15 @@ int csg_generate_ics_impl(int kind, int n, uint64_t seed, Body *out)
 CSG_EXPORT int csg_generate_ics(int kind, int n, uint64_t seed, Body *out)
 {
     return csg_generate_ics_impl(kind, n, seed, out);
+}
+
+CSG_EXPORT int csg_generate_ics_device(int kind, int n, uint64_t seed, Body *device_out,
+                                       void *stream)
+{
+    csgd_disk_plan p;
+    if (n < 0 || (n > 0 && !device_out) || csg_disk_plan(kind, seed, &p))
+        return -1;
+    if (n == 0)
+        return 0;
+    return csgd_generate_disks(stream, &p, &n, 1, device_out) ? -1 : n;
 }

@@ -72,6 +72,9 @@ _SIGS = {
     "cosmosim_set_bodies": ([_vp, _vp, _i], _i),
     "cosmosim_snapshot_f32": ([_vp, _i, _vp, _i, _i], _i),
     "cosmosim_compact": ([_vp], _i),
+    "csg_generate_ics_device": ([_i, _i, ctypes.c_uint64, _vp, _vp], _i),
+    "cosmosim_create_ensemble_ics": ([_i, _i, _ip, ctypes.c_uint64, ctypes.POINTER(CsgSimParams)],
+                                     _vp),
     "csg_quasar_step": ([_vp, _ip, _i, _vp, _d], None),
     "csg_quasar_seed": ([ctypes.c_uint64, _i], None),
     "csg_quasar_default_config": ([], QuasarConfig),
@@ -276,6 +279,18 @@ class Sim:
         p = CsgSimParams(G, softening, theta, dt, substeps, 0, precision)
         return cls(lib.cosmosim_create_ensemble(ptr(bodies), len(bodies), len(c),
                                                 c.ctypes.data_as(_ip), ctypes.byref(p)))
+
+    @classmethod
+    def ensemble_ics(cls, kind, counts, seed0, G=1.0, softening=0.01, theta=0.5, dt=1e-3,
+                     substeps=1, precision=PREC_FP64):
+        """Ensemble whose systems are generated on the GPU
+        (cosmosim_create_ensemble_ics): system g = csg_generate_ics(kind,
+        counts[g], seed0 + g)."""
+        lib = load()
+        c = np.ascontiguousarray(counts, dtype=np.int32)
+        p = CsgSimParams(G, softening, theta, dt, substeps, 0, precision)
+        return cls(lib.cosmosim_create_ensemble_ics(kind, len(c), c.ctypes.data_as(_ip), seed0,
+                                                    ctypes.byref(p)))
 
     @property
     def system_count(self):

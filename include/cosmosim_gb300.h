@@ -288,6 +288,20 @@ CSG_EXPORT void csg_octree_compute_forces_exact(const OctreeNode *pool, int root
    Returns the number of bodies written (n). */
 CSG_EXPORT int csg_generate_ics(int kind, int n, uint64_t seed, Body *out);
 
+/* The same initial conditions generated on the GPU into a device Body array
+   (kinds 0, 3, 5 and 6: the single exponential disks). Each body draws the
+   same random numbers as on the host (the generator is jumped ahead per run
+   of bodies); log/exp/sin/cos are CUDA's, so positions and velocities agree
+   to a few ulp, masses and types exactly. Returns n, or -1. Blocking. */
+CSG_EXPORT int csg_generate_ics_device(int kind, int n, uint64_t seed, Body *device_out,
+                                       void *stream);
+
+/* An ensemble handle whose systems are generated on the GPU: system g has
+   counts[g] bodies of csg_generate_ics kind `kind` (0, 3, 5 or 6) with seed
+   seed0 + g. Otherwise as cosmosim_create_ensemble. */
+CSG_EXPORT SimHandle cosmosim_create_ensemble_ics(int kind, int n_sys, const int *counts,
+                                                  uint64_t seed0, const CsgSimParams *params);
+
 #ifdef __cplusplus
 }
 #endif
