@@ -51,6 +51,11 @@ CONFIGS = {
 ENSEMBLE = dict(n_gal=64, n_min=2000, n_max=50000, size_seed=12, theta=0.5, eps=0.01, dt=1e-3,
                 desc="64 independent exp.-disk galaxies, N log-uniform [2000, 50000], one handle")
 FLOP_PER_INTERACTION = 20  # monopole body-cell interaction: 3 sub, 3 fma d2, rsqrt, 3 mul, 3 fma acc
+# DRAM bytes per body of one k_walk32 launch, from the ncu capture of the
+# 100k merger (profiles/k_walk32_merger100k_fp32.md: 10.06 MB read, 0 written
+# for 100,000 bodies): the first touch of the tree and the bodies; the tree
+# stays in L2 during the walk. Other workloads scale it by the body count.
+WALK32_DRAM_BYTES_PER_BODY = 10.06e6 / 100_000
 SEED = 0x5EED0000
 
 
@@ -427,7 +432,7 @@ def ensemble_line(args, torch, lib, rank, world, fp32_peak):
         "interactions_per_substep": f32["interactions"],
         "roofline": {"bound": "fp32-pipe", "kernel": "k_walk32 (gravity walk, all systems)",
                      "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp32_peak, "traffic": None},
+                     "frac": achieved / fp32_peak, "traffic": WALK32_DRAM_BYTES_PER_BODY * n},
         "errors": r["errors"],
         "e2e": {"value": n * r["e2e_steps"] * world / times[1], "unit": UNIT,
                 "api": "cosmosim_set_bodies + cosmosim_substeps_async(1) + cosmosim_copy_bodies "
@@ -803,10 +808,13 @@ def main():
                            "interactions_per_lane_step": f32["interactions"] / max(32 * f32["warp_steps"], 1)},
         "roofline": {"bound": "fp32-pipe", "kernel": "k_walk32 (gravity walk)",
                      "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp32_peak, "traffic": None,
+                     "frac": achieved / fp32_peak,
+                     "traffic": WALK32_DRAM_BYTES_PER_BODY * cfg["n"],
                      "note": "20 flop per reference interaction / walk event time; peak = FP32 "
                              "FMA throughput measured live by csg_measure_fp_peaks (the walk is "
-                             "CUDA-core bound: no dense contraction, tree resident in L2)"},
+                             "CUDA-core bound: no dense contraction, tree resident in L2); "
+                             "traffic = DRAM bytes per launch from the ncu capture of the 100k "
+                             "merger scaled by the body count"},
         "errors": r["errors"],
         "e2e": {"value": e2e_value, "unit": UNIT, "api": "integrator_step (pinned host Body[])",
                 "steps": r["e2e_steps"], "h2d_bytes_per_step": 168 * cfg["n"],
