@@ -124,9 +124,13 @@ int csgd_gravity_ex(csgd_t *d, const csgd_force_params *p, int exact);
 int csgd_walk_lists(csgd_t *d, const csgd_force_params *p, int *counts, const int *offs,
                     int *ids, int cap, int fill);
 
-/* SPH on the current tree (needs geometry). */
+/* SPH on the current tree (needs geometry). csgd_sph_forces =
+   csgd_sph_force_terms (pair terms; touches no acceleration) then
+   csgd_sph_force_sums (adds them to the accelerations). */
 int csgd_sph_density(csgd_t *d);
 int csgd_sph_forces(csgd_t *d);
+int csgd_sph_force_terms(csgd_t *d);
+int csgd_sph_force_sums(csgd_t *d);
 int csgd_sph_cooling(csgd_t *d, double dt);
 
 /* Leapfrog pieces: v += a*dt/2 and x += v*dt; and v += a*dt/2. */

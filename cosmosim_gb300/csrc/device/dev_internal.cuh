@@ -115,6 +115,8 @@ struct QuasarState {
 struct csgd {
     cudaStream_t stream;
     cudaStream_t own_stream;
+    cudaStream_t aux;             // SPH runs here beside the gravity walk
+    cudaEvent_t ev_fork, ev_join; // (timing disabled)
     int n;        // bodies in use
     int cap;      // body capacity
     int node_cap; // node capacity (8*cap + 64)

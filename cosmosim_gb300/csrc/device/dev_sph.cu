@@ -548,7 +548,7 @@ static int ensure_lists(csgd_t *d)
     return CSG_OK;
 }
 
-static int sph_pass(csgd_t *d, int forces)
+static int sph_pass(csgd_t *d, int forces, bool sums = true)
 {
     if (d->n_gal > 1) { // one system only (see csgd_set_systems)
         csgd_set_err(d, CSG_ERR_UNSUPPORTED);
@@ -578,7 +578,8 @@ static int sph_pass(csgd_t *d, int forces)
     if (forces) {
         { k_sph_body_terms<<<g, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
         { k_sph_force_terms<<<gp, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
-        { k_sph_force_sums<<<g, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
+        if (sums)
+            { k_sph_force_sums<<<g, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
     } else {
         { k_sph_density_terms<<<gp, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
         { k_sph_density_sums<<<g, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
@@ -591,6 +592,17 @@ extern "C" int csgd_sph_density(csgd_t *d) { return sph_pass(d, 0); }
 extern "C" int csgd_prepare_sph(csgd_t *d) { return ensure_lists(d); }
 
 extern "C" int csgd_sph_forces(csgd_t *d) { return sph_pass(d, 1); }
+
+extern "C" int csgd_sph_force_terms(csgd_t *d) { return sph_pass(d, 1, false); }
+
+extern "C" int csgd_sph_force_sums(csgd_t *d)
+{
+    if (d->n <= 0)
+        return CSG_OK;
+    SphArgs a = make_args(d);
+    { k_sph_force_sums<<<csgd_grid(d->n, SPH_THREADS), SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
+    return csgd_check(d, cudaGetLastError());
+}
 
 extern "C" int csgd_find_neighbors(csgd_t *d, double cx, double cy, double cz, double radius,
                                    int *buf, int cap, int *count_out)

@@ -242,6 +242,17 @@ extern "C" csgd_t *csgd_create(void)
         return nullptr;
     }
     d->stream = d->own_stream;
+    if (cudaStreamCreateWithFlags(&d->aux, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&d->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&d->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError(); // no overlap then: SPH runs on the main stream
+        if (d->aux)
+            cudaStreamDestroy(d->aux);
+        if (d->ev_fork)
+            cudaEventDestroy(d->ev_fork);
+        d->aux = nullptr;
+        d->ev_fork = d->ev_join = nullptr;
+    }
     d->use_graphs = 1;
     d->n_gal = 1;
     d->walk_warps = 8;
@@ -302,6 +313,12 @@ extern "C" void csgd_destroy(csgd_t *d)
         cudaFreeHost(d->h_int);
     if (d->qs)
         cudaFree(d->qs);
+    if (d->aux) {
+        cudaStreamSynchronize(d->aux);
+        cudaStreamDestroy(d->aux);
+        cudaEventDestroy(d->ev_fork);
+        cudaEventDestroy(d->ev_join);
+    }
     if (d->own_stream)
         cudaStreamDestroy(d->own_stream);
     free(d);
@@ -600,17 +617,40 @@ extern "C" int csgd_sph_cooling(csgd_t *d, double dt)
     return csgd_check(d, cudaGetLastError());
 }
 
+// With SPH, the gravity walk and the SPH passes up to the force terms are
+// independent (the walk writes the accelerations; SPH writes density,
+// pressure, smoothing lengths and its pair terms), so they run on two streams
+// and the force sums, which add to the accelerations, wait for both. In a
+// captured substep the fork and join become graph edges.
 extern "C" int csgd_substep(csgd_t *d, double dt, const csgd_force_params *p, int sph)
 {
     int rc = csgd_kick_drift(d, dt);
     if (!rc)
         rc = csgd_build_tree(d, sph);
-    if (!rc)
-        rc = csgd_gravity(d, p);
-    if (!rc && sph) {
+    if (!rc && sph && d->aux && d->n_gal == 1) {
+        const cudaStream_t main = d->stream;
+        cudaEventRecord(d->ev_fork, main);
+        cudaStreamWaitEvent(d->aux, d->ev_fork, 0);
+        d->stream = d->aux;
         rc = csgd_sph_density(d);
         if (!rc)
-            rc = csgd_sph_forces(d);
+            rc = csgd_sph_force_terms(d);
+        d->stream = main;
+        cudaEventRecord(d->ev_join, d->aux);
+        const int rg = csgd_gravity(d, p);
+        cudaStreamWaitEvent(main, d->ev_join, 0); // always rejoin (a capture needs it)
+        if (!rc)
+            rc = rg;
+        if (!rc)
+            rc = csgd_sph_force_sums(d);
+    } else {
+        if (!rc)
+            rc = csgd_gravity(d, p);
+        if (!rc && sph) {
+            rc = csgd_sph_density(d);
+            if (!rc)
+                rc = csgd_sph_forces(d);
+        }
     }
     if (!rc)
         rc = csgd_kick(d, dt);
