@@ -65,7 +65,7 @@ CSG_EXPORT const char *csg_error_string(int code);
 CSG_EXPORT void csg_set_precision(int precision);
 
 /* Status of the handle's last call; 0 = success. The reference API has no
-   error channel; this is the additive one its survey asks for. */
+   error channel; this is an additive one. */
 CSG_EXPORT int cosmosim_last_error(SimHandle handle);
 
 /* Run-time physics parameters for a handle. */

@@ -2,7 +2,7 @@
  * orc.h — CPU oracle for the gravity/SPH hot path.
  *
  * TEST INFRASTRUCTURE ONLY. This is a plain-C (C11 + OpenMP) restatement of
- * cosmosim's double-precision CPU algorithm, used as the checker for the CUDA
+ * cosmosim's double-precision CPU algorithm, used as the oracle for the CUDA
  * path and as the timed CPU baseline. Only tests/, __graft_entry__.smoke() and
  * bench.py (its cpu_baseline leg and its --impl reference arm) may load it.
  * The product library never links or calls it.
