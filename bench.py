@@ -59,6 +59,19 @@ WALK32_DRAM_BYTES_PER_BODY = 10.06e6 / 100_000
 SEED = 0x5EED0000
 
 
+def max_over_ranks(torch, values, device):
+    """Each value's maximum over the ranks: a job's time is its slowest rank's."""
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return t.tolist()
+
+
+def job_rate(units_per_rank, world, secs_max):
+    """Whole-job throughput: every rank's units over the slowest rank's time
+    (replicas: each rank runs its own independent system)."""
+    return units_per_rank * world / secs_max
+
+
 def dist_env():
     return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
             int(os.environ.get("LOCAL_RANK", 0)))
@@ -397,15 +410,13 @@ def ensemble_line(args, torch, lib, rank, world, fp32_peak):
     runs = r["runs"]
     times = [runs["fp32"]["secs"], r["e2e_s"]]
     if world > 1:
-        t = torch.tensor(times, device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        times = t.tolist()
+        times = max_over_ranks(torch, times, "cuda")
     n = r["n_total"]
 
     def rate(run):
         return n * run["steps"] / run["secs"]
 
-    value = n * runs["fp32"]["steps"] * world / times[0]
+    value = job_rate(n * runs["fp32"]["steps"], world, times[0])
     f32 = runs["fp32"]
     achieved = FLOP_PER_INTERACTION * f32["interactions"] / f32["walk_s"] / 1e12
     e = ENSEMBLE
@@ -434,7 +445,7 @@ def ensemble_line(args, torch, lib, rank, world, fp32_peak):
                      "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak, "traffic": WALK32_DRAM_BYTES_PER_BODY * n},
         "errors": r["errors"],
-        "e2e": {"value": n * r["e2e_steps"] * world / times[1], "unit": UNIT,
+        "e2e": {"value": job_rate(n * r["e2e_steps"], world, times[1]), "unit": UNIT,
                 "api": "cosmosim_set_bodies + cosmosim_substeps_async(1) + cosmosim_copy_bodies "
                        "(pinned host Body[])",
                 "steps": r["e2e_steps"], "h2d_bytes_per_step": 168 * n,
@@ -779,14 +790,10 @@ def main():
     # whole-job aggregation: max time over ranks
     t32, t64, te = f32["secs"], f64["secs"], r["e2e_s"]
     if world > 1:
-        t = torch.tensor([t32, t64, te], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t32, t64, te = t.tolist()
-    work32 = r["n_alive"] * f32["steps"] * world
-    work64 = r["n_alive"] * f64["steps"] * world
-    value = work32 / t32
-    v64 = work64 / t64
-    e2e_value = r["n_alive"] * r["e2e_steps"] * world / te
+        t32, t64, te = max_over_ranks(torch, [t32, t64, te], "cuda")
+    value = job_rate(r["n_alive"] * f32["steps"], world, t32)
+    v64 = job_rate(r["n_alive"] * f64["steps"], world, t64)
+    e2e_value = job_rate(r["n_alive"] * r["e2e_steps"], world, te)
     achieved = FLOP_PER_INTERACTION * f32["interactions"] / f32["walk_s"] / 1e12
     achieved64 = FLOP_PER_INTERACTION * f64["interactions"] / f64["walk_s"] / 1e12
     line = {
