@@ -425,7 +425,7 @@ def ensemble_line(args, torch, lib, rank, world, fp32_peak):
         "unit": UNIT, "n_gpus": world, "steps": f32["steps"], "warmup": args.warmup,
         "ms_per_step": 1e3 * f32["secs"] / f32["steps"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 pair forces / f64 positions, tree moments, drift", "data": "synthetic",
+        "dtype": "f32", "precision": "FP32 pair forces (compensated sums); FP64 positions, tree moments, drift", "data": "synthetic",
         "config": {"workload": f"ensemble64: {e['desc']}", "n_bodies": n, "n_systems": e["n_gal"],
                    "sizes_min_max": [int(min(r["sizes"])), int(max(r["sizes"]))],
                    "theta": e["theta"], "softening": e["eps"], "dt": e["dt"], "sph": False,
@@ -800,7 +800,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": f32["steps"],
         "warmup": args.warmup, "ms_per_step": 1e3 * f32["secs"] / f32["steps"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 pair forces / f64 positions, tree moments, drift", "data": "synthetic",
+        "dtype": "f32", "precision": "FP32 pair forces (compensated sums); FP64 positions, tree moments, drift", "data": "synthetic",
         "config": config,
         "fp64_plain": {"value": v64, "ms_per_step": 1e3 * f64["secs"] / f64["steps"],
                        "steps": f64["steps"], "fp32_mixed_speedup": value / v64,
