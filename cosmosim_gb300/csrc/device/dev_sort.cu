@@ -73,10 +73,11 @@ __global__ void k_scan_tile(const int *__restrict__ in, int *__restrict__ out, i
         sums[blockIdx.x] = run;
 }
 
-// Exclusive scan of up to SCAN_SMALL items by one block: each thread sums a
-// contiguous chunk, the block scans the chunk sums, each thread rescans its
-// chunk. One launch instead of the tile/recursion/add/total sequence for the
-// small scans a substep does; writes out[n] = total.
+// Exclusive scan of up to SCAN_SMALL items by one block, which walks the input
+// in 4096-item tiles (each warp reads 128 consecutive items) and carries the
+// running total from tile to tile. One launch instead of the
+// tile/recursion/add/total sequence for the small scans a substep does;
+// writes out[n] = total.
 constexpr int SCAN_SMALL = 16 * SCAN_TILE;
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_small(const int *__restrict__ in,
@@ -84,33 +85,45 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_small(const int *__restri
                                                              const int *__restrict__ limit)
 {
     __shared__ int warp_tot[SCAN_THREADS / 32];
-    __shared__ int total_s;
+    __shared__ int tile_tot;
     const int lim = limit ? min(n, *limit) : n;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int chunk = (n + SCAN_THREADS - 1) / SCAN_THREADS;
-    const int b0 = min(n, threadIdx.x * chunk), b1 = min(n, b0 + chunk);
-    int local = 0;
-    for (int i = b0; i < b1; i++)
-        local += (i < lim) ? in[i] : 0;
-    const int incl = warp_incl_scan(local);
-    if (lane == 31)
-        warp_tot[warp] = incl;
-    __syncthreads();
-    if (warp == 0) {
-        const int t = warp_tot[lane];
-        const int ti = warp_incl_scan(t);
-        warp_tot[lane] = ti - t;
+    int carry = 0;
+    for (int t0 = 0; t0 < n; t0 += SCAN_TILE) {
+        const int base = t0 + threadIdx.x * SCAN_ITEMS;
+        int v[SCAN_ITEMS];
+        int local = 0;
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; k++) {
+            const int i = base + k;
+            v[k] = (i < lim) ? in[i] : 0;
+            local += v[k];
+        }
+        const int incl = warp_incl_scan(local);
         if (lane == 31)
-            total_s = ti;
-    }
-    __syncthreads();
-    int run = warp_tot[warp] + incl - local;
-    for (int i = b0; i < b1; i++) {
-        out[i] = run;
-        run += (i < lim) ? in[i] : 0;
+            warp_tot[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            const int t = warp_tot[lane];
+            const int ti = warp_incl_scan(t);
+            warp_tot[lane] = ti - t;
+            if (lane == 31)
+                tile_tot = ti;
+        }
+        __syncthreads();
+        int run = carry + warp_tot[warp] + incl - local;
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; k++) {
+            const int i = base + k;
+            if (i < n)
+                out[i] = run;
+            run += v[k];
+        }
+        carry += tile_tot;
+        __syncthreads(); // warp_tot and tile_tot are rewritten by the next tile
     }
     if (threadIdx.x == 0)
-        out[n] = total_s;
+        out[n] = carry;
 }
 
 __global__ void k_scan_add(int *__restrict__ out, int n, const int *__restrict__ offs)
