@@ -126,10 +126,14 @@ int csgd_walk_lists(csgd_t *d, const csgd_force_params *p, int *counts, const in
 
 /* SPH on the current tree (needs geometry). csgd_sph_forces =
    csgd_sph_force_terms (pair terms; touches no acceleration) then
-   csgd_sph_force_sums (adds them to the accelerations). */
+   csgd_sph_force_sums (adds them to the accelerations). reuse_lists = 1 is
+   for a force pass right after csgd_sph_density on the same tree and bodies:
+   only the gas bodies whose smoothing length that pass changed search the
+   tree again; the others keep the density pass's list, which is the list a
+   new search would find (same tree, position and radius). */
 int csgd_sph_density(csgd_t *d);
-int csgd_sph_forces(csgd_t *d);
-int csgd_sph_force_terms(csgd_t *d);
+int csgd_sph_forces(csgd_t *d, int reuse_lists);
+int csgd_sph_force_terms(csgd_t *d, int reuse_lists);
 int csgd_sph_force_sums(csgd_t *d);
 int csgd_sph_cooling(csgd_t *d, double dt);
 

@@ -164,6 +164,7 @@ struct csgd {
     int *nb_count;
     double *pr2, *cs; // SPH per-body force terms
     double *sph_term; // SPH pair terms, 3 x 128 x cap (slot-major)
+    int *sph_relist;  // per gas slot: 1 when the density pass changed h
     int nb_cap;
 
     // nodes

@@ -65,6 +65,8 @@ struct SphArgs {
     DevScalars *sc;
     int *nb;       // neighbour lists, slot-major
     int *nb_count; // neighbours per gas body
+    int *relist;   // per gas body: the density pass changed h (search again)
+    int reuse;     // force pass: keep the density lists of bodies with relist 0
     double *pr2, *cs; // per-body force terms (k_sph_body_terms)
     double *term;     // pair terms, 3 planes of 128 slots x stride (slot-major)
     int n, node_cap, stride;
@@ -213,7 +215,8 @@ __global__ void __launch_bounds__(SPH_THREADS) k_sph_lists(SphArgs a)
     const int nwarps = (int)((gridDim.x * (long long)SPH_THREADS) >> 5);
     for (int k = (int)(((long long)blockIdx.x * SPH_THREADS + threadIdx.x) >> 5); k < n_gas;
          k += nwarps) // warp-uniform
-        list_one(a, k, lane);
+        if (!a.reuse || a.relist[k])
+            list_one(a, k, lane);
 }
 
 // Pair kernels. Each pass runs in two kernels so that the FP64 pair
@@ -264,10 +267,14 @@ __global__ void __launch_bounds__(SPH_THREADS) k_sph_density_sums(SphArgs a)
     double rho = 0.0;
     for (int s = 0; s < nn; s++)
         rho += a.term[stride * s + k];
+    int relist = 1;
     if (nn < 20 && h < 50.0)
         a.h[i] = h * 1.2;
     else if (nn > 48 && h > 0.1)
         a.h[i] = h * 0.8;
+    else
+        relist = 0;
+    a.relist[k] = relist;
     if (rho < 1e-15 || isnan(rho))
         rho = 1e-15;
     a.rho[i] = rho;
@@ -457,6 +464,8 @@ SphArgs make_args(csgd_t *d)
     a.sc = d->sc;
     a.nb = d->nb;
     a.nb_count = d->nb_count;
+    a.relist = d->sph_relist;
+    a.reuse = 0;
     a.pr2 = d->pr2;
     a.cs = d->cs;
     a.term = d->sph_term;
@@ -530,12 +539,15 @@ static int ensure_lists(csgd_t *d)
         cudaFree(d->cs);
     if (d->sph_term)
         cudaFree(d->sph_term);
+    if (d->sph_relist)
+        cudaFree(d->sph_relist);
     d->nb = nullptr;
-    d->nb_count = nullptr;
+    d->nb_count = d->sph_relist = nullptr;
     d->pr2 = d->cs = d->sph_term = nullptr;
     size_t c = (size_t)(d->cap > 0 ? d->cap : 1);
     if (cudaMalloc((void **)&d->nb, sizeof(int) * CSG_SPH_MAX_NEIGHBORS * c) != cudaSuccess ||
         cudaMalloc((void **)&d->nb_count, sizeof(int) * c) != cudaSuccess ||
+        cudaMalloc((void **)&d->sph_relist, sizeof(int) * c) != cudaSuccess ||
         cudaMalloc((void **)&d->pr2, sizeof(double) * c) != cudaSuccess ||
         cudaMalloc((void **)&d->cs, sizeof(double) * c) != cudaSuccess ||
         cudaMalloc((void **)&d->sph_term, sizeof(double) * 3 * CSG_SPH_MAX_NEIGHBORS * c) !=
@@ -548,7 +560,7 @@ static int ensure_lists(csgd_t *d)
     return CSG_OK;
 }
 
-static int sph_pass(csgd_t *d, int forces, bool sums = true)
+static int sph_pass(csgd_t *d, int forces, bool sums = true, bool reuse = false)
 {
     if (d->n_gal > 1) { // one system only (see csgd_set_systems)
         csgd_set_err(d, CSG_ERR_UNSUPPORTED);
@@ -566,6 +578,7 @@ static int sph_pass(csgd_t *d, int forces, bool sums = true)
     if (rc)
         return rc;
     SphArgs a = make_args(d);
+    a.reuse = (forces && reuse) ? 1 : 0;
     const int g = csgd_grid(d->n, SPH_THREADS);
     // one warp per gas body for the lists, warps striding over the gas bodies
     int gl = csgd_grid((long long)d->n * CSG_WARP, SPH_THREADS);
@@ -591,9 +604,15 @@ extern "C" int csgd_sph_density(csgd_t *d) { return sph_pass(d, 0); }
 
 extern "C" int csgd_prepare_sph(csgd_t *d) { return ensure_lists(d); }
 
-extern "C" int csgd_sph_forces(csgd_t *d) { return sph_pass(d, 1); }
+extern "C" int csgd_sph_forces(csgd_t *d, int reuse_lists)
+{
+    return sph_pass(d, 1, true, reuse_lists != 0);
+}
 
-extern "C" int csgd_sph_force_terms(csgd_t *d) { return sph_pass(d, 1, false); }
+extern "C" int csgd_sph_force_terms(csgd_t *d, int reuse_lists)
+{
+    return sph_pass(d, 1, false, reuse_lists != 0);
+}
 
 extern "C" int csgd_sph_force_sums(csgd_t *d)
 {

@@ -303,6 +303,8 @@ extern "C" void csgd_destroy(csgd_t *d)
         cudaFree(d->cs);
     if (d->sph_term)
         cudaFree(d->sph_term);
+    if (d->sph_relist)
+        cudaFree(d->sph_relist);
     if (d->sc)
         cudaFree(d->sc);
     if (d->roots)
@@ -634,7 +636,7 @@ extern "C" int csgd_substep(csgd_t *d, double dt, const csgd_force_params *p, in
         d->stream = d->aux;
         rc = csgd_sph_density(d);
         if (!rc)
-            rc = csgd_sph_force_terms(d);
+            rc = csgd_sph_force_terms(d, 1);
         d->stream = main;
         cudaEventRecord(d->ev_join, d->aux);
         const int rg = csgd_gravity(d, p);
@@ -649,7 +651,7 @@ extern "C" int csgd_substep(csgd_t *d, double dt, const csgd_force_params *p, in
         if (!rc && sph) {
             rc = csgd_sph_density(d);
             if (!rc)
-                rc = csgd_sph_forces(d);
+                rc = csgd_sph_forces(d, 1);
         }
     }
     if (!rc)

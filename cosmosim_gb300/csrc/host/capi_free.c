@@ -189,7 +189,7 @@ static void sph_pass(Body *bodies, int n, const OctreeNode *tree, int which)
     }
     int rc = load_pool(d, tree, 0, bodies, n);
     if (!rc)
-        rc = which == 0 ? csgd_sph_density(d) : csgd_sph_forces(d);
+        rc = which == 0 ? csgd_sph_density(d) : csgd_sph_forces(d, 0);
     if (!rc)
         rc = csgd_download_bodies(d, bodies, n);
     if (!rc)
