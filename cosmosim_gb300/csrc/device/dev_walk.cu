@@ -38,7 +38,11 @@ struct WalkArgs {
     DevScalars *sc;
     double *ax, *ay, *az;
     double G, eps2, theta2, t2lo, t2hi;
-    float Gf, eps2f, theta2f, guard_abs, guard_rel;
+    float Gf, eps2f;
+    // FP32 opening test: accept when s^2 acc_k < d^2, open when s^2 opn_k > d^2
+    // (acc_k, opn_k = (1 +- g) / theta^2); in between, |theta^2 d^2 - s^2| is
+    // inside the FP32 error band g s^2 and the FP64 test decides
+    float acc_k, opn_k;
     int node_cap;
     int group; // 0: one warp per task; g > 0: take g tasks at a time from a counter
 };
@@ -380,10 +384,8 @@ __device__ __forceinline__ void walk_cells(const WalkArgs &a, NodeW32 *win, int 
             cur = c.next;
             continue;
         } else {
-            const float lhs = a.theta2f * d2;
-            const float band = c.B.w * a.guard_rel;
-            bool acc = (c.B.w < lhs - band) && d2 > 0.f;
-            const bool amb = active && !acc && !(c.B.w > lhs + band);
+            bool acc = c.B.w * a.acc_k < d2; // implies d2 > 0
+            const bool amb = active && !acc && !(c.B.w * a.opn_k > d2);
             if (amb) // rare
                 acc = decide64(a, cur, b.px, b.py, b.pz);
             take = active && acc;
@@ -475,10 +477,8 @@ __device__ __forceinline__ void walk32_task(const WalkArgs &a, NodeW32 *win, con
                         skip = c.next;
                 } else {
                     // |theta^2 d^2 - s^2| inside the FP32 error band -> decide in FP64
-                    const float lhs = a.theta2f * d2;
-                    const float band = c.s2 * a.guard_rel;
-                    acc = (c.s2 < lhs - band) && d2 > 0.f;
-                    const bool amb = active && !acc && !(c.s2 > lhs + band);
+                    acc = c.s2 * a.acc_k < d2; // implies d2 > 0
+                    const bool amb = active && !acc && !(c.s2 * a.opn_k > d2);
                     if (amb) // rare
                         acc = decide64(a, cur, px, py, pz);
                     open = active && !acc;
@@ -686,11 +686,13 @@ WalkArgs walk_args(csgd_t *d, const csgd_force_params *p)
     a.t2hi = a.theta2 * (1.0 + 0x1p-50);
     a.Gf = (float)p->G;
     a.eps2f = (float)a.eps2;
-    a.theta2f = (float)a.theta2;
     // FP32 error band: |d| is exact to ~2^-46 |coordinates| (hi/lo pairs), d^2
-    // to a few FP32 ulps; 2^-19 relative covers both with a wide margin.
-    a.guard_abs = 0.0f;
-    a.guard_rel = 0x1p-19f * (1.0f + a.theta2f);
+    // to a few FP32 ulps, each product below to 2^-23; g = 2^-19 (1 + theta^2)
+    // relative covers them with a wide margin. theta = 0 gives acc_k = opn_k =
+    // inf: nothing is accepted, every cell with d^2 > 0 opens.
+    const double g = 0x1p-19 * (1.0 + a.theta2);
+    a.acc_k = (float)((1.0 + g) / a.theta2);
+    a.opn_k = (float)((1.0 - g) / a.theta2);
     a.node_cap = d->node_cap;
     a.group = d->walk_group;
     return a;
