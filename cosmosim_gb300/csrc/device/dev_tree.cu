@@ -677,45 +677,19 @@ __device__ __forceinline__ void put_moments(const csgd_t &dd, int node, double s
     v[6] = (float)(sz - (double)hi.z);
 }
 
+// Cell moments. A cell with at most MOM_DIRECT bodies, and every leaf, sums
+// its sorted bodies directly (one thread per cell, no atomics); a larger cell
+// is formed from its children's moments by the last child to finish (a ticket
+// per cell), climbing from the directly summed cells whose parent is large.
+// A single-body leaf keeps the body's position exactly (the reference's leaf
+// centre); bodies that coincide to depth 64 share one leaf, in caller index
+// order, so the two smallest caller indices of a cell are its first two.
+constexpr int MOM_DIRECT = 32;
+
 template <bool EXPORT>
-__global__ void k_moments(csgd_t dd, DevScalars *sc, const double *__restrict__ x,
-                          const double *__restrict__ y, const double *__restrict__ z,
-                          const double *__restrict__ m, const int *__restrict__ perm,
-                          const int *__restrict__ leaf_of)
+__device__ __forceinline__ void moments_climb(const csgd_t &dd, int node, double sx, double sy,
+                                              double sz, double M, int2 mi)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= sc->n_alive || sc->n_nodes > dd.node_cap)
-        return;
-    const int id = leaf_of[p];
-    if (id < 0 || id >= dd.node_cap)
-        return;
-    NodeLink l = dd.link[id];
-    double M, sx, sy, sz;
-    int2 mi = make_int2(INT_MAX, INT_MAX);
-    if (l.count == 1) {
-        int b = perm[l.first];
-        M = m[b];
-        sx = x[b];
-        sy = y[b];
-        sz = z[b];
-        mi.x = b;
-    } else { // bodies that coincide to depth 64 share one leaf
-        M = 0.0;
-        double ax = 0.0, ay = 0.0, az = 0.0;
-        for (int k = 0; k < l.count; k++) {
-            int b = perm[l.first + k];
-            M += m[b];
-            ax += m[b] * x[b];
-            ay += m[b] * y[b];
-            az += m[b] * z[b];
-        }
-        const double inv = 1.0 / M;
-        sx = ax * inv;
-        sy = ay * inv;
-        sz = az * inv;
-        mi = make_int2(perm[l.first], perm[l.first + 1]);
-    }
-    int node = id;
     while (true) {
         put_moments(dd, node, sx, sy, sz, M);
         if (EXPORT)
@@ -765,6 +739,61 @@ __global__ void k_moments(csgd_t dd, DevScalars *sc, const double *__restrict__ 
         mi = make_int2(m1, m2);
         node = parent;
     }
+}
+
+template <bool EXPORT>
+__global__ void k_moments(csgd_t dd, DevScalars *sc, const double *__restrict__ x,
+                          const double *__restrict__ y, const double *__restrict__ z,
+                          const double *__restrict__ m, const int *__restrict__ perm)
+{
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nn = sc->n_nodes;
+    if (id >= nn || nn > dd.node_cap || sc->n_alive == 0)
+        return;
+    const NodeLink l = dd.link[id];
+    const bool leaf = dd.nchild[id] == 0;
+    if ((!leaf && l.count > MOM_DIRECT) || l.count < 1)
+        return; // formed by the climb (or a cell without bodies)
+    double M, sx, sy, sz;
+    int2 mi = make_int2(INT_MAX, INT_MAX);
+    if (l.count == 1) {
+        const int b = perm[l.first];
+        M = m[b];
+        sx = x[b];
+        sy = y[b];
+        sz = z[b];
+        mi.x = b;
+    } else {
+        M = 0.0;
+        double ax = 0.0, ay = 0.0, az = 0.0;
+        for (int k = 0; k < l.count; k++) {
+            const int b = perm[l.first + k];
+            const double mb = m[b];
+            M += mb;
+            ax += mb * x[b];
+            ay += mb * y[b];
+            az += mb * z[b];
+            if (EXPORT) {
+                if (b < mi.x) {
+                    mi.y = mi.x;
+                    mi.x = b;
+                } else if (b < mi.y) {
+                    mi.y = b;
+                }
+            }
+        }
+        const double inv = 1.0 / M;
+        sx = ax * inv;
+        sy = ay * inv;
+        sz = az * inv;
+    }
+    if (l.parent >= 0 && dd.link[l.parent].count <= MOM_DIRECT) {
+        put_moments(dd, id, sx, sy, sz, M); // the parent sums its own bodies
+        if (EXPORT)
+            dd.minidx[id] = mi;
+        return;
+    }
+    moments_climb<EXPORT>(dd, id, sx, sy, sz, M, mi);
 }
 
 // FP32 neighbour-search record of one cell (see NodeS32).
@@ -1103,9 +1132,9 @@ extern "C" int csgd_build_tree(csgd_t *d, int geometry)
     // nodes beyond n_nodes exit at once; the grid covers the capacity
     { k_link<<<gn, B, 0, s>>>(*d, sc, d->key, d->ext); d->launches++; }
     if (d->export_order)
-        { k_moments<true><<<g, B, 0, s>>>(*d, sc, d->x, d->y, d->z, d->m, d->perm, d->cnt); d->launches++; }
+        { k_moments<true><<<gn, B, 0, s>>>(*d, sc, d->x, d->y, d->z, d->m, d->perm); d->launches++; }
     else
-        { k_moments<false><<<g, B, 0, s>>>(*d, sc, d->x, d->y, d->z, d->m, d->perm, d->cnt); d->launches++; }
+        { k_moments<false><<<gn, B, 0, s>>>(*d, sc, d->x, d->y, d->z, d->m, d->perm); d->launches++; }
     d->minidx_valid = d->export_order;
     { k_tasks<<<min(d->n_gal, 152), 256, 0, s>>>(sc, d->roots, d->n_gal, d->base, d->tasks, d->task_cap, 0); d->launches++; }
     d->geometry_valid = 0;
