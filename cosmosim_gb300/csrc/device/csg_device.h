@@ -45,6 +45,11 @@ void csgd_set_export_order(csgd_t *d, int on);
 
 /* Makes room for n bodies (grow-only). */
 int csgd_reserve(csgd_t *d, int n);
+
+/* The build's key sort on host keys (csg_sort_keys, cosmosim_gb300.h); uses
+   the state's key buffers. */
+int csgd_sort_keys(csgd_t *d, const unsigned long long *keys, int n, int bits,
+                   unsigned long long *out_keys, int *out_index);
 int csgd_count(const csgd_t *d);
 
 /* Forest: the n bodies form n_sys independent systems, system g holding the

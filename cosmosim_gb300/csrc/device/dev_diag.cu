@@ -193,7 +193,6 @@ extern "C" int csgd_direct_forces(csgd_t *d, const int *host_idx, int ns, double
     if (ns <= 0)
         return CSG_OK;
     if (ns > d->n) {
-        csgd_set_err(d, CSG_ERR_BAD_ARG);
         return CSG_ERR_BAD_ARG;
     }
     int *didx = nullptr;

@@ -81,7 +81,6 @@ extern "C" int csgd_snapshot_f32(csgd_t *d, int format, float *out, int out_is_d
     *count_out = 0;
     if ((format != CSG_SNAPSHOT_UE && format != CSG_SNAPSHOT_RENDER) || max_bodies < 0 ||
         (max_bodies > 0 && !out)) {
-        csgd_set_err(d, CSG_ERR_BAD_ARG);
         return CSG_ERR_BAD_ARG;
     }
     const int n = d->n;
@@ -127,7 +126,6 @@ extern "C" int csgd_compact(csgd_t *d, int *new_n)
     const int n = d->n;
     *new_n = n;
     if (d->n_gal > 1) { // the system layout would no longer match
-        csgd_set_err(d, CSG_ERR_UNSUPPORTED);
         return CSG_ERR_UNSUPPORTED;
     }
     if (n <= 0)

@@ -139,42 +139,102 @@ __global__ void k_scan_total(int *__restrict__ out, int n, const int *__restrict
 }
 
 // ---- radix sort kernels ----
+//
+// LSD radix sort, 8 bits per pass, in the single-pass form with decoupled
+// look-back (Merrill & Garland, "Single-pass Parallel Prefix Scan with
+// Decoupled Look-back", 2016; applied to radix sorting as "Onesweep", Adinets
+// & Merrill 2022): one kernel counts the digits of every pass in one read of
+// the keys; then each pass is one kernel. A block takes the next tile index
+// from a counter (so every earlier tile belongs to a block that is already
+// running), counts its tile's digits, publishes them, and sums the published
+// counts of the tiles before it, walking back until a tile that has
+// published its inclusive prefix. With the global digit offsets that gives
+// every key its place; within a tile keys keep their input order (stable).
 
-template <int IPL>
-__global__ void k_radix_hist(const unsigned long long *__restrict__ key, int n, int shift,
-                             unsigned int *__restrict__ hist, int nblocks)
+constexpr unsigned long long LB_AGG = 1ull << 62; // tile count published
+constexpr unsigned long long LB_PRE = 1ull << 63; // inclusive prefix published
+constexpr unsigned long long LB_VAL = LB_AGG - 1;
+constexpr int LB_SPIN_LIMIT = 1 << 22; // polls of one status word before giving up
+
+// layout of the sort scratch (32-bit words): digit counts [8][256], tile
+// counters [8], padding to an 8-byte boundary, then two status buffers of
+// 64-bit words, [tile][256] each (pass p uses buffer p % 2)
+constexpr int SORT_COUNTS = 0;
+constexpr int SORT_TILE_CTR = 8 * RADIX;
+constexpr int SORT_STATUS = 8 * RADIX + 64;
+
+__device__ __forceinline__ void lb_store(unsigned long long *p, unsigned long long v)
 {
-    __shared__ unsigned int h[RADIX];
-    for (int i = threadIdx.x; i < RADIX; i += blockDim.x)
-        h[i] = 0;
-    __syncthreads();
-    const long long t0 = (long long)blockIdx.x * sort_tile(IPL);
-    for (int k = threadIdx.x; k < sort_tile(IPL); k += blockDim.x) {
-        long long i = t0 + k;
-        if (i < n)
-            atomicAdd(&h[(unsigned)(key[i] >> shift) & (RADIX - 1)], 1u);
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < RADIX; i += blockDim.x)
-        hist[(size_t)i * nblocks + blockIdx.x] = h[i];
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-template <int IPL>
-__global__ void k_radix_scatter(const unsigned long long *__restrict__ key_in,
-                                const int *__restrict__ val_in,
-                                unsigned long long *__restrict__ key_out,
-                                int *__restrict__ val_out, int n, int shift,
-                                const int *__restrict__ offs, int nblocks)
+__device__ __forceinline__ unsigned long long lb_load(const unsigned long long *p)
 {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Digit counts of passes 0..passes-1 (counts[pass][digit], zeroed before).
+__global__ void __launch_bounds__(SORT_THREADS) k_radix_counts(const unsigned long long *__restrict__ key,
+                                                               int n, int passes,
+                                                               unsigned int *__restrict__ counts)
+{
+    __shared__ unsigned int h[8][RADIX];
+    for (int i = threadIdx.x; i < 8 * RADIX; i += blockDim.x)
+        (&h[0][0])[i] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    // warp-uniform trip count: every lane takes part in the match below
+    for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n;
+         base += stride) {
+        const long long i = base + lane;
+        const unsigned long long k = (i < n) ? key[i] : 0ull;
+        for (int p = 0; p < passes; p++) {
+            const int dg = (i < n) ? (int)((k >> (8 * p)) & (RADIX - 1)) : RADIX;
+            const unsigned peers = __match_any_sync(0xffffffffu, dg);
+            if (dg < RADIX && (peers & lt) == 0)
+                atomicAdd(&h[p][dg], (unsigned)__popc(peers));
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < passes * RADIX; i += blockDim.x) {
+        const unsigned c = (&h[0][0])[i];
+        if (c)
+            atomicAdd(&counts[i], c);
+    }
+}
+
+// One pass: keys/values of a tile to their places. counts: this pass's 256
+// digit counts; status / status_next: this pass's and the next pass's status
+// buffers (this pass clears its tile's entries of the next one).
+template <int IPL>
+__global__ void __launch_bounds__(SORT_THREADS) k_radix_onesweep(
+    const unsigned long long *__restrict__ key_in, const int *__restrict__ val_in,
+    unsigned long long *__restrict__ key_out, int *__restrict__ val_out, int n, int shift,
+    const unsigned int *__restrict__ counts, int *__restrict__ tile_ctr,
+    unsigned long long *status, unsigned long long *__restrict__ status_next, int nblocks,
+    DevScalars *sc)
+{
+    static_assert(SORT_THREADS == RADIX, "one digit per thread");
     __shared__ int wcount[SORT_WARPS][RADIX];
+    __shared__ int warp_tot[SORT_WARPS];
+    __shared__ int sh_tile;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0)
+        sh_tile = atomicAdd(tile_ctr, 1);
     for (int i = threadIdx.x; i < SORT_WARPS * RADIX; i += blockDim.x)
         (&wcount[0][0])[i] = 0;
     __syncthreads();
-    const long long w0 =
-        (long long)blockIdx.x * sort_tile(IPL) + (long long)warp * (CSG_WARP * IPL);
+    const int tile = sh_tile;
+    if (tile >= nblocks) // more blocks than tiles cannot happen (grid = nblocks)
+        return;
+    status_next[(size_t)tile * RADIX + threadIdx.x] = 0ull;
+    const long long w0 = (long long)tile * sort_tile(IPL) + (long long)warp * (CSG_WARP * IPL);
     const unsigned lt = (1u << lane) - 1u;
-    // pass 1: per-warp digit counts
+    // per-warp digit counts
     for (int c = 0; c < IPL; c++) {
         long long i = w0 + c * CSG_WARP + lane;
         int dg = (i < n) ? (int)((key_in[i] >> shift) & (RADIX - 1)) : RADIX;
@@ -184,37 +244,69 @@ __global__ void k_radix_scatter(const unsigned long long *__restrict__ key_in,
         __syncwarp();
     }
     __syncthreads();
-    // per digit: tile offset + counts of earlier warps
-    for (int dg = threadIdx.x; dg < RADIX; dg += blockDim.x) {
-        int run = offs[(size_t)dg * nblocks + blockIdx.x];
-        for (int w = 0; w < SORT_WARPS; w++) {
-            int c = wcount[w][dg];
-            wcount[w][dg] = run;
-            run += c;
+    const int dg = threadIdx.x;
+    int tot = 0;
+    for (int w = 0; w < SORT_WARPS; w++)
+        tot += wcount[w][dg];
+    unsigned long long *mine = status + (size_t)tile * RADIX + dg;
+    lb_store(mine, (tile == 0 ? LB_PRE : LB_AGG) | (unsigned long long)tot);
+    // global exclusive offset of the digit: block scan of the pass's counts
+    const int c = (int)counts[dg];
+    const int incl = warp_incl_scan(c);
+    if (lane == 31)
+        warp_tot[warp] = incl;
+    __syncthreads();
+    int gex = incl - c;
+    for (int w = 0; w < warp; w++)
+        gex += warp_tot[w];
+    // keys of this digit in earlier tiles
+    long long excl = 0;
+    if (tile > 0) {
+        for (int j = tile - 1; j >= 0; j--) {
+            const unsigned long long *q = status + (size_t)j * RADIX + dg;
+            unsigned long long v = lb_load(q);
+            int spins = 0;
+            while (!(v & (LB_AGG | LB_PRE)) && ++spins < LB_SPIN_LIMIT)
+                v = lb_load(q);
+            if (!(v & (LB_AGG | LB_PRE))) { // gave up: record it, leave the wait
+                dev_fail(sc, CSG_ERR_DEVICE_WAIT);
+                break;
+            }
+            excl += (long long)(v & LB_VAL);
+            if (v & LB_PRE)
+                break;
         }
+        lb_store(mine, LB_PRE | (unsigned long long)(excl + tot));
+    }
+    int run = gex + (int)excl;
+    for (int w = 0; w < SORT_WARPS; w++) {
+        const int cw = wcount[w][dg];
+        wcount[w][dg] = run;
+        run += cw;
     }
     __syncthreads();
-    // pass 2: stable placement in input order
-    for (int c = 0; c < IPL; c++) {
-        long long i = w0 + c * CSG_WARP + lane;
+    // stable placement in input order
+    for (int cc = 0; cc < IPL; cc++) {
+        long long i = w0 + cc * CSG_WARP + lane;
         unsigned long long k = 0;
         int v = 0;
-        int dg = RADIX;
+        int d = RADIX;
         if (i < n) {
             k = key_in[i];
             v = val_in[i];
-            dg = (int)((k >> shift) & (RADIX - 1));
+            d = (int)((k >> shift) & (RADIX - 1));
         }
-        unsigned peers = __match_any_sync(0xffffffffu, dg);
-        int pos = 0;
-        if (dg < RADIX) {
-            pos = wcount[warp][dg] + __popc(peers & lt);
-            key_out[pos] = k;
-            val_out[pos] = v;
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        if (d < RADIX) {
+            const int pos = wcount[warp][d] + __popc(peers & lt);
+            if (pos >= 0 && pos < n) {
+                key_out[pos] = k;
+                val_out[pos] = v;
+            }
         }
         __syncwarp();
-        if (dg < RADIX && (peers & lt) == 0)
-            wcount[warp][dg] += __popc(peers);
+        if (d < RADIX && (peers & lt) == 0)
+            wcount[warp][d] += __popc(peers);
         __syncwarp();
     }
 }
@@ -272,29 +364,34 @@ int csg_radix_sort(csgd_t *d, unsigned long long *key, int *val, unsigned long l
     const bool small = n < (2 << 20);
     const int tile = small ? sort_tile(4) : sort_tile(16);
     const int nblocks = (n + tile - 1) / tile;
-    const int hn = RADIX * nblocks;
-    if (2 * hn + 1 > d->sort_hist_cap) {
+    const size_t status_words = (size_t)RADIX * nblocks; // 64-bit words per buffer
+    const int passes = (bits + 7) / 8;
+    if (passes < 1)
+        return CSG_OK;
+    if (passes > 8 || SORT_STATUS + 4 * status_words > (size_t)d->sort_hist_cap) {
         csgd_set_err(d, CSG_ERR_NOMEM);
         return CSG_ERR_NOMEM;
     }
-    unsigned int *hist = d->sort_hist;
-    int *offs = (int *)(d->sort_hist + hn);
+    unsigned int *counts = d->sort_hist + SORT_COUNTS;
+    int *tile_ctr = (int *)(d->sort_hist + SORT_TILE_CTR);
+    unsigned long long *status = (unsigned long long *)(d->sort_hist + SORT_STATUS);
+    // counts, counters and the first pass's status buffer start at zero
+    cudaMemsetAsync(d->sort_hist, 0, sizeof(unsigned int) * SORT_STATUS + 8 * status_words,
+                    d->stream);
+    int gc = d->num_sms * 4;
+    if (gc > nblocks)
+        gc = nblocks;
+    { k_radix_counts<<<gc, SORT_THREADS, 0, d->stream>>>(key, n, passes, counts); d->launches++; }
     unsigned long long *ki = key, *ko = key_alt;
     int *vi = val, *vo = val_alt;
-    const int passes = (bits + 7) / 8;
     for (int p = 0; p < passes; p++) {
         const int shift = 8 * p;
+        unsigned long long *st = status + (size_t)(p & 1) * status_words;
+        unsigned long long *st_next = status + (size_t)((p + 1) & 1) * status_words;
         if (small)
-            { k_radix_hist<4><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, n, shift, hist, nblocks); d->launches++; }
+            { k_radix_onesweep<4><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, d->sc); d->launches++; }
         else
-            { k_radix_hist<16><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, n, shift, hist, nblocks); d->launches++; }
-        int rc = csg_scan_exclusive(d, (const int *)hist, offs, hn, nullptr);
-        if (rc)
-            return rc;
-        if (small)
-            { k_radix_scatter<4><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, offs, nblocks); d->launches++; }
-        else
-            { k_radix_scatter<16><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, offs, nblocks); d->launches++; }
+            { k_radix_onesweep<16><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, d->sc); d->launches++; }
         unsigned long long *tk = ki;
         ki = ko;
         ko = tk;
@@ -308,4 +405,36 @@ int csg_radix_sort(csgd_t *d, unsigned long long *key, int *val, unsigned long l
         cudaMemcpyAsync(val, vi, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, d->stream);
     }
     return csgd_check(d, cudaGetLastError());
+}
+
+namespace {
+__global__ void k_iota(int *__restrict__ v, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+        v[i] = i;
+}
+} // namespace
+
+extern "C" int csgd_sort_keys(csgd_t *d, const unsigned long long *keys, int n, int bits,
+                              unsigned long long *out_keys, int *out_index)
+{
+    if (n < 0 || bits < 1 || bits > 64 || (n > 0 && (!keys || !out_keys || !out_index))) {
+        return CSG_ERR_BAD_ARG;
+    }
+    if (n == 0)
+        return CSG_OK;
+    int rc = csgd_reserve(d, n);
+    if (rc)
+        return rc;
+    cudaStream_t s = d->stream;
+    cudaMemcpyAsync(d->key, keys, sizeof(unsigned long long) * (size_t)n, cudaMemcpyHostToDevice, s);
+    { k_iota<<<csgd_grid(n, 256), 256, 0, s>>>(d->perm, n); d->launches++; }
+    rc = csg_radix_sort(d, d->key, d->perm, d->key_alt, d->perm_alt, n, bits);
+    if (rc)
+        return rc;
+    cudaMemcpyAsync(out_keys, d->key, sizeof(unsigned long long) * (size_t)n,
+                    cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(out_index, d->perm, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost, s);
+    return csgd_sync(d);
 }

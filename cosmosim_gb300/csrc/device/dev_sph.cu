@@ -563,13 +563,11 @@ static int ensure_lists(csgd_t *d)
 static int sph_pass(csgd_t *d, int forces, bool sums = true, bool reuse = false)
 {
     if (d->n_gal > 1) { // one system only (see csgd_set_systems)
-        csgd_set_err(d, CSG_ERR_UNSUPPORTED);
         return CSG_ERR_UNSUPPORTED;
     }
     if (d->n <= 0)
         return CSG_OK;
     if (!d->geometry_valid) {
-        csgd_set_err(d, CSG_ERR_BAD_ARG);
         return CSG_ERR_BAD_ARG;
     }
     int rc = ensure_lists(d);
@@ -627,14 +625,12 @@ extern "C" int csgd_find_neighbors(csgd_t *d, double cx, double cy, double cz, d
                                    int *buf, int cap, int *count_out)
 {
     if (d->n_gal > 1) { // one system only (see csgd_set_systems)
-        csgd_set_err(d, CSG_ERR_UNSUPPORTED);
         return CSG_ERR_UNSUPPORTED;
     }
     *count_out = 0;
     if (cap <= 0)
         return CSG_OK;
     if (!d->geometry_valid) {
-        csgd_set_err(d, CSG_ERR_BAD_ARG);
         return CSG_ERR_BAD_ARG;
     }
     // scratch: the export rank buffer holds the result (node_cap >= cap is not

@@ -187,6 +187,9 @@ int csgd_grid(long long n, int block)
     return (int)(g > 0 ? g : 1);
 }
 
+// Records the first error of a launch sequence; the next csgd_sync reports
+// and clears it. Argument errors are returned to the caller at once instead,
+// so that a refused call leaves nothing for a later call to report.
 void csgd_set_err(csgd_t *d, int code)
 {
     if (d->host_err == 0)
@@ -218,6 +221,8 @@ extern "C" const char *csgd_error_string(int code)
         return "octree pool is not a tree";
     case CSG_ERR_WALK_LIMIT:
         return "tree walk stopped on a malformed tree";
+    case CSG_ERR_DEVICE_WAIT:
+        return "a device-side wait gave up (bounded wait expired)";
     case CSG_ERR_NO_DEVICE:
         return "no CUDA device";
     case CSG_ERR_UNSUPPORTED:
@@ -362,7 +367,6 @@ void csgd_drop_graph(csgd_t *d)
 extern "C" int csgd_reserve(csgd_t *d, int n)
 {
     if (n < 0) {
-        csgd_set_err(d, CSG_ERR_BAD_ARG);
         return CSG_ERR_BAD_ARG;
     }
     if (n != d->n && d->n_gal > 1) { // the system layout no longer fits: one system
@@ -401,11 +405,14 @@ extern "C" int csgd_reserve(csgd_t *d, int n)
     ok &= dalloc(&d->perm, cap) == cudaSuccess;
     ok &= dalloc(&d->perm_alt, cap) == cudaSuccess;
     ok &= dalloc(&d->ext, 3 * cap) == cudaSuccess;
-    // digit-major tile histograms: tiles of 1024 keys below 2M keys, else 4096
+    // radix sort scratch: digit counts and tile counters (8 * 256 + 64 words),
+    // then two status buffers of 256 64-bit words per tile; tiles of 1024 keys
+    // below 2M keys, else 4096 (sized for any key count up to ncap)
     const size_t sort_items = ncap;
-    const size_t hist = 256 * (sort_items < (2u << 20) ? (sort_items + 1023) / 1024
-                                                       : (sort_items + 4095) / 4096);
-    d->sort_hist_cap = (int)(2 * hist + 1);
+    const size_t small_items = sort_items < (2u << 20) ? sort_items : (2u << 20) - 1;
+    const size_t tiles_small = (small_items + 1023) / 1024, tiles_large = (sort_items + 4095) / 4096;
+    const size_t hist = 256 * (tiles_small > tiles_large ? tiles_small : tiles_large);
+    d->sort_hist_cap = (int)(4 * hist + 8 * 256 + 64);
     ok &= dalloc(&d->sort_hist, (size_t)d->sort_hist_cap) == cudaSuccess;
     ok &= dalloc(&d->lcp, cap) == cudaSuccess;
     ok &= dalloc(&d->cnt, cap + 1) == cudaSuccess;
@@ -475,19 +482,16 @@ extern "C" int csgd_ensure_tree_extras(csgd_t *d, int geometry, int pool)
 extern "C" int csgd_set_systems(csgd_t *d, int n_sys, const int *host_counts)
 {
     if (n_sys < 1 || n_sys > CSG_MAX_SYSTEMS || (n_sys > 1 && !host_counts)) {
-        csgd_set_err(d, CSG_ERR_BAD_ARG);
         return CSG_ERR_BAD_ARG;
     }
     long long total = 0;
     for (int g = 0; n_sys > 1 && g < n_sys; g++) {
         if (host_counts[g] < 0) {
-            csgd_set_err(d, CSG_ERR_BAD_ARG);
             return CSG_ERR_BAD_ARG;
         }
         total += host_counts[g];
     }
     if (n_sys > 1 && total != d->n) {
-        csgd_set_err(d, CSG_ERR_BAD_ARG);
         return CSG_ERR_BAD_ARG;
     }
     csgd_drop_graph(d); // grid shapes and the system pass change
@@ -578,7 +582,6 @@ extern "C" int csgd_pack_aos(csgd_t *d)
 extern "C" int csgd_download_bodies(csgd_t *d, Body *host, int n)
 {
     if (n > d->n || n < 0) {
-        csgd_set_err(d, CSG_ERR_BAD_ARG);
         return CSG_ERR_BAD_ARG;
     }
     if (n == 0)

@@ -1150,7 +1150,6 @@ extern "C" int csgd_build_tree(csgd_t *d, int geometry)
 extern "C" int csgd_export_pool(csgd_t *d, OctreeNode *pool, int capacity, int *pool_size_out)
 {
     if (d->n_gal > 1) { // one system only (see csgd_set_systems)
-        csgd_set_err(d, CSG_ERR_UNSUPPORTED);
         return CSG_ERR_UNSUPPORTED;
     }
     cudaStream_t s = d->stream;
@@ -1194,11 +1193,9 @@ extern "C" int csgd_export_pool(csgd_t *d, OctreeNode *pool, int capacity, int *
 extern "C" int csgd_import_pool(csgd_t *d, const OctreeNode *pool, int n_nodes, int root)
 {
     if (d->n_gal > 1) { // one system only (see csgd_set_systems)
-        csgd_set_err(d, CSG_ERR_UNSUPPORTED);
         return CSG_ERR_UNSUPPORTED;
     }
     if (n_nodes <= 0 || n_nodes > d->node_cap || root < 0 || root >= n_nodes) {
-        csgd_set_err(d, CSG_ERR_BAD_ARG);
         return CSG_ERR_BAD_ARG;
     }
     cudaStream_t s = d->stream;

@@ -792,7 +792,6 @@ extern "C" int csgd_walk_lists(csgd_t *d, const csgd_force_params *p, int *count
     if (n <= 0)
         return CSG_OK;
     if (d->imported) { // lists are defined on trees built here
-        csgd_set_err(d, CSG_ERR_UNSUPPORTED);
         return CSG_ERR_UNSUPPORTED;
     }
     WalkArgs a = walk_args(d, p);
@@ -812,7 +811,6 @@ extern "C" int csgd_set_walk_shape(csgd_t *d, const CsgWalkShape *w)
 {
     if (!w || (w->warps_per_block != 4 && w->warps_per_block != 8) || w->task_group < 0 ||
         w->task_group > 64 || (w->task_group > 0 && (w->blocks_per_sm < 1 || w->blocks_per_sm > 32))) {
-        csgd_set_err(d, CSG_ERR_BAD_ARG);
         return CSG_ERR_BAD_ARG;
     }
     if (d->walk_warps != w->warps_per_block || d->walk_group != w->task_group ||
@@ -843,7 +841,6 @@ extern "C" int csgd_autotune_walk(csgd_t *d, const csgd_force_params *p, int rep
                                   int *n_all)
 {
     if (reps < 1 || reps > 64) {
-        csgd_set_err(d, CSG_ERR_BAD_ARG);
         return CSG_ERR_BAD_ARG;
     }
     // persistent candidates: 8, 16 or 24 resident warps per SM (24 is what

@@ -254,6 +254,18 @@ CSG_EXPORT void csg_quasar_step(Body *bodies, int *n, int n_alloc, QuasarConfig 
     csg_thread_set_error(rc);
 }
 
+CSG_EXPORT int csg_sort_keys(const uint64_t *keys, int n, int bits, uint64_t *out_keys,
+                             int *out_index)
+{
+    csgd_t *d = csg_thread_dev();
+    if (!d)
+        return CSG_ERR_NO_DEVICE;
+    int rc = csgd_sort_keys(d, (const unsigned long long *)keys, n, bits,
+                            (unsigned long long *)out_keys, out_index);
+    csg_thread_set_error(rc);
+    return rc;
+}
+
 CSG_EXPORT void csg_quasar_seed(uint64_t rng_state, int knot_phase)
 {
     csgd_t *d = csg_thread_dev();

@@ -94,6 +94,7 @@ _SIGS = {
     "cosmosim_energy": ([_vp, ctypes.POINTER(_d), ctypes.POINTER(_d)], _i),
     "cosmosim_launch_count": ([_vp], ctypes.c_int64),
     "csg_measure_fp_peaks": ([ctypes.POINTER(_d), ctypes.POINTER(_d)], _i),
+    "csg_sort_keys": ([_vp, _i, _i, _vp, _vp], _i),
     "cosmosim_enable_graphs": ([_vp, _i], _i),
     "csg_direct_forces_noalloc": ([_vp, _vp, _vp, _vp, _i, _vp, _i, _d, _d, _vp, _vp], _i),
     "cosmosim_create_ensemble": ([_vp, _i, _i, _ip, ctypes.POINTER(CsgSimParams)], _vp),
@@ -243,6 +244,19 @@ def generate_ics(kind, n, seed):
     if lib.csg_generate_ics(kind, n, seed, ptr(out)) != n:
         raise ValueError(f"bad ICs request kind={kind} n={n}")
     return out
+
+
+def sort_keys(keys, bits=64):
+    """The tree build's radix sort (csg_sort_keys) on uint64 keys: returns
+    (sorted keys, input position of each sorted key); stable."""
+    lib = load()
+    k = np.ascontiguousarray(keys, dtype=np.uint64)
+    out = np.empty_like(k)
+    idx = np.empty(len(k), dtype=np.int32)
+    rc = lib.csg_sort_keys(ptr(k), len(k), bits, ptr(out), ptr(idx))
+    if rc:
+        raise CudaError(f"csg_sort_keys: {lib.csg_error_string(rc).decode()} (code {rc})")
+    return out, idx
 
 
 # ---- handle API (reference cosmosim_api.h) ----

@@ -29,6 +29,7 @@ extern "C" {
 #define CSG_ERR_WALK_LIMIT 6
 #define CSG_ERR_NO_DEVICE 7
 #define CSG_ERR_UNSUPPORTED 8
+#define CSG_ERR_DEVICE_WAIT 9 /* a bounded device-side wait expired */
 
 /* Walk precision. FP64 is the drop-in default. FP32_MIXED evaluates pair
    accelerations in FP32 (positions as float hi/lo pairs, Kahan-compensated
@@ -192,6 +193,15 @@ CSG_EXPORT int64_t cosmosim_launch_count(SimHandle handle);
    timing independent FMA chains: the pipe peaks the gravity walks are
    bound by. */
 CSG_EXPORT int csg_measure_fp_peaks(double *fp32_tflops, double *fp64_tflops);
+
+/* The tree build's key sort on caller keys: an LSD radix sort, 8 bits a pass,
+   ceil(bits/8) passes (bits 1..64), stable. out_keys = keys in ascending order
+   of their low 8*ceil(bits/8) bits; out_index = the input position of each
+   sorted key (equal keys keep their input order). Host arrays of n entries
+   (n >= 0). Uses the calling thread's device state; returns CSG_OK or an
+   error code. */
+CSG_EXPORT int csg_sort_keys(const uint64_t *keys, int n, int bits, uint64_t *out_keys,
+                             int *out_index);
 
 /* FP64 direct-sum accelerations without any allocation — has no counterpart
    in the reference. For callers that cannot allocate device memory (an
