@@ -163,8 +163,10 @@ CSG_EXPORT void integrator_step(Body *bodies, int n, double dt, double G, double
     }
     csgd_force_params p = force_params(G, softening, theta);
     int rc = csgd_upload_bodies(d, bodies, n);
+    /* one substep, replayed from the thread state's captured graph while n
+       and the parameters stay the same (bit-identical to direct launches) */
     if (!rc)
-        rc = csgd_substep(d, dt, &p, sph_enabled ? 1 : 0);
+        rc = csgd_substeps(d, 1, dt, &p, sph_enabled ? 1 : 0);
     if (!rc)
         rc = store_pool(d, pool, NULL, n);
     if (!rc)
