@@ -160,8 +160,26 @@ void csgd_enable_graphs(csgd_t *d, int on);
 int csgd_prepare_sph(csgd_t *d);
 
 /* The tree as a reference-layout pool, in the reference's allocation order.
-   Blocks until done. pool must hold *pool_size_out <= capacity nodes. */
+   Blocks until done. pool must hold *pool_size_out <= capacity nodes; a
+   mapped (pinned) host pool is written by the export kernel directly. */
 int csgd_export_pool(csgd_t *d, OctreeNode *pool, int capacity, int *pool_size_out);
+
+/* The same export enqueued on the state's stream without a host round trip:
+   dst is device-accessible (device memory or the device view of a mapped
+   host array) with room for capacity cells; a larger tree records
+   CSG_ERR_NODE_CAPACITY for the next csgd_sync and writes nothing. Needs a
+   tree built with the export order (csgd_set_export_order). */
+int csgd_export_to(csgd_t *d, OctreeNode *dst, int capacity);
+
+/* Device view of a mapped (pinned) host pointer, or NULL for any other
+   memory. */
+void *csgd_host_view(const void *p);
+
+/* While set (dst != NULL), every substep also exports the tree it builds to
+   dst (as csgd_export_to), on a third stream beside the walk. Returns 1 when
+   set, 0 when this state cannot (no third stream, no export order, several
+   systems): the caller then exports after the substep. */
+int csgd_set_substep_export(csgd_t *d, OctreeNode *dst, int capacity);
 
 /* Replaces the device tree by the caller's pool (nodes reachable from root;
    n_nodes = highest reachable index + 1). */

@@ -117,6 +117,10 @@ struct csgd {
     cudaStream_t own_stream;
     cudaStream_t aux;             // SPH runs here beside the gravity walk
     cudaEvent_t ev_fork, ev_join; // (timing disabled)
+    cudaStream_t aux2;            // pool export beside the walk (free functions)
+    cudaEvent_t ev_fork2, ev_join2;
+    OctreeNode *export_dst; // set: substeps also export their tree here (device view)
+    int export_cap;         // capacity of export_dst, cells
     int n;        // bodies in use
     int cap;      // body capacity
     int node_cap; // node capacity (8*cap + 64)
@@ -192,6 +196,8 @@ struct csgd {
     double graph_key[4];               // dt, G, softening, theta it was captured for
     int graph_prec, graph_sph, graph_n;
     cudaStream_t graph_stream;
+    OctreeNode *graph_export;
+    int graph_export_cap;
     int use_graphs;
     int imported;  // the tree came from a caller pool (no sorted order)
     int gas_valid; // d->gas / n_gas match the current tree
@@ -207,9 +213,11 @@ int csgd_grid(long long n, int block);
 
 // ---- sort / scan utilities (dev_sort.cu) ----
 // Stable LSD radix sort of (key, value) over n items, on key bits [0, bits).
-// Result in (key, val); alt buffers are scratch of the same size.
+// Result in (key, val); alt buffers are scratch of the same size. With n_dev
+// the item count is min(n, *n_dev), read on the device (no host round trip;
+// the launches are sized for n).
 int csg_radix_sort(csgd_t *d, unsigned long long *key, int *val, unsigned long long *key_alt,
-                   int *val_alt, int n, int bits);
+                   int *val_alt, int n, int bits, const int *n_dev = nullptr);
 // Exclusive scan of in[0..n) into out[0..n], out[n] = total. count_limit, when
 // non-NULL, is a device int: items at positions >= *count_limit count as 0.
 int csg_scan_exclusive(csgd_t *d, const int *in, int *out, int n, const int *count_limit);

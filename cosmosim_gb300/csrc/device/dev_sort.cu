@@ -177,9 +177,12 @@ __device__ __forceinline__ unsigned long long lb_load(const unsigned long long *
 
 // Digit counts of passes 0..passes-1 (counts[pass][digit], zeroed before).
 __global__ void __launch_bounds__(SORT_THREADS) k_radix_counts(const unsigned long long *__restrict__ key,
-                                                               int n, int passes,
+                                                               int n, const int *__restrict__ n_dev,
+                                                               int passes,
                                                                unsigned int *__restrict__ counts)
 {
+    if (n_dev)
+        n = max(0, min(n, *n_dev));
     __shared__ unsigned int h[8][RADIX];
     for (int i = threadIdx.x; i < 8 * RADIX; i += blockDim.x)
         (&h[0][0])[i] = 0;
@@ -216,8 +219,12 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_onesweep(
     unsigned long long *__restrict__ key_out, int *__restrict__ val_out, int n, int shift,
     const unsigned int *__restrict__ counts, int *__restrict__ tile_ctr,
     unsigned long long *status, unsigned long long *__restrict__ status_next, int nblocks,
-    DevScalars *sc)
+    const int *__restrict__ n_dev, DevScalars *sc)
 {
+    if (n_dev) { // key count known on the device only: the grid covers the bound
+        n = max(0, min(n, *n_dev));
+        nblocks = (n + sort_tile(IPL) - 1) / sort_tile(IPL);
+    }
     static_assert(SORT_THREADS == RADIX, "one digit per thread");
     __shared__ int wcount[SORT_WARPS][RADIX];
     __shared__ int warp_tot[SORT_WARPS];
@@ -229,7 +236,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_onesweep(
         (&wcount[0][0])[i] = 0;
     __syncthreads();
     const int tile = sh_tile;
-    if (tile >= nblocks) // more blocks than tiles cannot happen (grid = nblocks)
+    if (tile >= nblocks) // only when the live count is below the bound
         return;
     status_next[(size_t)tile * RADIX + threadIdx.x] = 0ull;
     const long long w0 = (long long)tile * sort_tile(IPL) + (long long)warp * (CSG_WARP * IPL);
@@ -357,7 +364,7 @@ int csg_scan_exclusive(csgd_t *d, const int *in, int *out, int n, const int *cou
 }
 
 int csg_radix_sort(csgd_t *d, unsigned long long *key, int *val, unsigned long long *key_alt,
-                   int *val_alt, int n, int bits)
+                   int *val_alt, int n, int bits, const int *n_dev)
 {
     if (n <= 1)
         return CSG_OK;
@@ -381,7 +388,7 @@ int csg_radix_sort(csgd_t *d, unsigned long long *key, int *val, unsigned long l
     int gc = d->num_sms * 4;
     if (gc > nblocks)
         gc = nblocks;
-    { k_radix_counts<<<gc, SORT_THREADS, 0, d->stream>>>(key, n, passes, counts); d->launches++; }
+    { k_radix_counts<<<gc, SORT_THREADS, 0, d->stream>>>(key, n, n_dev, passes, counts); d->launches++; }
     unsigned long long *ki = key, *ko = key_alt;
     int *vi = val, *vo = val_alt;
     for (int p = 0; p < passes; p++) {
@@ -389,9 +396,9 @@ int csg_radix_sort(csgd_t *d, unsigned long long *key, int *val, unsigned long l
         unsigned long long *st = status + (size_t)(p & 1) * status_words;
         unsigned long long *st_next = status + (size_t)((p + 1) & 1) * status_words;
         if (small)
-            { k_radix_onesweep<4><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, d->sc); d->launches++; }
+            { k_radix_onesweep<4><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, n_dev, d->sc); d->launches++; }
         else
-            { k_radix_onesweep<16><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, d->sc); d->launches++; }
+            { k_radix_onesweep<16><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, n_dev, d->sc); d->launches++; }
         unsigned long long *tk = ki;
         ki = ko;
         ko = tk;

@@ -258,6 +258,17 @@ extern "C" csgd_t *csgd_create(void)
         d->aux = nullptr;
         d->ev_fork = d->ev_join = nullptr;
     }
+    if (cudaStreamCreateWithFlags(&d->aux2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&d->ev_fork2, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&d->ev_join2, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError(); // no overlap then: pool exports follow the substep
+        if (d->aux2)
+            cudaStreamDestroy(d->aux2);
+        if (d->ev_fork2)
+            cudaEventDestroy(d->ev_fork2);
+        d->aux2 = nullptr;
+        d->ev_fork2 = d->ev_join2 = nullptr;
+    }
     d->use_graphs = 1;
     d->n_gal = 1;
     d->walk_warps = 4; // fastest one-warp-per-task shape at 20k..1M bodies
@@ -326,6 +337,12 @@ extern "C" void csgd_destroy(csgd_t *d)
         cudaStreamDestroy(d->aux);
         cudaEventDestroy(d->ev_fork);
         cudaEventDestroy(d->ev_join);
+    }
+    if (d->aux2) {
+        cudaStreamSynchronize(d->aux2);
+        cudaStreamDestroy(d->aux2);
+        cudaEventDestroy(d->ev_fork2);
+        cudaEventDestroy(d->ev_join2);
     }
     if (d->own_stream)
         cudaStreamDestroy(d->own_stream);
@@ -633,6 +650,18 @@ extern "C" int csgd_substep(csgd_t *d, double dt, const csgd_force_params *p, in
     int rc = csgd_kick_drift(d, dt);
     if (!rc)
         rc = csgd_build_tree(d, sph);
+    // the pool export reads the finished tree only: it runs beside the walk
+    bool exported = false;
+    if (!rc && d->export_dst && d->aux2) {
+        const cudaStream_t main = d->stream;
+        cudaEventRecord(d->ev_fork2, main);
+        cudaStreamWaitEvent(d->aux2, d->ev_fork2, 0);
+        d->stream = d->aux2;
+        rc = csgd_export_to(d, d->export_dst, d->export_cap);
+        d->stream = main;
+        cudaEventRecord(d->ev_join2, d->aux2);
+        exported = true;
+    }
     if (!rc && sph && d->aux && d->n_gal == 1) {
         const cudaStream_t main = d->stream;
         cudaEventRecord(d->ev_fork, main);
@@ -668,6 +697,8 @@ extern "C" int csgd_substep(csgd_t *d, double dt, const csgd_force_params *p, in
         rc = csgd_kick(d, dt);
     if (!rc && sph)
         rc = csgd_sph_cooling(d, dt);
+    if (exported)
+        cudaStreamWaitEvent(d->stream, d->ev_join2, 0); // always rejoin (a capture needs it)
     return rc;
 }
 
@@ -694,6 +725,29 @@ extern "C" int csgd_sync(csgd_t *d)
             rc = dev_err;
     }
     return rc;
+}
+
+extern "C" int csgd_set_substep_export(csgd_t *d, OctreeNode *dst, int capacity)
+{
+    // the export stages its records in the pool buffer (allocated here, never
+    // inside a capture)
+    const bool ok = dst && d->aux2 && d->export_order && d->n_gal == 1 &&
+                    csgd_ensure_tree_extras(d, 1, 1) == CSG_OK;
+    d->export_dst = ok ? dst : nullptr;
+    d->export_cap = d->export_dst ? capacity : 0;
+    return d->export_dst != nullptr;
+}
+
+extern "C" void *csgd_host_view(const void *p)
+{
+    cudaPointerAttributes a;
+    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost && a.devicePointer)
+        return a.devicePointer;
+    return nullptr;
 }
 
 extern "C" int csgd_node_count(csgd_t *d, int *n_nodes)
@@ -750,7 +804,8 @@ static bool graph_matches(const csgd_t *d, double dt, const csgd_force_params *p
     return d->graph && d->graph_key[0] == dt && d->graph_key[1] == p->G &&
            d->graph_key[2] == p->softening && d->graph_key[3] == p->theta &&
            d->graph_prec == p->precision && d->graph_sph == sph && d->graph_n == d->n &&
-           d->graph_stream == d->stream;
+           d->graph_stream == d->stream && d->graph_export == d->export_dst &&
+           d->graph_export_cap == d->export_cap;
 }
 
 // Captures one substep on the state's stream. Returns CSG_OK or an error (the
@@ -762,6 +817,8 @@ static int capture_substep(csgd_t *d, double dt, const csgd_force_params *p, int
         d->graph = nullptr;
     }
     if (sph && csgd_prepare_sph(d))
+        return CSG_ERR_NOMEM;
+    if (d->export_dst && csgd_ensure_tree_extras(d, 1, 1))
         return CSG_ERR_NOMEM;
     // host-side flags a substep resets anyway; start from the same state
     d->gas_valid = 0;
@@ -798,6 +855,8 @@ static int capture_substep(csgd_t *d, double dt, const csgd_force_params *p, int
     d->graph_sph = sph;
     d->graph_n = d->n;
     d->graph_stream = d->stream;
+    d->graph_export = d->export_dst;
+    d->graph_export_cap = d->export_cap;
     return CSG_OK;
 }
 

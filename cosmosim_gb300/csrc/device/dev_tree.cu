@@ -888,10 +888,18 @@ __global__ void k_rank(csgd_t dd, DevScalars *sc)
     dd.rank[dd.ord_id[r]] = r;
 }
 
-__global__ void k_export(csgd_t dd, DevScalars *sc)
+// Pool records in the reference's numbering, written to dst (device memory or
+// a caller's mapped host array of `capacity` cells; a larger tree is refused).
+__global__ void k_export(csgd_t dd, DevScalars *sc, OctreeNode *__restrict__ dst, int capacity)
 {
     const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= min(sc->n_nodes, dd.node_cap))
+    const int nn = min(sc->n_nodes, dd.node_cap);
+    if (nn > capacity) {
+        if (id == 0)
+            dev_fail(sc, CSG_ERR_NODE_CAPACITY);
+        return;
+    }
+    if (id >= nn)
         return;
     NodeW64 w = dd.w64[id];
     double4 g = dd.geo[id];
@@ -909,7 +917,36 @@ __global__ void k_export(csgd_t dd, DevScalars *sc)
         int c = dd.child[8 * (size_t)id + q];
         o.children[q] = (c >= 0) ? dd.rank[c] : -1;
     }
-    dd.pool[dd.rank[id]] = o;
+    dst[dd.rank[id]] = o;
+}
+
+// Streams the exported records (nn cells, nn read on the device) from the
+// device staging array to a caller's mapped host array in address order:
+// 16-byte words when both ends allow, 8-byte words otherwise.
+__global__ void k_pool_out(const OctreeNode *__restrict__ src, OctreeNode *__restrict__ dst,
+                           const DevScalars *__restrict__ sc, int capacity, int node_cap)
+{
+    const int nn = min(sc->n_nodes, node_cap);
+    if (nn > capacity)
+        return; // refused by k_export
+    const size_t bytes = sizeof(OctreeNode) * (size_t)nn;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if ((((size_t)src | (size_t)dst) & 15) == 0) {
+        const size_t n16 = bytes / 16;
+        const int4 *s4 = (const int4 *)src;
+        int4 *d4 = (int4 *)dst;
+        for (size_t i = t0; i < n16; i += stride)
+            d4[i] = s4[i];
+        if (t0 == 0 && (bytes & 15)) // OctreeNode is 8-byte aligned: at most one tail word
+            ((unsigned long long *)dst)[bytes / 8 - 1] = ((const unsigned long long *)src)[bytes / 8 - 1];
+    } else {
+        const size_t n8 = bytes / 8;
+        const unsigned long long *s8 = (const unsigned long long *)src;
+        unsigned long long *d8 = (unsigned long long *)dst;
+        for (size_t i = t0; i < n8; i += stride)
+            d8[i] = s8[i];
+    }
 }
 
 // ---- import of a caller pool ---------------------------------------------
@@ -1147,14 +1184,46 @@ extern "C" int csgd_build_tree(csgd_t *d, int geometry)
     return csgd_check(d, cudaGetLastError());
 }
 
-extern "C" int csgd_export_pool(csgd_t *d, OctreeNode *pool, int capacity, int *pool_size_out)
+// Export without a host round trip: the cell count is read on the device
+// (order keys, sort, ranks and records are sized for `capacity` cells).
+// Needs the export order (minidx) of the current tree.
+extern "C" int csgd_export_to(csgd_t *d, OctreeNode *dst, int capacity)
 {
-    if (d->n_gal > 1) { // one system only (see csgd_set_systems)
+    if (d->n_gal > 1) // one system only (see csgd_set_systems)
         return CSG_ERR_UNSUPPORTED;
-    }
+    if (!d->minidx_valid || !dst || capacity < 1)
+        return CSG_ERR_BAD_ARG;
     cudaStream_t s = d->stream;
     DevScalars *sc = d->sc;
     const int B = 256;
+    if (!d->geometry_valid) {
+        const int gn = csgd_grid(d->node_cap, B);
+        { k_geometry<<<gn, B, 0, s>>>(*d, sc, d->roots, d->key, d->ext, d->sgid); d->launches++; }
+        d->geometry_valid = 1;
+    }
+    if (dst != d->pool && !d->pool)
+        return CSG_ERR_BAD_ARG; // staging not allocated (csgd_ensure_tree_extras)
+    const int bound = capacity < d->node_cap ? capacity : d->node_cap;
+    const int g = csgd_grid(bound, B);
+    { k_order_keys<<<g, B, 0, s>>>(*d, sc); d->launches++; }
+    int rc = csg_radix_sort(d, d->ord_key, d->ord_id, d->ord_key_alt, d->ord_id_alt, bound, 40,
+                            &sc->n_nodes);
+    if (rc)
+        return rc;
+    { k_rank<<<g, B, 0, s>>>(*d, sc); d->launches++; }
+    if (dst == d->pool) {
+        { k_export<<<g, B, 0, s>>>(*d, sc, dst, capacity); d->launches++; }
+    } else { // records land in rank order: stage them, then stream them out in address order
+        { k_export<<<g, B, 0, s>>>(*d, sc, d->pool, capacity); d->launches++; }
+        { k_pool_out<<<4 * d->num_sms, B, 0, s>>>(d->pool, dst, sc, capacity, d->node_cap); d->launches++; }
+    }
+    return csgd_check(d, cudaGetLastError());
+}
+
+extern "C" int csgd_export_pool(csgd_t *d, OctreeNode *pool, int capacity, int *pool_size_out)
+{
+    if (d->n_gal > 1) // one system only (see csgd_set_systems)
+        return CSG_ERR_UNSUPPORTED;
     int erc = csgd_ensure_tree_extras(d, 1, 1);
     if (erc)
         return erc;
@@ -1166,27 +1235,17 @@ extern "C" int csgd_export_pool(csgd_t *d, OctreeNode *pool, int capacity, int *
         if (erc)
             return erc;
     }
-    if (!d->geometry_valid) {
-        const int gn = csgd_grid(d->node_cap, B);
-        { k_geometry<<<gn, B, 0, s>>>(*d, sc, d->roots, d->key, d->ext, d->sgid); d->launches++; }
-        d->geometry_valid = 1;
-    }
-    int rc = csgd_node_count(d, pool_size_out);
-    if (rc)
+    // a caller's mapped (pinned) host array takes the records directly
+    OctreeNode *mapped = (OctreeNode *)csgd_host_view(pool);
+    const int cap = mapped ? capacity : (capacity < d->node_cap ? capacity : d->node_cap);
+    int rc = csgd_export_to(d, mapped ? mapped : d->pool, cap);
+    if (!rc)
+        rc = csgd_node_count(d, pool_size_out); // reports a refused export
+    if (rc || mapped)
         return rc;
     const int nn = *pool_size_out;
-    if (nn > capacity || nn > d->node_cap) {
-        csgd_set_err(d, CSG_ERR_NODE_CAPACITY);
-        return CSG_ERR_NODE_CAPACITY;
-    }
-    const int g = csgd_grid(nn, B);
-    { k_order_keys<<<g, B, 0, s>>>(*d, sc); d->launches++; }
-    rc = csg_radix_sort(d, d->ord_key, d->ord_id, d->ord_key_alt, d->ord_id_alt, nn, 40);
-    if (rc)
-        return rc;
-    { k_rank<<<g, B, 0, s>>>(*d, sc); d->launches++; }
-    { k_export<<<g, B, 0, s>>>(*d, sc); d->launches++; }
-    cudaMemcpyAsync(pool, d->pool, sizeof(OctreeNode) * (size_t)nn, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(pool, d->pool, sizeof(OctreeNode) * (size_t)nn, cudaMemcpyDeviceToHost,
+                    d->stream);
     return csgd_sync(d);
 }
 

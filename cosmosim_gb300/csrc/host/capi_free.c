@@ -163,11 +163,17 @@ CSG_EXPORT void integrator_step(Body *bodies, int n, double dt, double G, double
     }
     csgd_force_params p = force_params(G, softening, theta);
     int rc = csgd_upload_bodies(d, bodies, n);
+    /* a mapped (pinned) pool is filled by the export kernels beside the walk;
+       any other pool after the substep */
+    OctreeNode *pool_view = n > 0 ? (OctreeNode *)csgd_host_view(pool) : NULL;
+    if (pool_view && !csgd_set_substep_export(d, pool_view, 8 * (n > 1 ? n : 1)))
+        pool_view = NULL;
     /* one substep, replayed from the thread state's captured graph while n
        and the parameters stay the same (bit-identical to direct launches) */
     if (!rc)
         rc = csgd_substeps(d, 1, dt, &p, sph_enabled ? 1 : 0);
-    if (!rc)
+    csgd_set_substep_export(d, NULL, 0);
+    if (!rc && !pool_view)
         rc = store_pool(d, pool, NULL, n);
     if (!rc)
         rc = csgd_download_bodies(d, bodies, n);

@@ -184,3 +184,23 @@ def test_energy_drift_bound_and_precision(lib):
         s.close()
     assert max(drifts) < 2e-2, drifts
     assert abs(drifts[0] - drifts[1]) <= 1e-5, drifts
+
+
+@pytest.mark.parametrize("sph", [0, 1])
+def test_integrator_step_pinned_pool_equals_pageable(lib, sph):
+    """A pinned (mapped) pool is written by the export kernels beside the walk,
+    a pageable one by a copy after the substep: bodies and pools must agree
+    bit for bit, step after step."""
+    torch = pytest.importorskip("torch")
+    b = lib.generate_ics(1, 3000, 5)
+    n = len(b)
+    page_b, page_pool = b.copy(), np.zeros(8 * n, dtype=NODE_DTYPE)
+    pin_b = torch.empty(n * b.dtype.itemsize, dtype=torch.uint8, pin_memory=True).numpy().view(b.dtype)
+    pin_b[:] = b
+    pin_pool = torch.zeros(8 * n * NODE_DTYPE.itemsize, dtype=torch.uint8,
+                           pin_memory=True).numpy().view(NODE_DTYPE)
+    for step in range(4):
+        lib.integrator_step(page_b, 1e-3, 1.0, 0.01, 0.5, page_pool, sph)
+        lib.integrator_step(pin_b, 1e-3, 1.0, 0.01, 0.5, pin_pool, sph)
+        assert page_b.tobytes() == pin_b.tobytes(), step
+        assert page_pool.tobytes() == pin_pool.tobytes(), step
