@@ -255,18 +255,33 @@ __global__ void __launch_bounds__(8 * CSG_WARP) k_walk64(WalkArgs a)
         add_hits(a, st);
 }
 
+// FP32 value of a positive double whose exponent lies in FP32's normal range,
+// from its bits alone (exponent rebased from 1023 to 127, mantissa truncated
+// to 23 bits: relative error < 2^-23), and the exact double of a positive
+// normal float. Integer operations only: conversion instructions would run on
+// the FP64 pipe, the walk's bottleneck on this GPU.
+__device__ __forceinline__ float f32_from_f64_bits(long long b)
+{
+    return __int_as_float((int)((b >> 29) - (896LL << 23)));
+}
+__device__ __forceinline__ double f64_from_f32_bits(float f)
+{
+    return __longlong_as_double(((long long)__float_as_int(f) + (896LL << 23)) << 29);
+}
+
 // m/r^3 for the queued FP64 walk, with few FP64 operations (the FP64 pipe
 // is the walk's bottleneck on this GPU): y0 = FP32 rsqrt seed (rel. error
 // < 2^-21), y0^2 exact in FP64, e = 1 - r2*y0^2 by one fused multiply-add,
 // then m/r^3 = m*y0^3 * (1-e)^-3/2 = m*y0^3 * (1 + e(3/2 + 15/8 e)) (the
-// series to second order; the next term is < 2^-60). Range check on the FP32
-// value; outside it the plain expression. (Forming 15/8 e^2 in FP32 instead
-// saves one FP64 operation but its two conversions cost more on this GPU.)
+// series to second order; the next term is < 2^-60). The seed's conversions
+// are bit operations, range-checked on the exponent (2^-99 <= r2 < 2^100);
+// outside that range the plain expression. (Forming 15/8 e^2 in FP32 instead
+// saves one FP64 operation but needs real conversions.)
 __device__ __forceinline__ double m_inv_r3_q(double m, double r2)
 {
-    const float r2f = (float)r2;
-    if (r2f >= 1e-30f && r2f <= 1e30f) {
-        const double y0 = (double)rsqrtf(r2f);
+    const long long bits = __double_as_longlong(r2);
+    if ((unsigned long long)((bits >> 52) - 924) <= 198ull) { // sign clear, exponent 924..1122
+        const double y0 = f64_from_f32_bits(rsqrtf(f32_from_f64_bits(bits)));
         const double y0sq = y0 * y0;
         const double e = fma(-r2, y0sq, 1.0);
         const double mz = m * (y0sq * y0);
