@@ -541,11 +541,16 @@ __global__ void __launch_bounds__(WARPS * CSG_WARP, persist_min_blocks(WARPS, PE
 // has work, in the order they were accepted (the reference's depth-first
 // order). The FP64 pipe then does useful work on (almost) every lane instead
 // of once per traversal step for the few lanes that interact at that step.
-constexpr int Q64 = 32; // queue slots per lane
-constexpr int F64 = 8;  // entries per lane per dense batch
+// Queue slots per lane (a power of two): 64 for 4-warp blocks, 32 for 8-warp
+// blocks (static shared memory stays below 48 KB). Deeper queues make the
+// overflow drains, which leave lanes idle, rarer. The evaluation order (FIFO)
+// and so the results do not depend on the depth.
+constexpr int q64_slots(int warps) { return warps == 4 ? 64 : 32; }
+constexpr int F64 = 8; // entries per lane per dense batch
 
 // Evaluates the lane's next `count` queued cells (count >= 0; lanes without a
 // body pass 0 and never read their queue).
+template <int Q64>
 __device__ __forceinline__ void q64_eval(const WalkArgs &a, const int *q, int lane, int &head,
                                          int count, double px, double py, double pz,
                                          double &sx, double &sy, double &sz)
@@ -568,7 +573,7 @@ __device__ __forceinline__ void q64_eval(const WalkArgs &a, const int *q, int la
     head += count;
 }
 
-template <bool STATS, bool EMPTY>
+template <bool STATS, bool EMPTY, int Q64>
 __device__ __forceinline__ void walk64q_task(const WalkArgs &a, NodeW32 *win, int *q,
                                              const TaskRange &tr, WalkStats &st)
 {
@@ -596,12 +601,12 @@ __device__ __forceinline__ void walk64q_task(const WalkArgs &a, NodeW32 *win, in
             const int cmin = (int)__reduce_min_sync(0xffffffffu, (unsigned)(valid ? cnt : INT_MAX));
             const int cmax = (int)__reduce_max_sync(0xffffffffu, (unsigned)cnt);
             if (cmin >= F64)
-                q64_eval(a, q, lane, head, valid ? F64 : 0, b.px, b.py, b.pz, sx, sy, sz);
+                q64_eval<Q64>(a, q, lane, head, valid ? F64 : 0, b.px, b.py, b.pz, sx, sy, sz);
             else if (cmax >= Q64 - 1) // a lane is about to overflow: drain what is there
-                q64_eval(a, q, lane, head, min(cnt, F64), b.px, b.py, b.pz, sx, sy, sz);
+                q64_eval<Q64>(a, q, lane, head, min(cnt, F64), b.px, b.py, b.pz, sx, sy, sz);
         });
     while (__any_sync(0xffffffffu, tail - head > 0))
-        q64_eval(a, q, lane, head, min(tail - head, F64), b.px, b.py, b.pz, sx, sy, sz);
+        q64_eval<Q64>(a, q, lane, head, min(tail - head, F64), b.px, b.py, b.pz, sx, sy, sz);
     if (valid) {
         a.ax[me] = a.G * sx;
         a.ay[me] = a.G * sy;
@@ -612,13 +617,14 @@ __device__ __forceinline__ void walk64q_task(const WalkArgs &a, NodeW32 *win, in
 template <bool STATS, bool EMPTY, int WARPS, bool PERSIST>
 __global__ void __launch_bounds__(WARPS * CSG_WARP, w64q_min_blocks(WARPS, PERSIST)) k_walk64q(WalkArgs a)
 {
+    constexpr int Q64 = q64_slots(WARPS);
     __shared__ int q_all[WARPS][Q64 * CSG_WARP];
     __shared__ NodeW32 win_all[WARPS][CSG_WARP];
     const int warp = threadIdx.x >> 5;
     int *q = q_all[warp];
     NodeW32 *win = win_all[warp];
     WalkStats st;
-    for_each_task<WARPS, PERSIST>(a, [&](const TaskRange &tr) { walk64q_task<STATS, EMPTY>(a, win, q, tr, st); });
+    for_each_task<WARPS, PERSIST>(a, [&](const TaskRange &tr) { walk64q_task<STATS, EMPTY, Q64>(a, win, q, tr, st); });
     if (STATS)
         add_hits(a, st);
 }
