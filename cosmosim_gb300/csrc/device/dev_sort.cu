@@ -1,13 +1,14 @@
 // dev_sort.cu — exclusive scan and stable LSD radix sort used by the tree build.
 //
-// Radix sort: 8-bit digits, three kernels per digit (tile histogram, scan of
-// the digit-major histogram, stable scatter); tiles of 1024 keys below 2M keys,
-// 4096 above. Stability inside a tile comes
-// from giving each warp a contiguous slice of the tile and ranking equal
-// digits with __match_any_sync in input order; across tiles from the
-// digit-major exclusive scan. Stability matters: keys that tie keep caller
-// index order, which the tree build relies on (reference inserts bodies in
-// index order, src/octree.c:163-168).
+// Radix sort: 8-bit digits; one kernel counts the digits of every pass, then
+// one single-pass kernel per digit (tiles of 1024 keys below 2M keys, 4096
+// above) finds each tile's offsets by decoupled look-back. Stability inside a
+// tile comes from giving each warp a contiguous slice of the tile and ranking
+// equal digits in input order (a lane's peers, the lanes holding the same
+// digit, from nine ballots on the digit's bits); across tiles from the
+// look-back's tile order. Stability matters: keys that tie keep caller index
+// order, which the tree build relies on (reference inserts bodies in index
+// order, src/octree.c:163-168).
 #include "dev_internal.cuh"
 
 namespace {
@@ -22,6 +23,20 @@ constexpr int SORT_WARPS = SORT_THREADS / CSG_WARP;
 // below 2M keys, so that a 100k-key sort still spreads over ~100 blocks.
 constexpr int sort_tile(int ipl) { return SORT_WARPS * CSG_WARP * ipl; }
 constexpr int RADIX = 256;
+
+// Lanes of the warp whose value equals this lane's (values 0..511): the
+// intersection over the nine bits of the ballots that agree with this lane's
+// bit. All lanes take part.
+__device__ __forceinline__ unsigned same_digit_lanes(unsigned v)
+{
+    unsigned m = 0xffffffffu;
+#pragma unroll
+    for (int b = 0; b < 9; b++) {
+        const unsigned bal = __ballot_sync(0xffffffffu, (v >> b) & 1u);
+        m &= ((v >> b) & 1u) ? bal : ~bal;
+    }
+    return m;
+}
 
 __device__ __forceinline__ int warp_incl_scan(int v)
 {
@@ -197,7 +212,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_counts(const unsigned lo
         const unsigned long long k = (i < n) ? key[i] : 0ull;
         for (int p = 0; p < passes; p++) {
             const int dg = (i < n) ? (int)((k >> (8 * p)) & (RADIX - 1)) : RADIX;
-            const unsigned peers = __match_any_sync(0xffffffffu, dg);
+            const unsigned peers = same_digit_lanes((unsigned)dg);
             if (dg < RADIX && (peers & lt) == 0)
                 atomicAdd(&h[p][dg], (unsigned)__popc(peers));
         }
@@ -245,7 +260,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_onesweep(
     for (int c = 0; c < IPL; c++) {
         long long i = w0 + c * CSG_WARP + lane;
         int dg = (i < n) ? (int)((key_in[i] >> shift) & (RADIX - 1)) : RADIX;
-        unsigned peers = __match_any_sync(0xffffffffu, dg);
+        unsigned peers = same_digit_lanes((unsigned)dg);
         if (dg < RADIX && (peers & lt) == 0)
             wcount[warp][dg] += __popc(peers);
         __syncwarp();
@@ -303,7 +318,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_onesweep(
             v = val_in[i];
             d = (int)((k >> shift) & (RADIX - 1));
         }
-        unsigned peers = __match_any_sync(0xffffffffu, d);
+        unsigned peers = same_digit_lanes((unsigned)d);
         if (d < RADIX) {
             const int pos = wcount[warp][d] + __popc(peers & lt);
             if (pos >= 0 && pos < n) {

@@ -644,18 +644,23 @@ __global__ void k_tasks(DevScalars *sc, DevRoot *roots, int n_gal, const int *__
     }
 }
 
+// Kernels over cells loop over ids (grid-stride): the cell count is known on
+// the device only, and a grid of about 2n threads covers it in one round for
+// the usual trees (cells ~1.3-2 per body) without launching for the capacity.
 __global__ void k_link(csgd_t dd, DevScalars *sc, const unsigned long long *__restrict__ key,
                        const unsigned long long *__restrict__ ext)
 {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= min(sc->n_nodes, dd.node_cap))
+    const int nn = sc->n_nodes;
+    if (nn > dd.node_cap)
         return;
-    NodeLink l = dd.link[id];
-    if (l.parent < 0 || l.parent >= dd.node_cap || sc->n_nodes > dd.node_cap)
-        return;
-    int dg = digit_at(key, ext, l.first, l.level - 1);
-    dd.child[8 * (size_t)l.parent + dg] = id;
-    atomicAdd(&dd.nchild[l.parent], 1);
+    for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < nn; id += gridDim.x * blockDim.x) {
+        NodeLink l = dd.link[id];
+        if (l.parent < 0 || l.parent >= dd.node_cap)
+            continue;
+        int dg = digit_at(key, ext, l.first, l.level - 1);
+        dd.child[8 * (size_t)l.parent + dg] = id;
+        atomicAdd(&dd.nchild[l.parent], 1);
+    }
 }
 
 // Bottom-up moments: one thread per leaf (sorted positions that start one);
@@ -684,7 +689,7 @@ __device__ __forceinline__ void put_moments(const csgd_t &dd, int node, double s
 // A single-body leaf keeps the body's position exactly (the reference's leaf
 // centre); bodies that coincide to depth 64 share one leaf, in caller index
 // order, so the two smallest caller indices of a cell are its first two.
-constexpr int MOM_DIRECT = 32;
+constexpr int MOM_DIRECT = 16;
 
 template <bool EXPORT>
 __device__ __forceinline__ void moments_climb(const csgd_t &dd, int node, double sx, double sy,
@@ -742,14 +747,12 @@ __device__ __forceinline__ void moments_climb(const csgd_t &dd, int node, double
 }
 
 template <bool EXPORT>
-__global__ void k_moments(csgd_t dd, DevScalars *sc, const double *__restrict__ x,
-                          const double *__restrict__ y, const double *__restrict__ z,
-                          const double *__restrict__ m, const int *__restrict__ perm)
+__device__ __forceinline__ void moments_cell(const csgd_t &dd, int id, const double *__restrict__ x,
+                                             const double *__restrict__ y,
+                                             const double *__restrict__ z,
+                                             const double *__restrict__ m,
+                                             const int *__restrict__ perm)
 {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nn = sc->n_nodes;
-    if (id >= nn || nn > dd.node_cap || sc->n_alive == 0)
-        return;
     const NodeLink l = dd.link[id];
     const bool leaf = dd.nchild[id] == 0;
     if ((!leaf && l.count > MOM_DIRECT) || l.count < 1)
@@ -796,6 +799,18 @@ __global__ void k_moments(csgd_t dd, DevScalars *sc, const double *__restrict__ 
     moments_climb<EXPORT>(dd, id, sx, sy, sz, M, mi);
 }
 
+template <bool EXPORT>
+__global__ void k_moments(csgd_t dd, DevScalars *sc, const double *__restrict__ x,
+                          const double *__restrict__ y, const double *__restrict__ z,
+                          const double *__restrict__ m, const int *__restrict__ perm)
+{
+    const int nn = sc->n_nodes;
+    if (nn > dd.node_cap || sc->n_alive == 0)
+        return;
+    for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < nn; id += gridDim.x * blockDim.x)
+        moments_cell<EXPORT>(dd, id, x, y, z, m, perm);
+}
+
 // FP32 neighbour-search record of one cell (see NodeS32).
 __device__ __forceinline__ void write_s32(const csgd_t &dd, int id, double cx, double cy,
                                           double cz, double hs, int body, int next)
@@ -830,24 +845,26 @@ __global__ void k_geometry(csgd_t dd, DevScalars *sc, const DevRoot *__restrict_
                            const unsigned long long *__restrict__ ext,
                            const int *__restrict__ sgid)
 {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= min(sc->n_nodes, dd.node_cap) || sc->n_nodes > dd.node_cap)
+    const int nn = sc->n_nodes;
+    if (nn > dd.node_cap)
         return;
-    NodeLink l = dd.link[id];
-    const DevRoot *r = &roots[sc->n_alive > 0 ? sgid[l.first] : 0];
-    double cx = r->c0[0], cy = r->c0[1], cz = r->c0[2], hs = r->hs0;
-    for (int lev = 0; lev < l.level; lev++) {
-        int q = digit_at(key, ext, l.first, lev);
-        double ox = (q & 1) ? 0.5 : -0.5;
-        double oy = (q & 2) ? -0.5 : 0.5;
-        double oz = (q & 4) ? -0.5 : 0.5;
-        cx = cx + ox * hs;
-        cy = cy + oy * hs;
-        cz = cz + oz * hs;
-        hs = hs * 0.5;
+    for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < nn; id += gridDim.x * blockDim.x) {
+        NodeLink l = dd.link[id];
+        const DevRoot *r = &roots[sc->n_alive > 0 ? sgid[l.first] : 0];
+        double cx = r->c0[0], cy = r->c0[1], cz = r->c0[2], hs = r->hs0;
+        for (int lev = 0; lev < l.level; lev++) {
+            int q = digit_at(key, ext, l.first, lev);
+            double ox = (q & 1) ? 0.5 : -0.5;
+            double oy = (q & 2) ? -0.5 : 0.5;
+            double oz = (q & 4) ? -0.5 : 0.5;
+            cx = cx + ox * hs;
+            cy = cy + oy * hs;
+            cz = cz + oz * hs;
+            hs = hs * 0.5;
+        }
+        dd.geo[id] = make_double4(cx, cy, cz, hs);
+        write_s32(dd, id, cx, cy, cz, hs, dd.w64[id].body, dd.w64[id].next);
     }
-    dd.geo[id] = make_double4(cx, cy, cz, hs);
-    write_s32(dd, id, cx, cy, cz, hs, dd.w64[id].body, dd.w64[id].next);
 }
 
 // ---- export in the reference's allocation order --------------------------
@@ -1145,6 +1162,13 @@ static int order_bodies(csgd_t *d)
     return csgd_check(d, cudaGetLastError());
 }
 
+// Threads for the grid-stride kernels over cells.
+static long long cell_threads(const csgd_t *d)
+{
+    const long long t = 2LL * d->n + 64;
+    return t < d->node_cap ? t : d->node_cap;
+}
+
 extern "C" int csgd_build_tree(csgd_t *d, int geometry)
 {
     const int n = d->n;
@@ -1165,8 +1189,7 @@ extern "C" int csgd_build_tree(csgd_t *d, int geometry)
         return rc;
     // d->cnt (the counts, consumed by the scan) now holds each position's leaf
     { k_nodes<<<g, B, 0, s>>>(*d, sc, d->roots, d->key, d->ext, d->sgid, d->lcp, d->base, d->perm, d->cnt); d->launches++; }
-    const int gn = csgd_grid(d->node_cap, B);
-    // nodes beyond n_nodes exit at once; the grid covers the capacity
+    const int gn = csgd_grid(cell_threads(d), B);
     { k_link<<<gn, B, 0, s>>>(*d, sc, d->key, d->ext); d->launches++; }
     if (d->export_order)
         { k_moments<true><<<gn, B, 0, s>>>(*d, sc, d->x, d->y, d->z, d->m, d->perm); d->launches++; }
@@ -1197,7 +1220,7 @@ extern "C" int csgd_export_to(csgd_t *d, OctreeNode *dst, int capacity)
     DevScalars *sc = d->sc;
     const int B = 256;
     if (!d->geometry_valid) {
-        const int gn = csgd_grid(d->node_cap, B);
+        const int gn = csgd_grid(cell_threads(d), B);
         { k_geometry<<<gn, B, 0, s>>>(*d, sc, d->roots, d->key, d->ext, d->sgid); d->launches++; }
         d->geometry_valid = 1;
     }
