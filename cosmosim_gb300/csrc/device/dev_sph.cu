@@ -23,22 +23,25 @@ constexpr int SPH_WARPS = SPH_THREADS / CSG_WARP;
 constexpr double GAMMA = 5.0 / 3.0;
 constexpr double PI_D = 3.14159265358979323846;
 
-// M4 cubic spline, src/sph.c:11-25
-__device__ __forceinline__ double kernel_W(double r, double h)
+// M4 cubic spline W(r, h), src/sph.c:11-25, with its normalisation 8/(pi h^3)
+// computed by the caller once per gas body (the same expression, so the same
+// value): one division fewer per pair.
+__device__ __forceinline__ double kernel_W_norm(double r, double h, double norm)
 {
     if (h < 1e-10)
         return 0.0;
     double q = r / h;
     if (q > 1.0)
         return 0.0;
-    double norm = 8.0 / (PI_D * h * h * h);
     if (q <= 0.5)
         return norm * (1.0 - 6.0 * q * q + 6.0 * q * q * q);
     double t = 1.0 - q;
     return norm * 2.0 * t * t * t;
 }
 
-// its radial derivative, src/sph.c:27-41
+__device__ __forceinline__ double kernel_norm(double h) { return 8.0 / (PI_D * h * h * h); }
+
+// the kernel's radial derivative dW/dr(r, h), src/sph.c:27-41
 __device__ __forceinline__ double kernel_dWdr(double r, double h)
 {
     if (h < 1e-10)
@@ -67,6 +70,7 @@ struct SphArgs {
     int *nb_count; // neighbours per gas body
     int *relist;   // per gas body: the density pass changed h (search again)
     int reuse;     // force pass: keep the density lists of bodies with relist 0
+    int density;   // density pass (the lists also store 8/(pi h^3) in pr2)
     double *pr2, *cs; // per-body force terms (k_sph_body_terms)
     double *term;     // pair terms, 3 planes of 128 slots x stride (slot-major)
     int n, node_cap, stride;
@@ -204,8 +208,11 @@ __device__ __forceinline__ void list_one(const SphArgs &a, int k, int lane)
         const int jump = __reduce_max_sync(0xffffffffu, (unsigned)max(fail_next, 0));
         cur = max(cur + CSG_WARP, jump); // strictly increases: the loop ends
     }
-    if (lane == 0)
+    if (lane == 0) {
         a.nb_count[k] = found;
+        if (a.density) // its pairs need 8/(pi h^3) of this body
+            a.pr2[i] = h < 1e-10 ? 0.0 : kernel_norm(h);
+    }
 }
 
 __global__ void __launch_bounds__(SPH_THREADS) k_sph_lists(SphArgs a)
@@ -250,7 +257,7 @@ __global__ void __launch_bounds__(SPH_THREADS) k_sph_density_terms(SphArgs a)
         double dy = a.y[i] - a.y[j];
         double dz = a.z[i] - a.z[j];
         double r = sqrt(dx * dx + dy * dy + dz * dz);
-        a.term[stride * s + k] = a.m[j] * kernel_W(r, a.h[i]);
+        a.term[stride * s + k] = a.m[j] * kernel_W_norm(r, a.h[i], a.pr2[i]);
     }
 }
 
@@ -466,6 +473,7 @@ SphArgs make_args(csgd_t *d)
     a.nb_count = d->nb_count;
     a.relist = d->sph_relist;
     a.reuse = 0;
+    a.density = 0;
     a.pr2 = d->pr2;
     a.cs = d->cs;
     a.term = d->sph_term;
@@ -577,6 +585,7 @@ static int sph_pass(csgd_t *d, int forces, bool sums = true, bool reuse = false)
         return rc;
     SphArgs a = make_args(d);
     a.reuse = (forces && reuse) ? 1 : 0;
+    a.density = forces ? 0 : 1;
     const int g = csgd_grid(d->n, SPH_THREADS);
     // one warp per gas body for the lists, warps striding over the gas bodies
     int gl = csgd_grid((long long)d->n * CSG_WARP, SPH_THREADS);
