@@ -557,14 +557,31 @@ __device__ __forceinline__ void q64_eval(const WalkArgs &a, const int *q, int la
 {
     count = max(count, 0);
     const int kmax = (int)__reduce_max_sync(0xffffffffu, (unsigned)count);
-    for (int s = 0; s < kmax; s++) {
-        if (s < count) {
-            const int node = q[((head + s) & (Q64 - 1)) * CSG_WARP + lane];
-            const double2 c01 = __ldg((const double2 *)&a.w64[node]);     // cx, cy
-            const double2 c23 = __ldg((const double2 *)&a.w64[node] + 1); // cz, m
-            const double dx = c01.x - px, dy = c01.y - py, dz = c23.x - pz;
+    for (int s = 0; s < kmax; s += 2) { // two entries: both loads in flight together
+        const bool v0 = s < count, v1 = s + 1 < count;
+        const int n0 = v0 ? q[((head + s) & (Q64 - 1)) * CSG_WARP + lane] : 0;
+        const int n1 = v1 ? q[((head + s + 1) & (Q64 - 1)) * CSG_WARP + lane] : 0;
+        double2 a01 = make_double2(0.0, 0.0), a23 = a01, b01 = a01, b23 = a01;
+        if (v0) {
+            a01 = __ldg((const double2 *)&a.w64[n0]);     // cx, cy
+            a23 = __ldg((const double2 *)&a.w64[n0] + 1); // cz, m
+        }
+        if (v1) {
+            b01 = __ldg((const double2 *)&a.w64[n1]);
+            b23 = __ldg((const double2 *)&a.w64[n1] + 1);
+        }
+        if (v0) {
+            const double dx = a01.x - px, dy = a01.y - py, dz = a23.x - pz;
             const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, a.eps2)));
-            const double f = m_inv_r3_q(c23.y, r2);
+            const double f = m_inv_r3_q(a23.y, r2);
+            sx = fma(f, dx, sx);
+            sy = fma(f, dy, sy);
+            sz = fma(f, dz, sz);
+        }
+        if (v1) {
+            const double dx = b01.x - px, dy = b01.y - py, dz = b23.x - pz;
+            const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, a.eps2)));
+            const double f = m_inv_r3_q(b23.y, r2);
             sx = fma(f, dx, sx);
             sy = fma(f, dy, sy);
             sz = fma(f, dz, sz);
