@@ -646,6 +646,183 @@ __global__ void __launch_bounds__(WARPS * CSG_WARP, w64q_min_blocks(WARPS, PERSI
         add_hits(a, st);
 }
 
+// FP64 walk, producer/consumer form. Each task has two warps: the producer
+// walks the tree (walk_cells, the FP32 decisions) and appends each lane's
+// accepted cells to that lane's ring in shared memory; the consumer evaluates
+// the rings in FP64, in the order the cells were accepted, so its sums are
+// the queued walk's bit for bit. The traversal (FP32/ALU pipes) and the
+// evaluation (FP64 pipe) then overlap on every SM instead of alternating in
+// one warp. The warps hand over through per-lane head and tail counters in
+// shared memory; every wait polls with a sleep and gives up after WS_POLLS
+// polls (recording CSG_ERR_DEVICE_WAIT, then both warps leave the task).
+constexpr int WS_RING = 128;   // ring slots per lane (power of two)
+constexpr int WS_PAIRS = 2;    // producer/consumer pairs per block
+constexpr int WS_BATCH = 16;   // dense batch the consumer waits for
+constexpr int WS_PUBLISH = 4;  // the producer publishes its tails every few steps
+constexpr int WS_POLLS = 1 << 22;
+
+struct WsShared {
+    int ring[WS_RING * CSG_WARP]; // slot-major: ring[slot * 32 + lane]
+    int tail[CSG_WARP];           // published by the producer
+    int head[CSG_WARP];           // published by the consumer
+    int done;                     // producer finished (tails final)
+    int broken;                   // a wait gave up: both warps leave
+};
+
+__device__ __forceinline__ int ws_load(const volatile int *p) { return *p; }
+
+template <bool STATS, bool EMPTY>
+__device__ __forceinline__ void ws_produce(const WalkArgs &a, NodeW32 *win, WsShared &sh,
+                                           const TaskRange &tr, WalkStats &st)
+{
+    const int lane = threadIdx.x & 31;
+    const bool valid = lane < tr.count;
+    const int me = valid ? a.perm[tr.pos0 + lane] : -1;
+    const BodyPos b = body_pos(a, me, valid);
+    int tail = 0, head_seen = 0, steps = 0;
+    bool broken = false;
+    auto publish = [&]() {
+        __threadfence_block(); // ring entries before the tail
+        ((volatile int *)sh.tail)[lane] = tail;
+    };
+    walk_cells<EMPTY>(a, win, tr.root, tr.end, me, valid, b,
+        [&](bool take, const Cell &, float, float, float, float, int cur) {
+            // room for one entry on every lane that takes (warp-uniform wait)
+            bool full = take && tail - head_seen >= WS_RING;
+            if (__any_sync(0xffffffffu, full)) {
+                publish();
+                for (int k = 0; k < WS_POLLS; k++) {
+                    head_seen = ws_load(&sh.head[lane]);
+                    full = take && tail - head_seen >= WS_RING;
+                    if (!__any_sync(0xffffffffu, full) || ws_load(&sh.broken))
+                        break;
+                    __nanosleep(64);
+                }
+                __threadfence_block(); // heads read before slots are overwritten
+                if (__any_sync(0xffffffffu, full)) { // gave up (or the consumer did)
+                    if (lane == 0) {
+                        dev_fail(a.sc, CSG_ERR_DEVICE_WAIT);
+                        ((volatile int *)&sh.broken)[0] = 1;
+                    }
+                    broken = true;
+                }
+            }
+            if (take && !broken) {
+                sh.ring[(tail & (WS_RING - 1)) * CSG_WARP + lane] = cur;
+                tail++;
+                if (STATS)
+                    st.hits++;
+            }
+        },
+        [&](int, bool active) {
+            if (STATS) {
+                st.steps++;
+                st.active += active;
+            }
+            if (++steps == WS_PUBLISH) {
+                steps = 0;
+                publish();
+            }
+        });
+    publish();
+    __syncwarp();
+    if (lane == 0)
+        ((volatile int *)&sh.done)[0] = 1; // after every lane's final tail (fenced above)
+}
+
+__device__ __forceinline__ void ws_consume(const WalkArgs &a, WsShared &sh, const TaskRange &tr)
+{
+    const int lane = threadIdx.x & 31;
+    const bool valid = lane < tr.count;
+    const int me = valid ? a.perm[tr.pos0 + lane] : -1;
+    const double px = valid ? a.x[me] : 0.0, py = valid ? a.y[me] : 0.0,
+                 pz = valid ? a.z[me] : 0.0;
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    int head = 0, polls = 0;
+    while (true) {
+        const bool done = ws_load(&sh.done) != 0; // read before the tails: they are final then
+        __threadfence_block();
+        const int tail = ws_load(&sh.tail[lane]);
+        __threadfence_block(); // the tail before the entries it covers
+        const int avail = valid ? tail - head : 0;
+        const int amin = (int)__reduce_min_sync(0xffffffffu, (unsigned)(valid ? avail : INT_MAX));
+        const int amax = (int)__reduce_max_sync(0xffffffffu, (unsigned)avail);
+        int take = 0;
+        if (amin >= WS_BATCH)
+            take = amin; // dense: every lane has work
+        else if (done || amax >= WS_RING - WS_BATCH)
+            take = -1; // the rest (done) or relief for a lane whose ring is nearly full
+        if (take != 0) {
+            const int k = take > 0 ? (valid ? take : 0) : min(avail, done ? avail : WS_BATCH);
+            q64_eval<WS_RING>(a, sh.ring, lane, head, k, px, py, pz, sx, sy, sz);
+            __threadfence_block(); // entries read before the head is published
+            ((volatile int *)sh.head)[lane] = head;
+            polls = 0;
+            if (done && __all_sync(0xffffffffu, !valid || head == tail))
+                break;
+            continue;
+        }
+        if (ws_load(&sh.broken))
+            return;
+        if (++polls >= WS_POLLS) {
+            if (lane == 0) {
+                dev_fail(a.sc, CSG_ERR_DEVICE_WAIT);
+                ((volatile int *)&sh.broken)[0] = 1;
+            }
+            return;
+        }
+        __nanosleep(64);
+    }
+    if (valid) {
+        a.ax[me] = a.G * sx;
+        a.ay[me] = a.G * sy;
+        a.az[me] = a.G * sz;
+    }
+}
+
+template <bool STATS, bool EMPTY>
+__global__ void __launch_bounds__(2 * WS_PAIRS * CSG_WARP, 24 / (2 * WS_PAIRS)) k_walk64ws(WalkArgs a)
+{
+    __shared__ WsShared sh_all[WS_PAIRS];
+    __shared__ NodeW32 win_all[WS_PAIRS][CSG_WARP];
+    const int warp = threadIdx.x >> 5, pair = warp >> 1, lane = threadIdx.x & 31;
+    WsShared &sh = sh_all[pair];
+    const int nn = a.sc->n_nodes;
+    if (nn > a.node_cap || nn < 1)
+        return;
+    const int t = blockIdx.x * WS_PAIRS + pair;
+    TaskRange tr{0, 0, 0, 0};
+    bool ok = t < a.sc->n_tasks;
+    if (ok) {
+        const WalkTask w = a.tasks[t];
+        const DevRoot &r = a.roots[w.gal];
+        tr = TaskRange{w.pos0, w.count, r.root, r.end};
+        if (tr.root < 0 || tr.end > nn || tr.root >= tr.end) {
+            if ((warp & 1) == 0 && lane == 0)
+                dev_fail(a.sc, CSG_ERR_WALK_LIMIT);
+            ok = false;
+        }
+    }
+    if (ok && (warp & 1) == 0) {
+        sh.tail[lane] = 0;
+        sh.head[lane] = 0;
+        if (lane == 0) {
+            sh.done = 0;
+            sh.broken = 0;
+        }
+    }
+    __syncthreads(); // every thread: counters set before either warp of any pair starts
+    if (!ok)
+        return; // both warps of the pair
+    WalkStats st;
+    if ((warp & 1) == 0)
+        ws_produce<STATS, EMPTY>(a, win_all[pair], sh, tr, st);
+    else
+        ws_consume(a, sh, tr);
+    if (STATS && (warp & 1) == 0)
+        add_hits(a, st);
+}
+
 // Dead bodies get a = 0 (src/octree.c:226-230); alive ones are overwritten by
 // the walk.
 // Also rewinds the task counter of the persistent walks.
@@ -754,6 +931,10 @@ WalkArgs walk_args(csgd_t *d, const csgd_force_params *p)
             K<false, false, W, false><<<grid, W * CSG_WARP, 0, s>>>(a);                     \
     } while (0)
 
+#ifndef CSG_WALK64_WS
+#define CSG_WALK64_WS 1
+#endif
+
 // One walk launch with the state's launch shape.
 void launch_walk(csgd_t *d, const WalkArgs &a, int precision, int exact)
 {
@@ -786,6 +967,18 @@ void launch_walk(csgd_t *d, const WalkArgs &a, int precision, int exact)
             CSG_LAUNCH_WALK(k_walk32, 4, grid, s, b);
         else
             CSG_LAUNCH_WALK(k_walk32, 8, grid, s, b);
+    } else if (CSG_WALK64_WS && !persist) {
+        const long long tasks = (long long)d->n / CSG_WARP + d->n_gal + 1; // >= n_tasks
+        const int gw = (int)((tasks + WS_PAIRS - 1) / WS_PAIRS);
+        const int blocks = 2 * WS_PAIRS * CSG_WARP;
+        if (stats && empty)
+            k_walk64ws<true, true><<<gw, blocks, 0, s>>>(b);
+        else if (stats)
+            k_walk64ws<true, false><<<gw, blocks, 0, s>>>(b);
+        else if (empty)
+            k_walk64ws<false, true><<<gw, blocks, 0, s>>>(b);
+        else
+            k_walk64ws<false, false><<<gw, blocks, 0, s>>>(b);
     } else {
         if (W == 4)
             CSG_LAUNCH_WALK(k_walk64q, 4, grid, s, b);
