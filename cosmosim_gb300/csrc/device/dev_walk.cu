@@ -14,10 +14,11 @@
 // The next 32 cells in preorder are staged per warp in shared memory with one
 // coalesced load, and re-staged only when the cursor leaves that window.
 //
-// FP64 walk: the drop-in precision (k_walk64q). Openings decided as in the
-//   FP32 walk (equal to the reference's FP64 rounding); interactions queued
-//   and evaluated densely in FP64, 1/r^3 from an FP32 rsqrt seed refined to
-//   full FP64 accuracy. k_walk64<EXACT=true> instead uses the reference's own
+// FP64 walk: the drop-in precision (k_walk64ws; k_walk64q for persistent
+//   launch shapes). Openings decided as in the FP32 walk (equal to the
+//   reference's FP64 rounding); interactions queued and evaluated densely in
+//   FP64 — by a second warp per task in k_walk64ws — with 1/r^3 from an FP32
+//   rsqrt seed refined to full FP64 accuracy. k_walk64<EXACT=true> instead uses the reference's own
 //   operation sequence per step (1/(r2*sqrt(r2)), no fused multiply-add) —
 //   bit-identical results on the reference's own tree; used by parity tests.
 // FP32-mixed walk: positions and centres as float hi/lo pairs (differences
