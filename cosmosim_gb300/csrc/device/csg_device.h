@@ -73,11 +73,11 @@ int csgd_autotune_walk(csgd_t *d, const csgd_force_params *p, int reps, CsgWalkS
 /* Body array-of-structs <-> device SoA (host buffers may be pageable). */
 int csgd_upload_bodies(csgd_t *d, const Body *host, int n);
 int csgd_download_bodies(csgd_t *d, Body *host, int n);
-/* Download of what a leapfrog step or an SPH pass changes (x..az, density,
+/* Download of what a leapfrog step changes (x..az, and with sph != 0 density,
    pressure, internal energy, smoothing length): into a mapped (pinned) host
    array those fields are written directly and the caller's other fields are
    left alone; any other host array gets csgd_download_bodies. */
-int csgd_download_step_fields(csgd_t *d, Body *host, int n);
+int csgd_download_step_fields(csgd_t *d, Body *host, int n, int sph);
 /* Refreshes the device Body staging from the SoA fields (no copy to the host),
    and the SoA fields from the staging. */
 int csgd_pack_aos(csgd_t *d);

@@ -597,21 +597,23 @@ extern "C" int csgd_pack_aos(csgd_t *d)
 }
 
 // Download into a mapped (pinned) host Body array: only the fields a step or
-// an SPH pass can change (x..az at word 0, density..smoothing_h at word 17 of
-// the 21-word record) are written, straight from the SoA arrays; mass, type
-// and the quasar fields of the caller's records stay as they are.
+// an SPH pass can change (x..az at word 0, and with SPH density..smoothing_h
+// at word 17 of the 21-word record) are written, straight from the SoA
+// arrays; mass, type and the quasar fields of the caller's records stay as
+// they are.
 __global__ void k_download_direct(double *__restrict__ hb, int n, const double *__restrict__ x,
                                   const double *__restrict__ y, const double *__restrict__ z,
                                   const double *__restrict__ vx, const double *__restrict__ vy,
                                   const double *__restrict__ vz, const double *__restrict__ ax,
                                   const double *__restrict__ ay, const double *__restrict__ az,
                                   const double *__restrict__ rho, const double *__restrict__ P,
-                                  const double *__restrict__ u, const double *__restrict__ h)
+                                  const double *__restrict__ u, const double *__restrict__ h,
+                                  int words)
 {
-    const long long total = 13LL * n;
+    const long long total = (long long)words * n;
     for (long long f = (long long)blockIdx.x * blockDim.x + threadIdx.x; f < total;
          f += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(f / 13), j = (int)(f - 13LL * i);
+        const int i = (int)(f / words), j = (int)(f - (long long)words * i);
         const double *src[13] = {x, y, z, vx, vy, vz, ax, ay, az, rho, P, u, h};
         hb[21LL * i + (j < 9 ? j : j + 8)] = src[j][i];
     }
@@ -632,13 +634,15 @@ extern "C" int csgd_download_bodies(csgd_t *d, Body *host, int n)
     return csgd_check(d, cudaGetLastError());
 }
 
-extern "C" int csgd_download_step_fields(csgd_t *d, Body *host, int n)
+extern "C" int csgd_download_step_fields(csgd_t *d, Body *host, int n, int sph)
 {
     static_assert(sizeof(Body) == 168, "21 words per Body");
     double *hv = (double *)csgd_host_view(host);
     if (!hv || n <= 0 || n > d->n)
         return csgd_download_bodies(d, host, n);
-    { k_download_direct<<<4 * d->num_sms, 256, 0, d->stream>>>(hv, n, d->x, d->y, d->z, d->vx, d->vy, d->vz, d->ax, d->ay, d->az, d->rho, d->P, d->u, d->h); d->launches++; }
+    // without SPH a step leaves density..smoothing_h as they were
+    const int words = sph ? 13 : 9;
+    { k_download_direct<<<4 * d->num_sms, 256, 0, d->stream>>>(hv, n, d->x, d->y, d->z, d->vx, d->vy, d->vz, d->ax, d->ay, d->az, d->rho, d->P, d->u, d->h, words); d->launches++; }
     return csgd_check(d, cudaGetLastError());
 }
 

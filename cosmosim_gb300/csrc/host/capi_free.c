@@ -176,7 +176,7 @@ CSG_EXPORT void integrator_step(Body *bodies, int n, double dt, double G, double
     if (!rc && !pool_view)
         rc = store_pool(d, pool, NULL, n);
     if (!rc)
-        rc = csgd_download_step_fields(d, bodies, n);
+        rc = csgd_download_step_fields(d, bodies, n, sph_enabled ? 1 : 0);
     if (!rc)
         rc = csgd_sync(d);
     csg_thread_set_error(rc);
