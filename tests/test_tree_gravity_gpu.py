@@ -205,12 +205,15 @@ def test_oracle_agrees_on_random_trees(lib, orc):
         assert np.all(fields(fb)[~alive] == 0.0)
 
 
-def test_interaction_count_matches_oracle(lib, orc):
+@pytest.mark.parametrize("precision", [0, 1])
+def test_interaction_count_matches_oracle(lib, orc, precision):
+    """Both walks (FP64 producer/consumer, FP32-mixed) give every body the
+    reference's interaction set: the totals equal the oracle's count."""
     from cosmosim_gb300.lib import Sim
 
     g = golden("disk_3000.npz")
     b = g["bodies"]
-    s = Sim.from_bodies(b, softening=0.01, theta=0.5)
+    s = Sim.from_bodies(b, softening=0.01, theta=0.5, precision=precision)
     s.enable_stats(True)
     s.gravity_async()
     got = s.interactions()
