@@ -1133,7 +1133,9 @@ static int order_bodies(csgd_t *d)
     const int B = 256;
     const int G = d->n_gal;
     { k_reset<<<1, 256, 0, s>>>(sc, d->roots, G); d->launches++; }
-    int gb = min(csgd_grid(n, B), 152 * 8);
+    // few blocks: each warp flushes its running box with atomics on the same
+    // words, so fewer warps contend less (4 blocks per SM keep HBM busy)
+    int gb = min(csgd_grid(n, B), 4 * d->num_sms);
     { k_bbox<<<gb > 0 ? gb : 1, B, 0, s>>>(d->x, d->y, d->z, d->m, d->gid, n, d->roots); d->launches++; }
     { k_root<<<1, 256, 0, s>>>(sc, d->roots, G); d->launches++; }
     if (n > 0)
