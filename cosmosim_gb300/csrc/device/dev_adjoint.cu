@@ -110,7 +110,9 @@ __global__ void k_adj_forces(const int *__restrict__ offs, const int *__restrict
             const double4 c = xm[ids[k]];
             const double dx = c.x - px, dy = c.y - py, dz = c.z - pz;
             const double r2 = dx * dx + dy * dy + dz * dz + eps2;
-            const double f = G * c.w / (r2 * sqrt(r2));
+            double inv3, inv5;
+            inv_r3_r5(r2, inv3, inv5);
+            const double f = G * c.w * inv3;
             sx += f * dx;
             sy += f * dy;
             sz += f * dz;
@@ -148,8 +150,8 @@ __global__ void k_adj_jt(const int *__restrict__ offs, const int *__restrict__ i
             const double4 q = xm[c];
             const double dx = q.x - px, dy = q.y - py, dz = q.z - pz;
             const double r2 = dx * dx + dy * dy + dz * dz + eps2;
-            const double inv3 = 1.0 / (r2 * sqrt(r2));
-            const double inv5 = inv3 / r2;
+            double inv3, inv5;
+            inv_r3_r5(r2, inv3, inv5);
             const double gm = G * q.w;
             const double dm = 3.0 * (dx * ux + dy * uy + dz * uz) * inv5;
             const double wx = gm * (ux * inv3 - dm * dx);

@@ -224,3 +224,38 @@ int csg_scan_exclusive(csgd_t *d, const int *in, int *out, int n, const int *cou
 
 // ---- device error codes written to DevScalars::err ----
 __device__ __forceinline__ void dev_fail(DevScalars *sc, int code) { atomicCAS(&sc->err, 0, code); }
+
+// FP32 value of a positive double whose exponent lies in FP32's normal range,
+// from its bits alone (exponent rebased from 1023 to 127, mantissa truncated
+// to 23 bits: relative error < 2^-23), and the exact double of a positive
+// normal float. Integer operations only: conversion instructions would run on
+// the FP64 pipe, the bottleneck of the FP64 force kernels on this GPU.
+__device__ __forceinline__ float f32_from_f64_bits(long long b)
+{
+    return __int_as_float((int)((b >> 29) - (896LL << 23)));
+}
+__device__ __forceinline__ double f64_from_f32_bits(float f)
+{
+    return __longlong_as_double(((long long)__float_as_int(f) + (896LL << 23)) << 29);
+}
+
+// r^-3 and r^-5 for r2 = r^2 without divisions: y0 = FP32 rsqrt seed (rel.
+// error < 2^-21), e = 1 - r2 y0^2 (one fused multiply-add, y0^2 exact), then
+// r^-2 = y0^2 (1 + e + e^2) and r^-3 = y0^3 (1 + 3/2 e + 15/8 e^2) (the
+// binomial series; the first omitted terms are < 2^-60). Outside
+// 2^-99 <= r2 < 2^100 the plain expressions.
+__device__ __forceinline__ void inv_r3_r5(double r2, double &inv3, double &inv5)
+{
+    const long long bits = __double_as_longlong(r2);
+    if ((unsigned long long)((bits >> 52) - 924) <= 198ull) {
+        const double y0 = f64_from_f32_bits(rsqrtf(f32_from_f64_bits(bits)));
+        const double y0sq = y0 * y0;
+        const double e = fma(-r2, y0sq, 1.0);
+        inv3 = (y0sq * y0) * fma(e, fma(1.875, e, 1.5), 1.0);
+        const double inv2 = fma(y0sq, fma(e, e, e), y0sq);
+        inv5 = inv3 * inv2;
+        return;
+    }
+    inv3 = 1.0 / (r2 * sqrt(r2));
+    inv5 = inv3 / r2;
+}

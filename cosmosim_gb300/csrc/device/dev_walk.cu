@@ -256,20 +256,6 @@ __global__ void __launch_bounds__(8 * CSG_WARP) k_walk64(WalkArgs a)
         add_hits(a, st);
 }
 
-// FP32 value of a positive double whose exponent lies in FP32's normal range,
-// from its bits alone (exponent rebased from 1023 to 127, mantissa truncated
-// to 23 bits: relative error < 2^-23), and the exact double of a positive
-// normal float. Integer operations only: conversion instructions would run on
-// the FP64 pipe, the walk's bottleneck on this GPU.
-__device__ __forceinline__ float f32_from_f64_bits(long long b)
-{
-    return __int_as_float((int)((b >> 29) - (896LL << 23)));
-}
-__device__ __forceinline__ double f64_from_f32_bits(float f)
-{
-    return __longlong_as_double(((long long)__float_as_int(f) + (896LL << 23)) << 29);
-}
-
 // m/r^3 for the queued FP64 walk, with few FP64 operations (the FP64 pipe
 // is the walk's bottleneck on this GPU): y0 = FP32 rsqrt seed (rel. error
 // < 2^-21), y0^2 exact in FP64, e = 1 - r2*y0^2 by one fused multiply-add,
@@ -846,13 +832,13 @@ __global__ void k_zero_acc(const double *__restrict__ m, double *ax, double *ay,
 // reference's depth-first order (the FP64 walk's interaction set), written
 // per caller index: ids[offs[i] .. offs[i] + counts[i]). FILL = false counts,
 // FILL = true writes (offs from an exclusive scan of the counts).
-template <bool FILL>
-__global__ void __launch_bounds__(8 * CSG_WARP) k_walk_lists(WalkArgs a, int *counts,
+template <bool FILL, int WARPS>
+__global__ void __launch_bounds__(WARPS * CSG_WARP) k_walk_lists(WalkArgs a, int *counts,
                                                              const int *offs, int *ids, int cap)
 {
-    __shared__ NodeW32 win_all[8][CSG_WARP];
+    __shared__ NodeW32 win_all[WARPS][CSG_WARP];
     NodeW32 *win = win_all[threadIdx.x >> 5];
-    for_each_task<8, false>(a, [&](const TaskRange &tr) {
+    for_each_task<WARPS, false>(a, [&](const TaskRange &tr) {
         const int lane = threadIdx.x & 31;
         const bool valid = lane < tr.count;
         const int me = valid ? a.perm[tr.pos0 + lane] : -1;
@@ -1029,11 +1015,21 @@ extern "C" int csgd_walk_lists(csgd_t *d, const csgd_force_params *p, int *count
     WalkArgs a = walk_args(d, p);
     a.group = 0;
     const long long tasks = (long long)n / CSG_WARP + d->n_gal + 1;
-    const int grid = (int)((tasks + 7) / 8);
-    if (fill)
-        { k_walk_lists<true><<<grid, 8 * CSG_WARP, 0, d->stream>>>(a, counts, offs, ids, cap); d->launches++; }
-    else
-        { k_walk_lists<false><<<grid, 8 * CSG_WARP, 0, d->stream>>>(a, counts, offs, ids, cap); d->launches++; }
+    // few tasks (the adjoint's 10k bodies are ~313): 2-warp blocks spread them
+    // over every SM instead of crowding 8 per SM on a quarter of the GPU
+    if (tasks < 8LL * d->num_sms) {
+        const int grid = (int)((tasks + 1) / 2);
+        if (fill)
+            { k_walk_lists<true, 2><<<grid, 2 * CSG_WARP, 0, d->stream>>>(a, counts, offs, ids, cap); d->launches++; }
+        else
+            { k_walk_lists<false, 2><<<grid, 2 * CSG_WARP, 0, d->stream>>>(a, counts, offs, ids, cap); d->launches++; }
+    } else {
+        const int grid = (int)((tasks + 7) / 8);
+        if (fill)
+            { k_walk_lists<true, 8><<<grid, 8 * CSG_WARP, 0, d->stream>>>(a, counts, offs, ids, cap); d->launches++; }
+        else
+            { k_walk_lists<false, 8><<<grid, 8 * CSG_WARP, 0, d->stream>>>(a, counts, offs, ids, cap); d->launches++; }
+    }
     return csgd_check(d, cudaGetLastError());
 }
 
