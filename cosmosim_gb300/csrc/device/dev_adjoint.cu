@@ -62,12 +62,24 @@ __global__ void k_adj_leaf_of(const NodeLink *__restrict__ link, const NodeW64 *
         leaf_of[l.first + q] = id;
 }
 
+// Position and mass of every sorted position (the member ranges of the cells
+// then read contiguous memory).
+__global__ void k_adj_gather(const int *__restrict__ perm, int n, const double *__restrict__ x,
+                             const double *__restrict__ y, const double *__restrict__ z,
+                             const double *__restrict__ m, double4 *__restrict__ sb)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n)
+        return;
+    const int j = perm[q];
+    sb[q] = make_double4(x[j], y[j], z[j], m[j]);
+}
+
 // Centre of mass and mass of every cell from the current positions of its
-// member bodies (sorted range [first, first+count)); one warp per cell.
-__global__ void k_adj_moments(const NodeLink *__restrict__ link, int nn, const int *__restrict__ perm,
-                              const double *__restrict__ x, const double *__restrict__ y,
-                              const double *__restrict__ z, const double *__restrict__ m,
-                              double4 *__restrict__ xm)
+// member bodies (sorted range [first, first+count) of sb); one warp per cell,
+// the lanes' partial sums combined by a fixed butterfly (deterministic).
+__global__ void k_adj_moments(const NodeLink *__restrict__ link, int nn,
+                              const double4 *__restrict__ sb, double4 *__restrict__ xm)
 {
     const int w = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
@@ -76,12 +88,11 @@ __global__ void k_adj_moments(const NodeLink *__restrict__ link, int nn, const i
     const NodeLink l = link[w];
     double M = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
     for (int q = l.first + lane; q < l.first + l.count; q += CSG_WARP) {
-        const int j = perm[q];
-        const double mj = m[j];
-        M += mj;
-        sx += mj * x[j];
-        sy += mj * y[j];
-        sz += mj * z[j];
+        const double4 b = sb[q];
+        M += b.w;
+        sx += b.w * b.x;
+        sy += b.w * b.y;
+        sz += b.w * b.z;
     }
     M = warp_sum(M);
     sx = warp_sum(sx);
@@ -370,6 +381,7 @@ struct csg_adjoint {
     double *jt = nullptr;       // 3n
     double *g = nullptr;        // 3 per cell
     double4 *xm = nullptr;      // per cell
+    double4 *sb = nullptr;      // per sorted position: x y z m (moment pass)
     int *counts = nullptr;      // n
     int *h_total = nullptr;     // pinned: list entries of the current substep
     std::vector<double> host_m, final_x, target;
@@ -494,7 +506,8 @@ int eval(csg_adjoint *a, Slot &s)
     if (rc)
         return rc;
     const int wb = AT / CSG_WARP;
-    { k_adj_moments<<<csgd_grid(nn, wb), AT, 0, st>>>(s.link, nn, s.perm, d->x, d->y, d->z, d->m, a->xm); d->launches++; }
+    { k_adj_gather<<<csgd_grid(n, AT), AT, 0, st>>>(s.perm, n, d->x, d->y, d->z, d->m, a->sb); d->launches++; }
+    { k_adj_moments<<<csgd_grid(nn, wb), AT, 0, st>>>(s.link, nn, a->sb, a->xm); d->launches++; }
     { k_adj_forces<<<csgd_grid(n, wb), AT, 0, st>>>(s.offs, s.ids, a->xm, d->x, d->y, d->z, d->m, n, a->G, a->eps * a->eps, d->ax, d->ay, d->az); d->launches++; }
     return csgd_check(d, cudaGetLastError());
 }
@@ -510,7 +523,8 @@ int eval_frozen(csg_adjoint *a, const Slot &s)
         return csgd_check(d, cudaGetLastError());
     }
     const int wb = AT / CSG_WARP;
-    { k_adj_moments<<<csgd_grid(s.nn, wb), AT, 0, st>>>(s.link, s.nn, s.perm, d->x, d->y, d->z, d->m, a->xm); d->launches++; }
+    { k_adj_gather<<<csgd_grid(n, AT), AT, 0, st>>>(s.perm, n, d->x, d->y, d->z, d->m, a->sb); d->launches++; }
+    { k_adj_moments<<<csgd_grid(s.nn, wb), AT, 0, st>>>(s.link, s.nn, a->sb, a->xm); d->launches++; }
     { k_adj_forces<<<csgd_grid(n, wb), AT, 0, st>>>(s.offs, s.ids, a->xm, d->x, d->y, d->z, d->m, n, a->G, a->eps * a->eps, d->ax, d->ay, d->az); d->launches++; }
     return csgd_check(d, cudaGetLastError());
 }
@@ -529,7 +543,8 @@ int jt_product(csg_adjoint *a, const Slot &s)
     }
     const int wb = AT / CSG_WARP;
     cudaMemsetAsync(a->g, 0, sizeof(double) * 3 * (size_t)s.nn, st);
-    { k_adj_moments<<<csgd_grid(s.nn, wb), AT, 0, st>>>(s.link, s.nn, s.perm, s.x, s.y, s.z, d->m, a->xm); d->launches++; }
+    { k_adj_gather<<<csgd_grid(n, AT), AT, 0, st>>>(s.perm, n, s.x, s.y, s.z, d->m, a->sb); d->launches++; }
+    { k_adj_moments<<<csgd_grid(s.nn, wb), AT, 0, st>>>(s.link, s.nn, a->sb, a->xm); d->launches++; }
     { k_adj_jt<<<csgd_grid(n, wb), AT, 0, st>>>(s.offs, s.ids, a->xm, s.x, s.y, s.z, d->m, mux, muy, muz, n, a->G, a->eps * a->eps, a->g, jx, jy, jz); d->launches++; }
     { k_adj_push<<<csgd_grid(s.n_alive, AT), AT, 0, st>>>(s.perm, s.leaf_of, s.link, a->xm, a->g, d->m, s.n_alive, s.nn, jx, jy, jz, d->sc); d->launches++; }
     return csgd_check(d, cudaGetLastError());
@@ -636,6 +651,7 @@ CSG_EXPORT csg_adjoint *csg_adjoint_create(int n, const CsgSimParams *params, in
         if (e == cudaSuccess) e = alloc(&a->jt, 3 * (size_t)n);
         if (e == cudaSuccess) e = alloc(&a->g, 3 * ncap);
         if (e == cudaSuccess) e = alloc(&a->xm, ncap);
+        if (e == cudaSuccess) e = alloc(&a->sb, (size_t)n);
         if (e == cudaSuccess) e = alloc(&a->counts, (size_t)n);
         if (e == cudaSuccess) e = cudaMallocHost((void **)&a->h_total, sizeof(int));
         rc = cuda_rc(a, e);
@@ -672,7 +688,7 @@ CSG_EXPORT void csg_adjoint_destroy(csg_adjoint *a)
         free_slot(s);
     for (double *c : a->ckpt)
         cudaFree(c);
-    void *p[] = {a->lam, a->mu, a->jt, a->g, a->xm, a->counts};
+    void *p[] = {a->lam, a->mu, a->jt, a->g, a->xm, a->sb, a->counts};
     for (void *q : p)
         if (q)
             cudaFree(q);
