@@ -643,7 +643,7 @@ __global__ void __launch_bounds__(WARPS * CSG_WARP, w64q_min_blocks(WARPS, PERSI
 // shared memory; every wait polls with a sleep and gives up after WS_POLLS
 // polls (recording CSG_ERR_DEVICE_WAIT, then both warps leave the task).
 constexpr int WS_RING = 128;   // ring slots per lane (power of two)
-constexpr int WS_PAIRS = 2;    // producer/consumer pairs per block
+constexpr int WS_PAIRS = 1;    // producer/consumer pairs per block
 constexpr int WS_BATCH = 8;    // dense batch the consumer waits for
 constexpr int WS_PUBLISH = 4;  // the producer publishes its tails every few steps
 constexpr int WS_POLLS = 1 << 22;
