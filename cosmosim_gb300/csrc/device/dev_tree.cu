@@ -876,65 +876,65 @@ __global__ void k_geometry(csgd_t dd, DevScalars *sc, const DevRoot *__restrict_
 // finally separates the old body j from k) j's cell comes first. Sorting
 // cells by (k, depth, [min S == k]) therefore reproduces pool numbering.
 
+// The export kernels stride over the cells (their count is known on the
+// device only) with a grid sized for the usual trees, not for the capacity:
+// they run beside the walk and should hold few of its warp slots.
 __global__ void k_order_keys(csgd_t dd, DevScalars *sc)
 {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
     const int nn = min(sc->n_nodes, dd.node_cap);
-    if (id >= nn)
-        return;
-    NodeLink l = dd.link[id];
-    unsigned long long k;
-    if (l.parent < 0) {
-        k = 0ull;
-    } else {
-        int s0 = dd.minidx[id].x;
-        int t1 = dd.minidx[l.parent].y;
-        int kc = max(s0, t1);
-        k = ((unsigned long long)(kc + 1) << 8) | ((unsigned long long)l.level << 1) |
-            (s0 == kc ? 1ull : 0ull);
+    for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < nn; id += gridDim.x * blockDim.x) {
+        NodeLink l = dd.link[id];
+        unsigned long long k;
+        if (l.parent < 0) {
+            k = 0ull;
+        } else {
+            int s0 = dd.minidx[id].x;
+            int t1 = dd.minidx[l.parent].y;
+            int kc = max(s0, t1);
+            k = ((unsigned long long)(kc + 1) << 8) | ((unsigned long long)l.level << 1) |
+                (s0 == kc ? 1ull : 0ull);
+        }
+        dd.ord_key[id] = k;
+        dd.ord_id[id] = id;
     }
-    dd.ord_key[id] = k;
-    dd.ord_id[id] = id;
 }
 
 __global__ void k_rank(csgd_t dd, DevScalars *sc)
 {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= min(sc->n_nodes, dd.node_cap))
-        return;
-    dd.rank[dd.ord_id[r]] = r;
+    const int nn = min(sc->n_nodes, dd.node_cap);
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nn; r += gridDim.x * blockDim.x)
+        dd.rank[dd.ord_id[r]] = r;
 }
 
 // Pool records in the reference's numbering, written to dst (device memory or
 // a caller's mapped host array of `capacity` cells; a larger tree is refused).
 __global__ void k_export(csgd_t dd, DevScalars *sc, OctreeNode *__restrict__ dst, int capacity)
 {
-    const int id = blockIdx.x * blockDim.x + threadIdx.x;
     const int nn = min(sc->n_nodes, dd.node_cap);
     if (nn > capacity) {
-        if (id == 0)
+        if (blockIdx.x == 0 && threadIdx.x == 0)
             dev_fail(sc, CSG_ERR_NODE_CAPACITY);
         return;
     }
-    if (id >= nn)
-        return;
-    NodeW64 w = dd.w64[id];
-    double4 g = dd.geo[id];
-    OctreeNode o;
-    o.cx = w.cx;
-    o.cy = w.cy;
-    o.cz = w.cz;
-    o.total_mass = w.m;
-    o.center_x = g.x;
-    o.center_y = g.y;
-    o.center_z = g.z;
-    o.half_size = g.w;
-    o.body_index = w.body;
-    for (int q = 0; q < 8; q++) {
-        int c = dd.child[8 * (size_t)id + q];
-        o.children[q] = (c >= 0) ? dd.rank[c] : -1;
+    for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < nn; id += gridDim.x * blockDim.x) {
+        NodeW64 w = dd.w64[id];
+        double4 g = dd.geo[id];
+        OctreeNode o;
+        o.cx = w.cx;
+        o.cy = w.cy;
+        o.cz = w.cz;
+        o.total_mass = w.m;
+        o.center_x = g.x;
+        o.center_y = g.y;
+        o.center_z = g.z;
+        o.half_size = g.w;
+        o.body_index = w.body;
+        for (int q = 0; q < 8; q++) {
+            int c = dd.child[8 * (size_t)id + q];
+            o.children[q] = (c >= 0) ? dd.rank[c] : -1;
+        }
+        dst[dd.rank[id]] = o;
     }
-    dst[dd.rank[id]] = o;
 }
 
 // Streams the exported records (nn cells, nn read on the device) from the
@@ -1229,7 +1229,8 @@ extern "C" int csgd_export_to(csgd_t *d, OctreeNode *dst, int capacity)
     if (dst != d->pool && !d->pool)
         return CSG_ERR_BAD_ARG; // staging not allocated (csgd_ensure_tree_extras)
     const int bound = capacity < d->node_cap ? capacity : d->node_cap;
-    const int g = csgd_grid(bound, B);
+    const long long cells = cell_threads(d); // the kernels stride beyond it
+    const int g = csgd_grid(cells < bound ? cells : bound, B);
     { k_order_keys<<<g, B, 0, s>>>(*d, sc); d->launches++; }
     int rc = csg_radix_sort(d, d->ord_key, d->ord_id, d->ord_key_alt, d->ord_id_alt, bound, 40,
                             &sc->n_nodes);
@@ -1240,7 +1241,9 @@ extern "C" int csgd_export_to(csgd_t *d, OctreeNode *dst, int capacity)
         { k_export<<<g, B, 0, s>>>(*d, sc, dst, capacity); d->launches++; }
     } else { // records land in rank order: stage them, then stream them out in address order
         { k_export<<<g, B, 0, s>>>(*d, sc, d->pool, capacity); d->launches++; }
-        { k_pool_out<<<4 * d->num_sms, B, 0, s>>>(d->pool, dst, sc, capacity, d->node_cap); d->launches++; }
+        // stores to host memory do not wait for completion: a few warps per
+        // SM keep the link busy and leave the walk its warp slots
+        { k_pool_out<<<d->num_sms, 128, 0, s>>>(d->pool, dst, sc, capacity, d->node_cap); d->launches++; }
     }
     return csgd_check(d, cudaGetLastError());
 }
