@@ -56,6 +56,8 @@ FLOP_PER_INTERACTION = 20  # monopole body-cell interaction: 3 sub, 3 fma d2, rs
 # for 100,000 bodies): the first touch of the tree and the bodies; the tree
 # stays in L2 during the walk. Other workloads scale it by the body count.
 WALK32_DRAM_BYTES_PER_BODY = 10.06e6 / 100_000
+# issue slots busy in the same capture (k_walk32, 100k merger): 57.8%
+WALK32_ISSUE_BUSY = 0.578
 SEED = 0x5EED0000
 
 
@@ -827,15 +829,19 @@ def main():
                      "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak,
                      "traffic": WALK32_DRAM_BYTES_PER_BODY * cfg["n"],
+                     "issue_slots_busy_ncu": WALK32_ISSUE_BUSY,
                      "note": "20 flop per reference interaction / walk event time; peak = FP32 "
                              "FMA throughput measured live by csg_measure_fp_peaks (the walk is "
-                             "CUDA-core bound: no dense contraction, tree resident in L2); "
-                             "traffic = DRAM bytes per launch from the ncu capture of the 100k "
-                             "merger scaled by the body count"},
+                             "CUDA-core bound: no dense contraction, tree resident in L2). What "
+                             "bounds it is instruction issue: the traversal's opening decisions "
+                             "take ~68 warp instructions per warp step against ~9 for the pair "
+                             "term; issue_slots_busy_ncu is from the ncu capture of the 100k "
+                             "merger. traffic = DRAM bytes per launch from that capture scaled "
+                             "by the body count"},
         "errors": r["errors"],
         "e2e": {"value": e2e_value, "unit": UNIT, "api": "integrator_step (pinned host Body[])",
                 "steps": r["e2e_steps"], "h2d_bytes_per_step": 168 * cfg["n"],
-                "d2h_bytes_per_step": 168 * cfg["n"] + 104 * r["e2e_nodes"]},
+                "d2h_bytes_per_step": (104 if cfg["sph"] else 72) * cfg["n"] + 104 * r["e2e_nodes"]},
         "gpu_launches": f32["launches"],
         "clocks": r["clocks"],
     }
