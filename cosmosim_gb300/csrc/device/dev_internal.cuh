@@ -239,19 +239,58 @@ __device__ __forceinline__ double f64_from_f32_bits(float f)
     return __longlong_as_double(((long long)__float_as_int(f) + (896LL << 23)) << 29);
 }
 
+// y^2 (exact: 48 significant bits) and y^3 (rounded to nearest, < 2^-53
+// relative error) as doubles, for a positive normal float 2^-60 < y < 2^60,
+// by integer multiplies of y's 24-bit significand Y (y = Y 2^(ey-150)):
+// no FP64 operations. Y^2 lies in [2^46, 2^48): shifted so its leading bit
+// sits at bit 52, added to (biased exponent - 1) << 52 (the leading bit
+// supplies the missing 1). Y^3 / 2^8 (the high word of (Y 2^40)(Y^2 2^16))
+// lies in [2^61, 2^64): rounded to 53 bits the same way (a carry out of the
+// significand moves into the exponent, as it should).
+__device__ __forceinline__ void pow23_from_f32(float y, double &y2, double &y3)
+{
+    const unsigned yb = __float_as_uint(y);
+    const unsigned Y = (yb & 0x7fffffu) | 0x800000u;
+    const long long ey = (long long)(yb >> 23);
+    const unsigned long long S = (unsigned long long)Y * Y;
+    const unsigned t = (unsigned)(S >> 47); // 1: leading bit at 47
+    y2 = __longlong_as_double(((2 * ey + 768 + t) << 52) + (long long)(S << (6 - t)));
+    const unsigned long long hi = __umul64hi((unsigned long long)Y << 40, S << 16);
+    const int lz = __clz((unsigned)(hi >> 32)); // 0..2
+    const int sh = 11 - lz;
+    const unsigned long long M = (hi + (1ull << (sh - 1))) >> sh;
+    y3 = __longlong_as_double(((3 * ey + 643 - lz) << 52) + (long long)M);
+}
+
+// w = 3/2 e + 15/8 e^2 for |e| < 2^-19, the series term of (1-e)^-3/2 - 1.
+// 15/8 e^2 < 2^-37 needs only ~16 bits, so it is formed in FP32 from the bits
+// of |e| (relative error < 2^-21, i.e. < 2^-58 of the result) and enters by
+// the one FP64 fused multiply-add that forms w; for |e| < 2^-63 it is dropped
+// (< 2^-124). Keeps the squared term off the FP64 pipe.
+__device__ __forceinline__ double r3_series_w(double e)
+{
+    const long long eb = __double_as_longlong(e) & 0x7fffffffffffffffLL;
+    double g = 0.0;
+    if (eb >= (960LL << 52)) { // exponent >= 960: |e| >= 2^-63, in FP32's normal range
+        const float ef = f32_from_f64_bits(eb);
+        g = f64_from_f32_bits(1.875f * ef * ef); // >= 2^-126: a normal float
+    }
+    return fma(1.5, e, g);
+}
+
 // r^-3 and r^-5 for r2 = r^2 without divisions: y0 = FP32 rsqrt seed (rel.
-// error < 2^-21), e = 1 - r2 y0^2 (one fused multiply-add, y0^2 exact), then
-// r^-2 = y0^2 (1 + e + e^2) and r^-3 = y0^3 (1 + 3/2 e + 15/8 e^2) (the
-// binomial series; the first omitted terms are < 2^-60). Outside
-// 2^-99 <= r2 < 2^100 the plain expressions.
+// error < 2^-21; y0^2 and y0^3 by pow23_from_f32), e = 1 - r2 y0^2 (one
+// fused multiply-add), then r^-2 = y0^2 (1 + e + e^2) and
+// r^-3 = y0^3 (1 + 3/2 e + 15/8 e^2) (the binomial series; the first omitted
+// terms are < 2^-60). Outside 2^-99 <= r2 < 2^100 the plain expressions.
 __device__ __forceinline__ void inv_r3_r5(double r2, double &inv3, double &inv5)
 {
     const long long bits = __double_as_longlong(r2);
     if ((unsigned long long)((bits >> 52) - 924) <= 198ull) {
-        const double y0 = f64_from_f32_bits(rsqrtf(f32_from_f64_bits(bits)));
-        const double y0sq = y0 * y0;
+        double y0sq, y3;
+        pow23_from_f32(rsqrtf(f32_from_f64_bits(bits)), y0sq, y3);
         const double e = fma(-r2, y0sq, 1.0);
-        inv3 = (y0sq * y0) * fma(e, fma(1.875, e, 1.5), 1.0);
+        inv3 = fma(y3, r3_series_w(e), y3);
         const double inv2 = fma(y0sq, fma(e, e, e), y0sq);
         inv5 = inv3 * inv2;
         return;
