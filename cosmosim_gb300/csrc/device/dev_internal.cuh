@@ -262,20 +262,51 @@ __device__ __forceinline__ void pow23_from_f32(float y, double &y2, double &y3)
     y3 = __longlong_as_double(((3 * ey + 643 - lz) << 52) + (long long)M);
 }
 
-// w = 3/2 e + 15/8 e^2 for |e| < 2^-19, the series term of (1-e)^-3/2 - 1.
-// 15/8 e^2 < 2^-37 needs only ~16 bits, so it is formed in FP32 from the bits
-// of |e| (relative error < 2^-21, i.e. < 2^-58 of the result) and enters by
-// the one FP64 fused multiply-add that forms w; for |e| < 2^-63 it is dropped
-// (< 2^-124). Keeps the squared term off the FP64 pipe.
+// y^2 (exact) and m y^3 (one rounding to nearest: < 2^-53 relative error,
+// plus < 2^-59 from two truncated high words) as doubles, y as in
+// pow23_from_f32 (2^-51 < y < 2^50), mb the bits of a positive normal double
+// m whose biased exponent lies in [160, 1887] (then m y^3 stays a normal
+// double for every such y). The 53-bit significand of m, times the high word of Y^3 (as in
+// pow23_from_f32), by one 64 x 64 -> high-64 multiply, lands in [2^60, 2^64)
+// and is rounded to 53 bits: no FP64 operations.
+__device__ __forceinline__ void pow2_m3_from_f32(float y, long long mb, double &y2, double &mz)
+{
+    const unsigned yb = __float_as_uint(y);
+    const unsigned Y = (yb & 0x7fffffu) | 0x800000u;
+    const long long ey = (long long)(yb >> 23);
+    const unsigned long long S = (unsigned long long)Y * Y;
+    const unsigned t = (unsigned)(S >> 47);
+    y2 = __longlong_as_double(((2 * ey + 768 + t) << 52) + (long long)(S << (6 - t)));
+    const unsigned long long hi = __umul64hi((unsigned long long)Y << 40, S << 16);
+    const unsigned long long Mm = ((unsigned long long)mb & 0xfffffffffffffull) | (1ull << 52);
+    const unsigned long long Q = __umul64hi(Mm << 11, hi);
+    const int lz = __clz((unsigned)(Q >> 32)); // 0..3
+    const int sh = 11 - lz;
+    const unsigned long long M = (Q + (1ull << (sh - 1))) >> sh;
+    mz = __longlong_as_double((((mb >> 52) + 3 * ey - 379 - lz) << 52) + (long long)M);
+}
+
+// w = 3/2 e + 15/8 e^2 = e c, c = 3/2 + 15/8 e, the series term of
+// (1-e)^-3/2 - 1, for |e| < 2^-7 (the seeds give |e| < 2^-20), by integer
+// arithmetic: c in 62-bit fixed point (C in [2^62, 2^63)), times e's 53-bit
+// significand by one 64 x 64 -> high-64 multiply, rounded to 53 bits (w
+// within 2^-53 relative, plus < 2^-60 from truncations). For |e| < 2^-63,
+// w = 0 (then w < 2^-62: below the result's rounding). Keeps the series off
+// the FP64 pipe.
 __device__ __forceinline__ double r3_series_w(double e)
 {
-    const long long eb = __double_as_longlong(e) & 0x7fffffffffffffffLL;
-    double g = 0.0;
-    if (eb >= (960LL << 52)) { // exponent >= 960: |e| >= 2^-63, in FP32's normal range
-        const float ef = f32_from_f64_bits(eb);
-        g = f64_from_f32_bits(1.875f * ef * ef); // >= 2^-126: a normal float
-    }
-    return fma(1.5, e, g);
+    const long long eb = __double_as_longlong(e);
+    const long long ee = (eb >> 52) & 0x7ff;
+    const unsigned long long Em = ((unsigned long long)eb & 0xfffffffffffffull) | (1ull << 52);
+    const int s = (int)min(max(1016 - ee, 0LL), 63LL);
+    const unsigned long long T = (15ull * Em) >> s; // 15/8 |e| 2^62, < 2^57
+    const unsigned long long C = eb < 0 ? (3ull << 61) - T : (3ull << 61) + T;
+    const unsigned long long R = __umul64hi(Em << 11, C << 1); // [2^62, 2^64)
+    const int lz = __clz((unsigned)(R >> 32));                 // 0 or 1
+    const int sh = 11 - lz;
+    const unsigned long long M = (R + (1ull << (sh - 1))) >> sh;
+    const long long w = (eb & (1LL << 63)) | (((ee - lz) << 52) + (long long)M);
+    return ee < 960 ? 0.0 : __longlong_as_double(w);
 }
 
 // r^-3 and r^-5 for r2 = r^2 without divisions: y0 = FP32 rsqrt seed (rel.
