@@ -262,28 +262,45 @@ __device__ __forceinline__ void pow23_from_f32(float y, double &y2, double &y3)
     y3 = __longlong_as_double(((3 * ey + 643 - lz) << 52) + (long long)M);
 }
 
-// y^2 (exact) and m y^3 (one rounding to nearest: < 2^-53 relative error,
-// plus < 2^-59 from two truncated high words) as doubles, y as in
-// pow23_from_f32 (2^-51 < y < 2^50), mb the bits of a positive normal double
-// m whose biased exponent lies in [160, 1887] (then m y^3 stays a normal
-// double for every such y). The 53-bit significand of m, times the high word of Y^3 (as in
-// pow23_from_f32), by one 64 x 64 -> high-64 multiply, lands in [2^60, 2^64)
-// and is rounded to 53 bits: no FP64 operations.
-__device__ __forceinline__ void pow2_m3_from_f32(float y, long long mb, double &y2, double &mz)
+// m r^-3 by integer arithmetic only, for r2 = r^2 in [2^-99, 2^100) and m a
+// positive normal double with biased exponent in [160, 1887] (then every
+// step below stays in range and the result is a normal double), from the
+// FP32 seed y0 of r^-1 (|1 - r2 y0^2| < 2^-20). With y0 = Y 2^(ey-150)
+// (Y its 24-bit significand), S = Y^2 and r2 = Mr 2^(er-1075):
+//   e = 1 - r2 y0^2 = 1 - Mr S / 2^K, K = 1375 - er - 2 ey in [98, 101]:
+//       Mr S is one 53 x 48-bit product (128 bits); e 2^64 is the
+//       difference 2^K - Mr S shifted right by K - 64 (|e 2^64| < 2^45);
+//   c = (1-e)^-3/2 = 1 + 3/2 e + 15/8 e^2 (next term < 2^-58) in 62-bit
+//       fixed point;
+//   m y0^3 c = Mm Y^3 C 2^(em + 3 ey - 1587): Y^3 2^-8 (the high word of
+//       (Y 2^40)(S 2^16)), times 2C, times Mm 2^11, each keeping the high
+//       64 bits, leaves Q in [2^58, 2^63.1), rounded to 53 bits and packed
+//       with its exponent (a carry out of the significand moves into the
+//       exponent).
+// Relative error < 1.01 x 2^-53 (one rounding; the truncated high words and
+// series add < 2^-57).
+__device__ __forceinline__ double m_r3_from_seed(long long rb, long long mb, float y0)
 {
-    const unsigned yb = __float_as_uint(y);
+    const unsigned long long MANT = 0xfffffffffffffull, HID = 1ull << 52;
+    const unsigned yb = __float_as_uint(y0);
     const unsigned Y = (yb & 0x7fffffu) | 0x800000u;
     const long long ey = (long long)(yb >> 23);
     const unsigned long long S = (unsigned long long)Y * Y;
-    const unsigned t = (unsigned)(S >> 47);
-    y2 = __longlong_as_double(((2 * ey + 768 + t) << 52) + (long long)(S << (6 - t)));
-    const unsigned long long hi = __umul64hi((unsigned long long)Y << 40, S << 16);
-    const unsigned long long Mm = ((unsigned long long)mb & 0xfffffffffffffull) | (1ull << 52);
-    const unsigned long long Q = __umul64hi(Mm << 11, hi);
-    const int lz = __clz((unsigned)(Q >> 32)); // 0..3
-    const int sh = 11 - lz;
-    const unsigned long long M = (Q + (1ull << (sh - 1))) >> sh;
-    mz = __longlong_as_double((((mb >> 52) + 3 * ey - 379 - lz) << 52) + (long long)M);
+    const unsigned long long Mr = ((unsigned long long)rb & MANT) | HID;
+    const unsigned long long L = Mr * S, H = __umul64hi(Mr, S);
+    const int sh = (int)(1375 - 64 - (rb >> 52) - 2 * ey); // K - 64, 34..37
+    const long long Dhi = (1LL << sh) - (long long)H - (L != 0ull);
+    const unsigned long long Dlo = 0ull - L;
+    const long long E64 = (long long)(((unsigned long long)Dhi << (64 - sh)) | (Dlo >> sh));
+    const unsigned long long aE = (unsigned long long)(E64 < 0 ? -E64 : E64);
+    const long long C = (1LL << 62) + ((3 * E64) >> 3) + (long long)((15ull * __umul64hi(aE, aE)) >> 5);
+    const unsigned long long hi3 = __umul64hi((unsigned long long)Y << 40, S << 16);
+    const unsigned long long Z = __umul64hi(hi3, (unsigned long long)C << 1);
+    const unsigned long long Q = __umul64hi((((unsigned long long)mb & MANT) | HID) << 11, Z);
+    const int lz = __clz((unsigned)(Q >> 32)); // 0..5
+    const int s = 11 - lz;
+    const unsigned long long M = (Q + (1ull << (s - 1))) >> s;
+    return __longlong_as_double((((mb >> 52) + 3 * ey - 378 - lz) << 52) + (long long)M);
 }
 
 // w = 3/2 e + 15/8 e^2 = e c, c = 3/2 + 15/8 e, the series term of

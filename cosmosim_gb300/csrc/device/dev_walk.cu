@@ -256,27 +256,20 @@ __global__ void __launch_bounds__(8 * CSG_WARP) k_walk64(WalkArgs a)
         add_hits(a, st);
 }
 
-// m/r^3 for the queued FP64 walk, with few FP64 operations (the FP64 pipe
-// is the walk's bottleneck on this GPU): y0 = FP32 rsqrt seed (rel. error
-// < 2^-21), y0^2 (exact) and m*y0^3 (one rounding) by integer arithmetic
-// (pow2_m3_from_f32), e = 1 - r2*y0^2 by one fused multiply-add, then
-// m/r^3 = m*y0^3 * (1-e)^-3/2 = m*y0^3 * (1 + w), w = 3/2 e + 15/8 e^2
-// (the series to second order; the next term is < 2^-60; w by integer
-// arithmetic in r3_series_w), applied with one fused multiply-add: 2 FP64
-// operations. The seed's conversion is a bit operation. Range checks on the
-// exponents (2^-99 <= r2 < 2^100, 2^-863 <= m < 2^865) keep every integer
-// step in range; outside them (and for m = 0) the plain expression.
+// m/r^3 for the queued FP64 walk without FP64 operations (the FP64 pipe is
+// the walk's bottleneck on this GPU): from the FP32 rsqrt seed y0 (rel.
+// error < 2^-21) by integer arithmetic (m_r3_from_seed: the series of
+// (1-e)^-3/2, e = 1 - r2 y0^2, one rounding). The seed's conversion is a bit
+// operation. Range checks on the exponents (2^-99 <= r2 < 2^100,
+// 2^-863 <= m < 2^865) keep every integer step in range; outside them (and
+// for m = 0) the plain expression.
 __device__ __forceinline__ double m_inv_r3_q(double m, double r2)
 {
     const long long bits = __double_as_longlong(r2);
     const long long mb = __double_as_longlong(m);
     if ((unsigned long long)((bits >> 52) - 924) <= 198ull && // sign clear, exponent 924..1122
-        (unsigned long long)((mb >> 52) - 160) < 1728ull) {   // sign clear, exponent 160..1887
-        double y0sq, mz;
-        pow2_m3_from_f32(rsqrtf(f32_from_f64_bits(bits)), mb, y0sq, mz);
-        const double e = fma(-r2, y0sq, 1.0);
-        return fma(mz, r3_series_w(e), mz);
-    }
+        (unsigned long long)((mb >> 52) - 160) < 1728ull)     // sign clear, exponent 160..1887
+        return m_r3_from_seed(bits, mb, rsqrtf(f32_from_f64_bits(bits)));
     return m / (r2 * sqrt(r2));
 }
 
