@@ -9,6 +9,7 @@
 // The probes time long independent FMA chains (8 per thread) and report the
 // FP32 and FP64 CUDA-core throughput of this GPU: the denominators for the
 // walk kernels, which are bound by those pipes, not by tensor cores or HBM.
+#include "dev_fpint.cuh"
 #include "dev_internal.cuh"
 
 namespace {
@@ -435,4 +436,125 @@ extern "C" CSG_EXPORT int csg_direct_forces_noalloc(const double *x, const doubl
     if (cudaGetLastError() != cudaSuccess)
         return CSG_ERR_CUDA;
     return CSG_OK;
+}
+
+// ---- integer-pipe division and square root: self-check ----------------------
+//
+// div_rn and sqrt_rn (dev_fpint.cuh) against the compiler's correctly rounded
+// operators, bit for bit, on n seeded operand pairs of several kinds: operands
+// of moderate exponents, arbitrary bit patterns (zeros, subnormals,
+// infinities, NaNs, exponents near the fast path's bounds), integer operands
+// over small odd divisors (exact quotients and ties), power-of-two divisors,
+// signed zeros and SPH-like distances and smoothing lengths.
+
+namespace {
+
+__device__ __forceinline__ unsigned long long xs_next(unsigned long long &s)
+{
+    s ^= s << 13;
+    s ^= s >> 7;
+    s ^= s << 17;
+    return s;
+}
+
+__device__ __forceinline__ double rand_moderate(unsigned long long &s, int span)
+{
+    const unsigned long long r = xs_next(s);
+    const long long e = 1023 + (long long)(r % (unsigned long long)(2 * span + 1)) - span;
+    return __longlong_as_double((long long)((r & (1ull << 63)) | ((unsigned long long)e << 52) |
+                                            (xs_next(s) & fpint::MANT)));
+}
+
+__global__ void k_check_div_sqrt(unsigned long long seed, long long n, unsigned long long *out)
+{
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    unsigned long long bad_div = 0, bad_sqrt = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        unsigned long long s = (seed ^ ((unsigned long long)i * 0x9E3779B97F4A7C15ull)) | 1ull;
+        xs_next(s);
+        xs_next(s);
+        double a, b;
+        switch ((unsigned)(xs_next(s) % 8)) {
+        case 0:
+        case 1:
+            a = rand_moderate(s, 60);
+            b = rand_moderate(s, 60);
+            break;
+        case 2:
+            a = __longlong_as_double((long long)xs_next(s));
+            b = __longlong_as_double((long long)xs_next(s));
+            break;
+        case 3: {
+            const unsigned sh = 11 + (unsigned)(xs_next(s) % 40);
+            a = (double)(long long)(xs_next(s) >> sh);
+            const double odd[6] = {3.0, 5.0, 7.0, 9.0, 11.0, 1.0 + (double)(xs_next(s) & 255) * 2.0};
+            b = odd[xs_next(s) % 6] * ((xs_next(s) & 1) ? 1.0 : -1.0);
+            break;
+        }
+        case 4:
+            a = rand_moderate(s, 500);
+            b = __longlong_as_double((long long)((unsigned long long)(1023 + (long long)(xs_next(s) % 1001) - 500)
+                                                 << 52));
+            break;
+        case 5:
+            a = (xs_next(s) & 1) ? 0.0 : -0.0;
+            b = rand_moderate(s, 1000);
+            break;
+        case 6: // exponents near the fast path's limits
+            a = rand_moderate(s, 1022);
+            b = rand_moderate(s, 1022);
+            break;
+        default: { // distances, smoothing lengths, densities of the SPH passes
+            const double r = (double)(xs_next(s) >> 11) * 0x1p-53 * 4.0;
+            const double h = 0.01 + (double)(xs_next(s) >> 11) * 0x1p-53;
+            a = (xs_next(s) & 1) ? r * r : r;
+            b = (xs_next(s) & 1) ? h : h * h * h * 3.141592653589793;
+            break;
+        }
+        }
+        if (__double_as_longlong(div_rn(a, b)) != __double_as_longlong(__ddiv_rn(a, b)))
+            bad_div++;
+        const double x = (xs_next(s) & 3) ? fabs(a) : a;
+        if (__double_as_longlong(sqrt_rn(x)) != __double_as_longlong(__dsqrt_rn(x)))
+            bad_sqrt++;
+    }
+    if (bad_div)
+        atomicAdd(&out[0], bad_div);
+    if (bad_sqrt)
+        atomicAdd(&out[1], bad_sqrt);
+}
+
+} // namespace
+
+extern "C" CSG_EXPORT int csg_check_div_sqrt(int64_t n, uint64_t seed, int64_t *div_mismatches,
+                                             int64_t *sqrt_mismatches)
+{
+    if (n < 0 || !div_mismatches || !sqrt_mismatches)
+        return CSG_ERR_BAD_ARG;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return CSG_ERR_NO_DEVICE;
+    }
+    unsigned long long *out = nullptr;
+    if (cudaMalloc((void **)&out, 2 * sizeof(unsigned long long)) != cudaSuccess) {
+        cudaGetLastError();
+        return CSG_ERR_NOMEM;
+    }
+    unsigned long long h[2] = {0, 0};
+    int rc = CSG_OK;
+    if (cudaMemset(out, 0, sizeof(h)) != cudaSuccess)
+        rc = CSG_ERR_CUDA;
+    if (!rc && n > 0) {
+        k_check_div_sqrt<<<sms * 8, 256>>>((unsigned long long)seed, (long long)n, out);
+        if (cudaGetLastError() != cudaSuccess)
+            rc = CSG_ERR_CUDA;
+    }
+    if (!rc && cudaMemcpy(h, out, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess)
+        rc = CSG_ERR_CUDA;
+    cudaFree(out);
+    *div_mismatches = (int64_t)h[0];
+    *sqrt_mismatches = (int64_t)h[1];
+    return rc;
 }

@@ -7,13 +7,16 @@
 // the cap binds often. Walking the preorder tree with per-lane subtree skips
 // (as in dev_walk.cu) meets the leaves in exactly that order. Each pass runs in
 // two kernels: the walk records every gas body's capped list, then a pair
-// kernel sums over the lists in that order — the FP64 pair arithmetic (sqrt,
-// divisions: slow on this GPU) then runs densely, one lane per gas body,
-// instead of once per walk step for whichever lanes found a neighbour.
-// Lanes are the gas bodies in key order.
+// kernel sums over the lists in that order — the FP64 pair arithmetic then
+// runs densely, one lane per gas body, instead of once per walk step for
+// whichever lanes found a neighbour. Lanes are the gas bodies in key order.
+// Its divisions and square roots (about ten FP64 operations each with the
+// compiler's operators, on a GPU whose FP64 rate is 1/64 of FP32) run on the
+// integer pipes (div_rn, sqrt_rn): correctly rounded, so bit-identical.
 //
 // Compiled with -fmad=false, with the reference's operation order, so for the
 // same inputs every sum rounds as the reference's does.
+#include "dev_fpint.cuh"
 #include "dev_internal.cuh"
 
 namespace {
@@ -30,7 +33,7 @@ __device__ __forceinline__ double kernel_W_norm(double r, double h, double norm)
 {
     if (h < 1e-10)
         return 0.0;
-    double q = r / h;
+    double q = div_rn(r, h);
     if (q > 1.0)
         return 0.0;
     if (q <= 0.5)
@@ -39,21 +42,21 @@ __device__ __forceinline__ double kernel_W_norm(double r, double h, double norm)
     return norm * 2.0 * t * t * t;
 }
 
-__device__ __forceinline__ double kernel_norm(double h) { return 8.0 / (PI_D * h * h * h); }
+__device__ __forceinline__ double kernel_norm(double h) { return div_rn(8.0, PI_D * h * h * h); }
 
 // the kernel's radial derivative dW/dr(r, h), src/sph.c:27-41
 __device__ __forceinline__ double kernel_dWdr(double r, double h)
 {
     if (h < 1e-10)
         return 0.0;
-    double q = r / h;
+    double q = div_rn(r, h);
     if (q > 1.0 || r < 1e-15)
         return 0.0;
-    double norm = 8.0 / (PI_D * h * h * h);
+    double norm = div_rn(8.0, PI_D * h * h * h);
     if (q <= 0.5)
-        return norm * (-12.0 * q + 18.0 * q * q) / h;
+        return div_rn(norm * (-12.0 * q + 18.0 * q * q), h);
     double t = 1.0 - q;
-    return norm * (-6.0 * t * t) / h;
+    return div_rn(norm * (-6.0 * t * t), h);
 }
 
 struct SphArgs {
@@ -256,7 +259,7 @@ __global__ void __launch_bounds__(SPH_THREADS) k_sph_density_terms(SphArgs a)
         double dx = a.x[i] - a.x[j];
         double dy = a.y[i] - a.y[j];
         double dz = a.z[i] - a.z[j];
-        double r = sqrt(dx * dx + dy * dy + dz * dz);
+        double r = sqrt_rn(dx * dx + dy * dy + dz * dz);
         a.term[stride * s + k] = a.m[j] * kernel_W_norm(r, a.h[i], a.pr2[i]);
     }
 }
@@ -302,8 +305,8 @@ __global__ void __launch_bounds__(SPH_THREADS) k_sph_body_terms(SphArgs a)
         return;
     const int j = a.gas[k];
     const double rho = a.rho[j], P = a.P[j];
-    a.pr2[j] = P / (rho * rho + 1e-15);
-    a.cs[j] = sqrt(GAMMA * P / (rho + 1e-15));
+    a.pr2[j] = div_rn(P, rho * rho + 1e-15);
+    a.cs[j] = sqrt_rn(div_rn(GAMMA * P, rho + 1e-15));
 }
 
 // Pressure gradient + Monaghan viscosity terms, src/sph.c:126-186.
@@ -326,7 +329,7 @@ __global__ void __launch_bounds__(SPH_THREADS) k_sph_force_terms(SphArgs a)
             double dx = a.x[i] - a.x[j];
             double dy = a.y[i] - a.y[j];
             double dz = a.z[i] - a.z[j];
-            double r = sqrt(dx * dx + dy * dy + dz * dz);
+            double r = sqrt_rn(dx * dx + dy * dy + dz * dz);
             if (!(r < 1e-15)) {
                 const double h_i = a.h[i], rho_i = a.rho[i];
                 double h_avg = 0.5 * (h_i + a.h[j]);
@@ -337,15 +340,15 @@ __global__ void __launch_bounds__(SPH_THREADS) k_sph_force_terms(SphArgs a)
                 double vr = dvx * dx + dvy * dy + dvz * dz;
                 double visc = 0.0;
                 if (vr < 0.0) {
-                    double mu = h_avg * vr / (r * r + 0.01 * h_avg * h_avg);
+                    double mu = div_rn(h_avg * vr, r * r + 0.01 * h_avg * h_avg);
                     double c_avg = 0.5 * (a.cs[i] + a.cs[j]);
                     double rho_avg = 0.5 * (rho_i + rho_j);
-                    visc = (-1.0 * c_avg * mu + 2.0 * mu * mu) / (rho_avg + 1e-15);
+                    visc = div_rn(-1.0 * c_avg * mu + 2.0 * mu * mu, rho_avg + 1e-15);
                 }
                 double g = kernel_dWdr(r, h_avg);
-                double gx = g * dx / r;
-                double gy = g * dy / r;
-                double gz = g * dz / r;
+                double gx = div_rn(g * dx, r);
+                double gy = div_rn(g * dy, r);
+                double gz = div_rn(g * dz, r);
                 double f = a.m[j] * (a.pr2[i] + a.pr2[j] + visc);
                 tx = f * gx;
                 ty = f * gy;

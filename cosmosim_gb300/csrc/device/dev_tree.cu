@@ -24,6 +24,7 @@
 // Cell centres are recomputed with the reference's own arithmetic
 // (centre +/- 0.5*half_size per level, half_size*0.5), so split decisions and
 // geometry are identical to the reference's bit for bit.
+#include "dev_fpint.cuh"
 #include "dev_internal.cuh"
 
 #include <float.h>
@@ -737,7 +738,7 @@ __device__ __forceinline__ void moments_climb(const csgd_t &dd, int node, double
                 }
             }
         }
-        const double inv = 1.0 / M;
+        const double inv = div_rn(1.0, M); // correctly rounded, off the FP64 pipe
         sx = ax * inv;
         sy = ay * inv;
         sz = az * inv;
@@ -785,7 +786,7 @@ __device__ __forceinline__ void moments_cell(const csgd_t &dd, int id, const dou
                 }
             }
         }
-        const double inv = 1.0 / M;
+        const double inv = div_rn(1.0, M); // correctly rounded, off the FP64 pipe
         sx = ax * inv;
         sy = ay * inv;
         sz = az * inv;

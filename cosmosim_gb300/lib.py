@@ -94,6 +94,8 @@ _SIGS = {
     "cosmosim_energy": ([_vp, ctypes.POINTER(_d), ctypes.POINTER(_d)], _i),
     "cosmosim_launch_count": ([_vp], ctypes.c_int64),
     "csg_measure_fp_peaks": ([ctypes.POINTER(_d), ctypes.POINTER(_d)], _i),
+    "csg_check_div_sqrt": ([ctypes.c_int64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_int64),
+                            ctypes.POINTER(ctypes.c_int64)], _i),
     "csg_sort_keys": ([_vp, _i, _i, _vp, _vp], _i),
     "cosmosim_enable_graphs": ([_vp, _i], _i),
     "csg_direct_forces_noalloc": ([_vp, _vp, _vp, _vp, _i, _vp, _i, _d, _d, _vp, _vp], _i),
@@ -234,6 +236,16 @@ def measure_fp_peaks():
     rc = load().csg_measure_fp_peaks(ctypes.byref(a), ctypes.byref(b))
     if rc:
         raise CudaError(f"peak probe failed ({rc})")
+    return a.value, b.value
+
+
+def check_div_sqrt(n, seed=1):
+    """(division, square root) mismatches of the integer-pipe operators against
+    the compiler's correctly rounded ones over n seeded cases (csg_check_div_sqrt)."""
+    a, b = ctypes.c_int64(0), ctypes.c_int64(0)
+    rc = load().csg_check_div_sqrt(n, seed, ctypes.byref(a), ctypes.byref(b))
+    if rc:
+        raise CudaError(f"csg_check_div_sqrt failed ({rc})")
     return a.value, b.value
 
 

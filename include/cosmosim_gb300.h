@@ -194,6 +194,13 @@ CSG_EXPORT int64_t cosmosim_launch_count(SimHandle handle);
    bound by. */
 CSG_EXPORT int csg_measure_fp_peaks(double *fp32_tflops, double *fp64_tflops);
 
+/* Self-check of the integer-pipe double division and square root the SPH
+   passes use (correctly rounded, so they must equal the compiler's operators
+   bit for bit): n seeded operand pairs of several kinds on the current GPU;
+   the mismatch counts are returned (0 and 0 when correct). */
+CSG_EXPORT int csg_check_div_sqrt(int64_t n, uint64_t seed, int64_t *div_mismatches,
+                                  int64_t *sqrt_mismatches);
+
 /* The tree build's key sort on caller keys: an LSD radix sort, 8 bits a pass,
    ceil(bits/8) passes (bits 1..64), stable. out_keys = keys in ascending order
    of their low 8*ceil(bits/8) bits; out_index = the input position of each
