@@ -264,19 +264,36 @@ __global__ void __launch_bounds__(SPH_THREADS) k_sph_density_terms(SphArgs a)
     }
 }
 
+// The per-body sums run one thread per gas body in small blocks (the gas
+// bodies are ~10% of all: 64-thread blocks spread them over every SM) and
+// load SUM_BATCH slots ahead of the additions, which stay in list order.
+constexpr int SUM_THREADS = 64;
+constexpr int SUM_BATCH = 8;
+
 // Density, adaptive h and pressure, src/sph.c:45-97.
-__global__ void __launch_bounds__(SPH_THREADS) k_sph_density_sums(SphArgs a)
+__global__ void __launch_bounds__(SUM_THREADS) k_sph_density_sums(SphArgs a)
 {
-    const int k = blockIdx.x * SPH_THREADS + threadIdx.x;
+    const int k = blockIdx.x * SUM_THREADS + threadIdx.x;
     if (k >= a.sc->n_gas)
         return;
     const int i = a.gas[k];
     const double h = a.h[i];
     const int nn = a.nb_count[k];
     const size_t stride = (size_t)a.stride;
+    const double *__restrict__ term = a.term;
     double rho = 0.0;
-    for (int s = 0; s < nn; s++)
-        rho += a.term[stride * s + k];
+    int s = 0;
+    for (; s + SUM_BATCH <= nn; s += SUM_BATCH) {
+        double t[SUM_BATCH];
+#pragma unroll
+        for (int u = 0; u < SUM_BATCH; u++)
+            t[u] = __ldg(&term[stride * (s + u) + k]);
+#pragma unroll
+        for (int u = 0; u < SUM_BATCH; u++)
+            rho += t[u];
+    }
+    for (; s < nn; s++)
+        rho += __ldg(&term[stride * s + k]);
     int relist = 1;
     if (nn < 20 && h < 50.0)
         a.h[i] = h * 1.2;
@@ -298,9 +315,9 @@ __global__ void __launch_bounds__(SPH_THREADS) k_sph_density_sums(SphArgs a)
 // sqrt(gamma P/(rho + 1e-15)) (src/sph.c:112, :153-154, :170-171). The pair
 // terms need them for both bodies of every pair; computing them once per body
 // gives the same values as the reference's per-pair evaluation.
-__global__ void __launch_bounds__(SPH_THREADS) k_sph_body_terms(SphArgs a)
+__global__ void __launch_bounds__(SUM_THREADS) k_sph_body_terms(SphArgs a)
 {
-    const int k = blockIdx.x * SPH_THREADS + threadIdx.x;
+    const int k = blockIdx.x * SUM_THREADS + threadIdx.x;
     if (k >= a.sc->n_gas)
         return;
     const int j = a.gas[k];
@@ -362,21 +379,39 @@ __global__ void __launch_bounds__(SPH_THREADS) k_sph_force_terms(SphArgs a)
 }
 
 // Sums of the force terms in list order, src/sph.c:187-196.
-__global__ void __launch_bounds__(SPH_THREADS) k_sph_force_sums(SphArgs a)
+__global__ void __launch_bounds__(SUM_THREADS) k_sph_force_sums(SphArgs a)
 {
-    const int k = blockIdx.x * SPH_THREADS + threadIdx.x;
+    const int k = blockIdx.x * SUM_THREADS + threadIdx.x;
     if (k >= a.sc->n_gas)
         return;
     const int i = a.gas[k];
     const int nn = a.nb_count[k];
     const size_t stride = (size_t)a.stride;
     const size_t plane = stride * CSG_SPH_MAX_NEIGHBORS;
+    const double *__restrict__ term = a.term;
     double sx = 0.0, sy = 0.0, sz = 0.0;
-    for (int s = 0; s < nn; s++) {
+    int s = 0;
+    for (; s + SUM_BATCH <= nn; s += SUM_BATCH) {
+        double tx[SUM_BATCH], ty[SUM_BATCH], tz[SUM_BATCH];
+#pragma unroll
+        for (int u = 0; u < SUM_BATCH; u++) {
+            const size_t o = stride * (s + u) + k;
+            tx[u] = __ldg(&term[o]);
+            ty[u] = __ldg(&term[plane + o]);
+            tz[u] = __ldg(&term[2 * plane + o]);
+        }
+#pragma unroll
+        for (int u = 0; u < SUM_BATCH; u++) {
+            sx -= tx[u];
+            sy -= ty[u];
+            sz -= tz[u];
+        }
+    }
+    for (; s < nn; s++) {
         const size_t o = stride * s + k;
-        sx -= a.term[o];
-        sy -= a.term[plane + o];
-        sz -= a.term[2 * plane + o];
+        sx -= __ldg(&term[o]);
+        sy -= __ldg(&term[plane + o]);
+        sz -= __ldg(&term[2 * plane + o]);
     }
     if (isnan(sx))
         sx = 0.0;
@@ -589,23 +624,23 @@ static int sph_pass(csgd_t *d, int forces, bool sums = true, bool reuse = false)
     SphArgs a = make_args(d);
     a.reuse = (forces && reuse) ? 1 : 0;
     a.density = forces ? 0 : 1;
-    const int g = csgd_grid(d->n, SPH_THREADS);
+    const int g = csgd_grid(d->n, SUM_THREADS);
     // one warp per gas body for the lists, warps striding over the gas bodies
     int gl = csgd_grid((long long)d->n * CSG_WARP, SPH_THREADS);
-    if (gl > 152 * 16)
-        gl = 152 * 16;
+    if (gl > d->num_sms * 16)
+        gl = d->num_sms * 16;
     { k_sph_lists<<<gl, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
     // pair terms: a grid-stride pass over (slot, gas body), sized for 32 warps
     // per SM (the gas count is known on the device only)
     const int gp = d->num_sms * (2048 / SPH_THREADS);
     if (forces) {
-        { k_sph_body_terms<<<g, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
+        { k_sph_body_terms<<<g, SUM_THREADS, 0, d->stream>>>(a); d->launches++; }
         { k_sph_force_terms<<<gp, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
         if (sums)
-            { k_sph_force_sums<<<g, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
+            { k_sph_force_sums<<<g, SUM_THREADS, 0, d->stream>>>(a); d->launches++; }
     } else {
         { k_sph_density_terms<<<gp, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
-        { k_sph_density_sums<<<g, SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
+        { k_sph_density_sums<<<g, SUM_THREADS, 0, d->stream>>>(a); d->launches++; }
     }
     return csgd_check(d, cudaGetLastError());
 }
@@ -629,7 +664,7 @@ extern "C" int csgd_sph_force_sums(csgd_t *d)
     if (d->n <= 0)
         return CSG_OK;
     SphArgs a = make_args(d);
-    { k_sph_force_sums<<<csgd_grid(d->n, SPH_THREADS), SPH_THREADS, 0, d->stream>>>(a); d->launches++; }
+    { k_sph_force_sums<<<csgd_grid(d->n, SUM_THREADS), SUM_THREADS, 0, d->stream>>>(a); d->launches++; }
     return csgd_check(d, cudaGetLastError());
 }
 
