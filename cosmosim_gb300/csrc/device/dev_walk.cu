@@ -531,43 +531,70 @@ __global__ void __launch_bounds__(WARPS * CSG_WARP, persist_min_blocks(WARPS, PE
 constexpr int q64_slots(int warps) { return warps == 4 ? 64 : 32; }
 constexpr int F64 = 8; // entries per lane per dense batch
 
-// Evaluates the lane's next `count` queued cells (count >= 0; lanes without a
-// body pass 0 and never read their queue).
+// Loads queued entry s of the lane (its cell's centre of mass and mass), or
+// zeros when s >= count (no queue read, no cell read).
 template <int Q64>
+__device__ __forceinline__ void q64_load(const WalkArgs &a, const int *q, int lane, int head, int s,
+                                         int count, double2 &p01, double2 &p23)
+{
+    p01 = make_double2(0.0, 0.0);
+    p23 = p01;
+    if (s < count) {
+        const int c = q[((head + s) & (Q64 - 1)) * CSG_WARP + lane];
+        p01 = __ldg((const double2 *)&a.w64[c]);     // cx, cy
+        p23 = __ldg((const double2 *)&a.w64[c] + 1); // cz, m
+    }
+}
+
+__device__ __forceinline__ void q64_term(const WalkArgs &a, const double2 &p01, const double2 &p23,
+                                         double px, double py, double pz, double &sx, double &sy,
+                                         double &sz)
+{
+    const double dx = p01.x - px, dy = p01.y - py, dz = p23.x - pz;
+    const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, a.eps2)));
+    const double f = m_inv_r3_q(p23.y, r2);
+    sx = fma(f, dx, sx);
+    sy = fma(f, dy, sy);
+    sz = fma(f, dz, sz);
+}
+
+// Evaluates the lane's next `count` queued cells (count >= 0; lanes without a
+// body pass 0 and never read their queue), two at a time in queue order. With
+// PREFETCH the next two cells' loads are in flight while the current two are
+// evaluated (the producer/consumer walk: few consumer warps per SM at small
+// N, each waiting on its loads); without, each pair is loaded and then
+// evaluated (the queued walk, whose registers are tighter). The sums are the
+// same either way.
+template <int Q64, bool PREFETCH = false>
 __device__ __forceinline__ void q64_eval(const WalkArgs &a, const int *q, int lane, int &head,
                                          int count, double px, double py, double pz,
                                          double &sx, double &sy, double &sz)
 {
     count = max(count, 0);
     const int kmax = (int)__reduce_max_sync(0xffffffffu, (unsigned)count);
-    for (int s = 0; s < kmax; s += 2) { // two entries: both loads in flight together
-        const bool v0 = s < count, v1 = s + 1 < count;
-        const int n0 = v0 ? q[((head + s) & (Q64 - 1)) * CSG_WARP + lane] : 0;
-        const int n1 = v1 ? q[((head + s + 1) & (Q64 - 1)) * CSG_WARP + lane] : 0;
-        double2 a01 = make_double2(0.0, 0.0), a23 = a01, b01 = a01, b23 = a01;
-        if (v0) {
-            a01 = __ldg((const double2 *)&a.w64[n0]);     // cx, cy
-            a23 = __ldg((const double2 *)&a.w64[n0] + 1); // cz, m
+    double2 a01, a23, b01, b23;
+    if (PREFETCH) {
+        q64_load<Q64>(a, q, lane, head, 0, count, a01, a23);
+        q64_load<Q64>(a, q, lane, head, 1, count, b01, b23);
+    }
+    for (int s = 0; s < kmax; s += 2) {
+        double2 c01, c23, d01, d23;
+        if (PREFETCH) {
+            q64_load<Q64>(a, q, lane, head, s + 2, count, c01, c23);
+            q64_load<Q64>(a, q, lane, head, s + 3, count, d01, d23);
+        } else {
+            q64_load<Q64>(a, q, lane, head, s, count, a01, a23);
+            q64_load<Q64>(a, q, lane, head, s + 1, count, b01, b23);
         }
-        if (v1) {
-            b01 = __ldg((const double2 *)&a.w64[n1]);
-            b23 = __ldg((const double2 *)&a.w64[n1] + 1);
-        }
-        if (v0) {
-            const double dx = a01.x - px, dy = a01.y - py, dz = a23.x - pz;
-            const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, a.eps2)));
-            const double f = m_inv_r3_q(a23.y, r2);
-            sx = fma(f, dx, sx);
-            sy = fma(f, dy, sy);
-            sz = fma(f, dz, sz);
-        }
-        if (v1) {
-            const double dx = b01.x - px, dy = b01.y - py, dz = b23.x - pz;
-            const double r2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, a.eps2)));
-            const double f = m_inv_r3_q(b23.y, r2);
-            sx = fma(f, dx, sx);
-            sy = fma(f, dy, sy);
-            sz = fma(f, dz, sz);
+        if (s < count)
+            q64_term(a, a01, a23, px, py, pz, sx, sy, sz);
+        if (s + 1 < count)
+            q64_term(a, b01, b23, px, py, pz, sx, sy, sz);
+        if (PREFETCH) {
+            a01 = c01;
+            a23 = c23;
+            b01 = d01;
+            b23 = d23;
         }
     }
     head += count;
@@ -737,7 +764,7 @@ __device__ __forceinline__ void ws_consume(const WalkArgs &a, WsShared &sh, cons
             take = -1; // the rest (done) or relief for a lane whose ring is nearly full
         if (take != 0) {
             const int k = take > 0 ? (valid ? take : 0) : min(avail, done ? avail : WS_BATCH);
-            q64_eval<WS_RING>(a, sh.ring, lane, head, k, px, py, pz, sx, sy, sz);
+            q64_eval<WS_RING, true>(a, sh.ring, lane, head, k, px, py, pz, sx, sy, sz);
             __threadfence_block(); // entries read before the head is published
             ((volatile int *)sh.head)[lane] = head;
             polls = 0;
