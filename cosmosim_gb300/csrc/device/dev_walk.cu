@@ -666,7 +666,6 @@ __global__ void __launch_bounds__(WARPS * CSG_WARP, w64q_min_blocks(WARPS, PERSI
 // shared memory; every wait polls with a sleep and gives up after WS_POLLS
 // polls (recording CSG_ERR_DEVICE_WAIT, then both warps leave the task).
 constexpr int WS_RING = 128;   // ring slots per lane (power of two)
-constexpr int WS_PAIRS = 1;    // producer/consumer pairs per block
 constexpr int WS_BATCH = 8;    // dense batch the consumer waits for
 constexpr int WS_PUBLISH = 4;  // the producer publishes its tails every few steps
 constexpr int WS_POLLS = 1 << 22;
@@ -790,17 +789,21 @@ __device__ __forceinline__ void ws_consume(const WalkArgs &a, WsShared &sh, cons
     }
 }
 
-template <bool STATS, bool EMPTY>
-__global__ void __launch_bounds__(2 * WS_PAIRS * CSG_WARP, 24 / (2 * WS_PAIRS)) k_walk64ws(WalkArgs a)
+// PAIRS producer/consumer pairs per block (task t of the grid is pair
+// t % PAIRS of block t / PAIRS), 12 pairs per SM either way: one pair for
+// launches of few tasks (finer blocks balance better over the SMs), two
+// otherwise (measured faster from ~100k bodies on).
+template <bool STATS, bool EMPTY, int PAIRS>
+__global__ void __launch_bounds__(2 * PAIRS * CSG_WARP, 24 / (2 * PAIRS)) k_walk64ws(WalkArgs a)
 {
-    __shared__ WsShared sh_all[WS_PAIRS];
-    __shared__ NodeW32 win_all[WS_PAIRS][CSG_WARP];
+    __shared__ WsShared sh_all[PAIRS];
+    __shared__ NodeW32 win_all[PAIRS][CSG_WARP];
     const int warp = threadIdx.x >> 5, pair = warp >> 1, lane = threadIdx.x & 31;
     WsShared &sh = sh_all[pair];
     const int nn = a.sc->n_nodes;
     if (nn > a.node_cap || nn < 1)
         return;
-    const int t = blockIdx.x * WS_PAIRS + pair;
+    const int t = blockIdx.x * PAIRS + pair;
     TaskRange tr{0, 0, 0, 0};
     bool ok = t < a.sc->n_tasks;
     if (ok) {
@@ -979,16 +982,25 @@ void launch_walk(csgd_t *d, const WalkArgs &a, int precision, int exact)
             CSG_LAUNCH_WALK(k_walk32, 8, grid, s, b);
     } else if (CSG_WALK64_WS && !persist) {
         const long long tasks = (long long)d->n / CSG_WARP + d->n_gal + 1; // >= n_tasks
-        const int gw = (int)((tasks + WS_PAIRS - 1) / WS_PAIRS);
-        const int blocks = 2 * WS_PAIRS * CSG_WARP;
+        const int pairs = tasks > 8LL * d->num_sms ? 2 : 1;
+        const int gw = (int)((tasks + pairs - 1) / pairs);
+        const int threads = 2 * pairs * CSG_WARP;
+#define CSG_WS(ST, EM)                                                                             \
+    do {                                                                                          \
+        if (pairs == 2)                                                                           \
+            k_walk64ws<ST, EM, 2><<<gw, threads, 0, s>>>(b);                                      \
+        else                                                                                      \
+            k_walk64ws<ST, EM, 1><<<gw, threads, 0, s>>>(b);                                      \
+    } while (0)
         if (stats && empty)
-            k_walk64ws<true, true><<<gw, blocks, 0, s>>>(b);
+            CSG_WS(true, true);
         else if (stats)
-            k_walk64ws<true, false><<<gw, blocks, 0, s>>>(b);
+            CSG_WS(true, false);
         else if (empty)
-            k_walk64ws<false, true><<<gw, blocks, 0, s>>>(b);
+            CSG_WS(false, true);
         else
-            k_walk64ws<false, false><<<gw, blocks, 0, s>>>(b);
+            CSG_WS(false, false);
+#undef CSG_WS
     } else {
         if (W == 4)
             CSG_LAUNCH_WALK(k_walk64q, 4, grid, s, b);
