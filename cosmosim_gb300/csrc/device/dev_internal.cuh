@@ -147,7 +147,6 @@ struct csgd {
     // per task, else tasks taken from an atomic counter this many at a time)
     // and, for the persistent form, blocks per SM
     int walk_warps, walk_group, walk_bps;
-    int walk_auto; // no shape set by the caller: 4-warp blocks, 8 beside SPH
     int num_sms;
     int export_order; // builds also keep what pool export needs (two lowest indices per cell)
     int minidx_valid; // the current tree has them

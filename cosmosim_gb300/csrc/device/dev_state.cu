@@ -272,7 +272,6 @@ extern "C" csgd_t *csgd_create(void)
     d->use_graphs = 1;
     d->n_gal = 1;
     d->walk_warps = 4; // fastest one-warp-per-task shape at 20k..1M bodies
-    d->walk_auto = 1;
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) == cudaSuccess &&
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0)
@@ -708,13 +707,7 @@ extern "C" int csgd_substep(csgd_t *d, double dt, const csgd_force_params *p, in
             rc = csgd_sph_force_terms(d, 1);
         d->stream = main;
         cudaEventRecord(d->ev_join, d->aux);
-        // beside the SPH kernels 8-warp walk blocks finish the pair sooner
-        // than the 4-warp blocks that are fastest alone (measured at 100k)
-        const int saved_warps = d->walk_warps;
-        if (d->walk_auto)
-            d->walk_warps = 8;
         const int rg = csgd_gravity(d, p);
-        d->walk_warps = saved_warps;
         cudaStreamWaitEvent(main, d->ev_join, 0); // always rejoin (a capture needs it)
         if (!rc)
             rc = rg;

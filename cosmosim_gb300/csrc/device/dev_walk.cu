@@ -1079,12 +1079,9 @@ extern "C" int csgd_set_walk_shape(csgd_t *d, const CsgWalkShape *w)
     if (d->walk_warps != w->warps_per_block || d->walk_group != w->task_group ||
         d->walk_bps != w->blocks_per_sm)
         csgd_drop_graph(d); // the captured walk launch changes
-    if (d->walk_auto)
-        csgd_drop_graph(d); // a substep with SPH no longer switches to 8 warps
     d->walk_warps = w->warps_per_block;
     d->walk_group = w->task_group;
     d->walk_bps = w->task_group > 0 ? w->blocks_per_sm : 0;
-    d->walk_auto = 0;
     return CSG_OK;
 }
 

@@ -43,7 +43,7 @@ extern "C" {
 /* Launch shape of the gravity walk. A walk task is up to 32 consecutive
    key-ordered bodies of one system, walked by one warp. Until a shape is
    set (cosmosim_set_walk_shape, cosmosim_autotune_walk) a handle uses
-   {4, 0, 0}, and {8, 0, 0} in substeps whose SPH passes run beside the walk.
+   {4, 0, 0}.
      warps_per_block  4 or 8
      task_group       0: one warp per task (grid covers every task);
                       g > 0: persistent launch, each warp takes g tasks at a
