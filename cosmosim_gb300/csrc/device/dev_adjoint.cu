@@ -66,20 +66,20 @@ __global__ void k_adj_leaf_of(const NodeLink *__restrict__ link, const NodeW64 *
 // then read contiguous memory).
 __global__ void k_adj_gather(const int *__restrict__ perm, int n, const double *__restrict__ x,
                              const double *__restrict__ y, const double *__restrict__ z,
-                             const double *__restrict__ m, double4 *__restrict__ sb)
+                             const double *__restrict__ m, double4_32a *__restrict__ sb)
 {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n)
         return;
     const int j = perm[q];
-    sb[q] = make_double4(x[j], y[j], z[j], m[j]);
+    sb[q] = make_double4_32a(x[j], y[j], z[j], m[j]);
 }
 
 // Centre of mass and mass of every cell from the current positions of its
 // member bodies (sorted range [first, first+count) of sb); one warp per cell,
 // the lanes' partial sums combined by a fixed butterfly (deterministic).
 __global__ void k_adj_moments(const NodeLink *__restrict__ link, int nn,
-                              const double4 *__restrict__ sb, double4 *__restrict__ xm)
+                              const double4_32a *__restrict__ sb, double4_32a *__restrict__ xm)
 {
     const int w = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
@@ -88,7 +88,7 @@ __global__ void k_adj_moments(const NodeLink *__restrict__ link, int nn,
     const NodeLink l = link[w];
     double M = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
     for (int q = l.first + lane; q < l.first + l.count; q += CSG_WARP) {
-        const double4 b = sb[q];
+        const double4_32a b = sb[q];
         M += b.w;
         sx += b.w * b.x;
         sy += b.w * b.y;
@@ -99,12 +99,12 @@ __global__ void k_adj_moments(const NodeLink *__restrict__ link, int nn,
     sy = warp_sum(sy);
     sz = warp_sum(sz);
     if (lane == 0)
-        xm[w] = make_double4(sx / M, sy / M, sz / M, M);
+        xm[w] = make_double4_32a(sx / M, sy / M, sz / M, M);
 }
 
 // a_i from the body's list; one warp per body (lanes stride the list).
 __global__ void k_adj_forces(const int *__restrict__ offs, const int *__restrict__ ids,
-                             const double4 *__restrict__ xm, const double *__restrict__ x,
+                             const double4_32a *__restrict__ xm, const double *__restrict__ x,
                              const double *__restrict__ y, const double *__restrict__ z,
                              const double *__restrict__ m, int n, double G, double eps2,
                              double *__restrict__ ax, double *__restrict__ ay,
@@ -118,7 +118,7 @@ __global__ void k_adj_forces(const int *__restrict__ offs, const int *__restrict
     if (m[i] > 0.0) {
         const double px = x[i], py = y[i], pz = z[i];
         for (int k = offs[i] + lane; k < offs[i + 1]; k += CSG_WARP) {
-            const double4 c = xm[ids[k]];
+            const double4_32a c = xm[ids[k]];
             const double dx = c.x - px, dy = c.y - py, dz = c.z - pz;
             const double r2 = dx * dx + dy * dy + dz * dz + eps2;
             double inv3, inv5;
@@ -141,7 +141,7 @@ __global__ void k_adj_forces(const int *__restrict__ offs, const int *__restrict
 
 // Self term of (J^T mu)_i and the scatter of T mu_i into the cells' g.
 __global__ void k_adj_jt(const int *__restrict__ offs, const int *__restrict__ ids,
-                         const double4 *__restrict__ xm, const double *__restrict__ x,
+                         const double4_32a *__restrict__ xm, const double *__restrict__ x,
                          const double *__restrict__ y, const double *__restrict__ z,
                          const double *__restrict__ m, const double *__restrict__ mux,
                          const double *__restrict__ muy, const double *__restrict__ muz, int n,
@@ -158,7 +158,7 @@ __global__ void k_adj_jt(const int *__restrict__ offs, const int *__restrict__ i
         const double ux = mux[i], uy = muy[i], uz = muz[i];
         for (int k = offs[i] + lane; k < offs[i + 1]; k += CSG_WARP) {
             const int c = ids[k];
-            const double4 q = xm[c];
+            const double4_32a q = xm[c];
             const double dx = q.x - px, dy = q.y - py, dz = q.z - pz;
             const double r2 = dx * dx + dy * dy + dz * dz + eps2;
             double inv3, inv5;
@@ -188,7 +188,7 @@ __global__ void k_adj_jt(const int *__restrict__ offs, const int *__restrict__ i
 
 // (J^T mu)_j += m_j * sum over the cells containing j of g_c / M_c.
 __global__ void k_adj_push(const int *__restrict__ perm, const int *__restrict__ leaf_of,
-                           const NodeLink *__restrict__ link, const double4 *__restrict__ xm,
+                           const NodeLink *__restrict__ link, const double4_32a *__restrict__ xm,
                            const double *__restrict__ g, const double *__restrict__ m, int n_alive,
                            int nn, double *__restrict__ jx, double *__restrict__ jy,
                            double *__restrict__ jz, DevScalars *sc)
@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(DT2) k_adj_direct_forces(const double *__restr
                                                            double *__restrict__ ay,
                                                            double *__restrict__ az)
 {
-    __shared__ double4 sj[DT2];
+    __shared__ double4_32a sj[DT2];
     const int i = blockIdx.x * DT2 + threadIdx.x;
     const bool live = i < n && m[i] > 0.0;
     const double px = i < n ? x[i] : 0.0, py = i < n ? y[i] : 0.0, pz = i < n ? z[i] : 0.0;
@@ -235,15 +235,15 @@ __global__ void __launch_bounds__(DT2) k_adj_direct_forces(const double *__restr
     for (int t = 0; t < n; t += DT2) {
         __syncthreads();
         const int j = t + threadIdx.x;
-        sj[threadIdx.x] = (j < n) ? make_double4(x[j], y[j], z[j], m[j] > 0.0 ? m[j] : 0.0)
-                                  : make_double4(0.0, 0.0, 0.0, 0.0);
+        sj[threadIdx.x] = (j < n) ? make_double4_32a(x[j], y[j], z[j], m[j] > 0.0 ? m[j] : 0.0)
+                                  : make_double4_32a(0.0, 0.0, 0.0, 0.0);
         __syncthreads();
         const int cnt = min(DT2, n - t);
         if (live) {
             for (int q = 0; q < cnt; q++) {
                 if (t + q == i)
                     continue;
-                const double4 b = sj[q];
+                const double4_32a b = sj[q];
                 const double dx = b.x - px, dy = b.y - py, dz = b.z - pz;
                 const double r2 = dx * dx + dy * dy + dz * dz + eps2;
                 const double f = G * b.w / (r2 * sqrt(r2));
@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(DT2) k_adj_direct_jt(const double *__restrict_
                                                        double *__restrict__ jy,
                                                        double *__restrict__ jz)
 {
-    __shared__ double4 sp[DT2];
+    __shared__ double4_32a sp[DT2];
     __shared__ double3 su[DT2];
     const int j = blockIdx.x * DT2 + threadIdx.x;
     const bool live = j < n && m[j] > 0.0;
@@ -284,13 +284,13 @@ __global__ void __launch_bounds__(DT2) k_adj_direct_jt(const double *__restrict_
         __syncthreads();
         const int i = t + threadIdx.x;
         const bool li = i < n && m[i] > 0.0;
-        sp[threadIdx.x] = li ? make_double4(x[i], y[i], z[i], m[i]) : make_double4(0, 0, 0, 0);
+        sp[threadIdx.x] = li ? make_double4_32a(x[i], y[i], z[i], m[i]) : make_double4_32a(0, 0, 0, 0);
         su[threadIdx.x] = li ? make_double3(mux[i], muy[i], muz[i]) : make_double3(0, 0, 0);
         __syncthreads();
         const int cnt = min(DT2, n - t);
         if (live) {
             for (int q = 0; q < cnt; q++) {
-                const double4 b = sp[q];
+                const double4_32a b = sp[q];
                 if (t + q == j || b.w == 0.0)
                     continue;
                 const double3 u = su[q];
@@ -380,8 +380,8 @@ struct csg_adjoint {
     double *mu = nullptr;       // 3n
     double *jt = nullptr;       // 3n
     double *g = nullptr;        // 3 per cell
-    double4 *xm = nullptr;      // per cell
-    double4 *sb = nullptr;      // per sorted position: x y z m (moment pass)
+    double4_32a *xm = nullptr;      // per cell
+    double4_32a *sb = nullptr;      // per sorted position: x y z m (moment pass)
     int *counts = nullptr;      // n
     int *h_total = nullptr;     // pinned: list entries of the current substep
     std::vector<double> host_m, final_x, target;
@@ -665,7 +665,7 @@ CSG_EXPORT csg_adjoint *csg_adjoint_create(int n, const CsgSimParams *params, in
                 a->ckpt.push_back(c);
         }
         a->bytes = sizeof(double) * (6 * (size_t)n * (nck + 1) + 6 * (size_t)n + 3 * ncap) +
-                   sizeof(double4) * ncap + sizeof(int) * (size_t)n;
+                   sizeof(double4_32a) * ncap + sizeof(int) * (size_t)n;
     }
     if (rc) {
         csg_adjoint_destroy(a);

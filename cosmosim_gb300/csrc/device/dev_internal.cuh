@@ -175,7 +175,7 @@ struct csgd {
     NodeW64 *w64;
     NodeW32 *w32;
     NodeLink *link;
-    double4 *geo;
+    double4_32a *geo;
     NodeS32 *s32;
     int *child;   // 8 per node
     int *nchild;
@@ -226,16 +226,12 @@ __device__ __forceinline__ void dev_fail(DevScalars *sc, int code) { atomicCAS(&
 
 // FP32 value of a positive double whose exponent lies in FP32's normal range,
 // from its bits alone (exponent rebased from 1023 to 127, mantissa truncated
-// to 23 bits: relative error < 2^-23), and the exact double of a positive
-// normal float. Integer operations only: conversion instructions would run on
-// the FP64 pipe, the bottleneck of the FP64 force kernels on this GPU.
+// to 23 bits: relative error < 2^-23). Integer operations only: conversion
+// instructions would run on the FP64 pipe, the bottleneck of the FP64 force
+// kernels on this GPU.
 __device__ __forceinline__ float f32_from_f64_bits(long long b)
 {
     return __int_as_float((int)((b >> 29) - (896LL << 23)));
-}
-__device__ __forceinline__ double f64_from_f32_bits(float f)
-{
-    return __longlong_as_double(((long long)__float_as_int(f) + (896LL << 23)) << 29);
 }
 
 // y^2 (exact: 48 significant bits) and y^3 (rounded to nearest, < 2^-53

@@ -65,7 +65,7 @@ struct SphArgs {
     const int *type;
     double *h, *rho, *P, *u;
     double *ax, *ay, *az;
-    const double4 *geo;
+    const double4_32a *geo;
     const NodeS32 *s32;
     const NodeW64 *w64;
     DevScalars *sc;
@@ -116,7 +116,7 @@ __device__ __forceinline__ bool box_reaches(const NodeS32 &c, float qx, float qy
     const float hi = hx * hx + hy * hy + hz * hz;
     if (hi < r2f * (1.0f - FP32_EPS_SUM))
         return true;
-    const double4 g = a.geo[cell]; // too close to call in FP32
+    const double4_32a g = a.geo[cell]; // too close to call in FP32
     double gx = fmax(0.0, fabs(px - g.x) - g.w);
     double gy = fmax(0.0, fabs(py - g.y) - g.w);
     double gz = fmax(0.0, fabs(pz - g.z) - g.w);
@@ -455,7 +455,7 @@ __global__ void k_find_one(SphArgs a, double cx, double cy, double cz, double ra
     const double r2 = radius * radius;
     int c = 0, cur = 0;
     while (cur < nn && c < cap) {
-        const double4 g = a.geo[cur];
+        const double4_32a g = a.geo[cur];
         const int next = a.w64[cur].next, body = a.w64[cur].body;
         if (next <= cur) {
             dev_fail(a.sc, CSG_ERR_WALK_LIMIT);

@@ -863,7 +863,7 @@ __global__ void k_geometry(csgd_t dd, DevScalars *sc, const DevRoot *__restrict_
             cz = cz + oz * hs;
             hs = hs * 0.5;
         }
-        dd.geo[id] = make_double4(cx, cy, cz, hs);
+        dd.geo[id] = make_double4_32a(cx, cy, cz, hs);
         write_s32(dd, id, cx, cy, cz, hs, dd.w64[id].body, dd.w64[id].next);
     }
 }
@@ -919,7 +919,7 @@ __global__ void k_export(csgd_t dd, DevScalars *sc, OctreeNode *__restrict__ dst
     }
     for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < nn; id += gridDim.x * blockDim.x) {
         NodeW64 w = dd.w64[id];
-        double4 g = dd.geo[id];
+        double4_32a g = dd.geo[id];
         OctreeNode o;
         o.cx = w.cx;
         o.cy = w.cy;
@@ -1088,7 +1088,7 @@ __global__ void k_imp_write(csgd_t dd, DevScalars *sc, int nn, int root,
     v.s = (float)s;
     v.pad = 0.0f;
     dd.w32[id] = v;
-    dd.geo[id] = make_double4(o.center_x, o.center_y, o.center_z, o.half_size);
+    dd.geo[id] = make_double4_32a(o.center_x, o.center_y, o.center_z, o.half_size);
     write_s32(dd, id, o.center_x, o.center_y, o.center_z, o.half_size, w.body, w.next);
     dd.link[id] = NodeLink{-1, depth, -1, 0};
 }

@@ -18,9 +18,10 @@
 //   launch shapes). Openings decided as in the FP32 walk (equal to the
 //   reference's FP64 rounding); interactions queued and evaluated densely in
 //   FP64 — by a second warp per task in k_walk64ws — with 1/r^3 from an FP32
-//   rsqrt seed refined to full FP64 accuracy. k_walk64<EXACT=true> instead uses the reference's own
-//   operation sequence per step (1/(r2*sqrt(r2)), no fused multiply-add) —
-//   bit-identical results on the reference's own tree; used by parity tests.
+//   rsqrt seed by integer arithmetic (one rounding). k_walk64_exact instead
+//   uses the reference's own operation sequence per step (1/(r2*sqrt(r2)),
+//   no fused multiply-add) — bit-identical results on the reference's own
+//   tree; used by parity tests.
 // FP32-mixed walk: positions and centres as float hi/lo pairs (differences
 //   keep ~48 bits), rsqrt/products in FP32, Kahan-compensated FP32 sums per
 //   body. Openings within the FP32 error band of the threshold are decided in
@@ -132,23 +133,11 @@ __device__ __forceinline__ bool accept64(double s2, double d2, const WalkArgs &a
     return __ddiv_rn(s2, d2) < a.theta2;
 }
 
-__device__ __forceinline__ double inv_r3_fast(double r2)
-{
-    if (r2 >= 1e-30 && r2 <= 1e30) {
-        double y = (double)rsqrtf((float)r2);
-        // Newton steps on y^-2 = r2: y += y/2 * (1 - r2*y*y)
-        double e = fma(-r2 * y, y, 1.0);
-        y = fma(0.5 * y, e, y);
-        e = fma(-r2 * y, y, 1.0);
-        y = fma(0.5 * y, e, y);
-        return y * y * y;
-    }
-    return 1.0 / (r2 * sqrt(r2));
-}
-
-template <bool EXACT, bool STATS>
-__device__ __forceinline__ void walk64_task(const WalkArgs &a, NodeW64 *win, const TaskRange &tr,
-                                            WalkStats &st)
+// The reference's own FP64 operation sequence per step, one warp per task,
+// no fused multiply-add: bit-identical accelerations on the reference's tree.
+template <bool STATS>
+__device__ __forceinline__ void walk64_exact_task(const WalkArgs &a, NodeW64 *win,
+                                                  const TaskRange &tr, WalkStats &st)
 {
     const int lane = threadIdx.x & 31;
     const int nn = tr.end;
@@ -177,43 +166,28 @@ __device__ __forceinline__ void walk64_task(const WalkArgs &a, NodeW64 *win, con
             if (c.m == 0.0) { // empty cell: reference returns at once (src/octree.c:181-182)
                 skip = c.next;
             } else {
-                double dx, dy, dz, d2;
-                if (EXACT) {
-                    dx = __dsub_rn(c.cx, px);
-                    dy = __dsub_rn(c.cy, py);
-                    dz = __dsub_rn(c.cz, pz);
-                    d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
-                                   __dmul_rn(dz, dz));
-                } else {
-                    dx = c.cx - px;
-                    dy = c.cy - py;
-                    dz = c.cz - pz;
-                    d2 = dx * dx + dy * dy + dz * dz;
-                }
+                const double dx = __dsub_rn(c.cx, px);
+                const double dy = __dsub_rn(c.cy, py);
+                const double dz = __dsub_rn(c.cz, pz);
+                const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)),
+                                            __dmul_rn(dz, dz));
                 bool take;
                 if (c.body >= 0) {
                     take = (c.body != me);
                 } else {
-                    take = EXACT ? (d2 > 0.0 && __ddiv_rn(c.s2, d2) < a.theta2) : accept64(c.s2, d2, a);
+                    take = d2 > 0.0 && __ddiv_rn(c.s2, d2) < a.theta2;
                     if (take)
                         skip = c.next;
                     else
                         open = true;
                 }
                 if (take) {
-                    if (EXACT) {
-                        double r2 = __dadd_rn(d2, a.eps2);
-                        double inv = __ddiv_rn(1.0, __dmul_rn(r2, __dsqrt_rn(r2)));
-                        double gm = __dmul_rn(a.G, c.m);
-                        sx = __dadd_rn(sx, __dmul_rn(__dmul_rn(gm, dx), inv));
-                        sy = __dadd_rn(sy, __dmul_rn(__dmul_rn(gm, dy), inv));
-                        sz = __dadd_rn(sz, __dmul_rn(__dmul_rn(gm, dz), inv));
-                    } else {
-                        double f = a.G * c.m * inv_r3_fast(d2 + a.eps2);
-                        sx = fma(f, dx, sx);
-                        sy = fma(f, dy, sy);
-                        sz = fma(f, dz, sz);
-                    }
+                    const double r2 = __dadd_rn(d2, a.eps2);
+                    const double inv = __ddiv_rn(1.0, __dmul_rn(r2, __dsqrt_rn(r2)));
+                    const double gm = __dmul_rn(a.G, c.m);
+                    sx = __dadd_rn(sx, __dmul_rn(__dmul_rn(gm, dx), inv));
+                    sy = __dadd_rn(sy, __dmul_rn(__dmul_rn(gm, dy), inv));
+                    sz = __dadd_rn(sz, __dmul_rn(__dmul_rn(gm, dz), inv));
                     if (STATS)
                         st.hits++;
                 }
@@ -245,13 +219,13 @@ __device__ __forceinline__ void add_hits(const WalkArgs &a, const WalkStats &w)
     }
 }
 
-template <bool EXACT, bool STATS>
-__global__ void __launch_bounds__(8 * CSG_WARP) k_walk64(WalkArgs a)
+template <bool STATS>
+__global__ void __launch_bounds__(8 * CSG_WARP) k_walk64_exact(WalkArgs a)
 {
     __shared__ NodeW64 win_all[8][CSG_WARP];
     NodeW64 *win = win_all[threadIdx.x >> 5];
     WalkStats st;
-    for_each_task<8, false>(a, [&](const TaskRange &tr) { walk64_task<EXACT, STATS>(a, win, tr, st); });
+    for_each_task<8, false>(a, [&](const TaskRange &tr) { walk64_exact_task<STATS>(a, win, tr, st); });
     if (STATS)
         add_hits(a, st);
 }
@@ -972,9 +946,9 @@ void launch_walk(csgd_t *d, const WalkArgs &a, int precision, int exact)
         grid = 1;
     if (exact) {
         if (stats)
-            k_walk64<true, true><<<grid, 8 * CSG_WARP, 0, s>>>(b);
+            k_walk64_exact<true><<<grid, 8 * CSG_WARP, 0, s>>>(b);
         else
-            k_walk64<true, false><<<grid, 8 * CSG_WARP, 0, s>>>(b);
+            k_walk64_exact<false><<<grid, 8 * CSG_WARP, 0, s>>>(b);
     } else if (precision == CSG_PREC_FP32_MIXED) {
         if (W == 4)
             CSG_LAUNCH_WALK(k_walk32, 4, grid, s, b);
