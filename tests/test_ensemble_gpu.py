@@ -39,9 +39,12 @@ def _make(lib, sizes=SIZES, dead=5):
     return parts
 
 
-@pytest.mark.parametrize("prec", [0, 1])
-def test_ensemble_equals_separate_handles(lib, prec):
-    parts = _make(lib)
+@pytest.mark.parametrize("prec,sizes", [(0, SIZES), (1, SIZES),
+                                        # 42.5k bodies: the FP64 walk of the ensemble takes the
+                                        # two-pairs-per-block layout, each system alone one pair
+                                        (0, [30000, 517, 12000])])
+def test_ensemble_equals_separate_handles(lib, prec, sizes):
+    parts = _make(lib, sizes)
     allb = _concat(parts)
     kw = dict(softening=0.01, theta=0.5, dt=1e-3, precision=prec)
     ens = lib.Sim.ensemble(allb, [len(p) for p in parts], **kw)

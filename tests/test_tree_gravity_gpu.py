@@ -182,9 +182,10 @@ def test_fp32_mixed_precision_error(lib):
 
 
 def test_oracle_agrees_on_random_trees(lib, orc):
-    """Fresh random inputs (not in any fixture): tree and forces vs the oracle."""
+    """Fresh random inputs (not in any fixture): tree and forces vs the oracle
+    (60,000 bodies: the FP64 walk's two-pairs-per-block layout)."""
     rng = np.random.default_rng(99)
-    for n in (5, 64, 777, 20000):
+    for n in (5, 64, 777, 20000, 60000):
         b = np.zeros(n, dtype=BODY_DTYPE)
         b["x"] = rng.standard_cauchy(n) * 0.3
         b["y"] = rng.normal(0, 1, n)
