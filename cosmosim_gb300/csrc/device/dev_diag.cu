@@ -193,9 +193,11 @@ extern "C" int csgd_direct_forces(csgd_t *d, const int *host_idx, int ns, double
 {
     if (ns <= 0)
         return CSG_OK;
-    if (ns > d->n) {
+    if (ns > d->n || !host_idx)
         return CSG_ERR_BAD_ARG;
-    }
+    for (int k = 0; k < ns; k++)
+        if (host_idx[k] < 0 || host_idx[k] >= d->n)
+            return CSG_ERR_BAD_ARG;
     int *didx = nullptr;
     double *part = nullptr, *out = nullptr;
     cudaError_t e = cudaMalloc((void **)&didx, sizeof(int) * (size_t)ns);
@@ -329,18 +331,23 @@ double *g_noalloc_ptr[NOALLOC_MAX_DEVICES];
 __global__ void __launch_bounds__(DT) k_direct_noalloc(const double *__restrict__ x,
                                                        const double *__restrict__ y,
                                                        const double *__restrict__ z,
-                                                       const double *__restrict__ m, int n,
+                                                       const double *__restrict__ m,
+                                                       const int *__restrict__ sys, int n,
                                                        const int *__restrict__ idx, int ns,
                                                        double G, double eps2,
                                                        double *__restrict__ part)
 {
     __shared__ double sx[DT], sy[DT], sz[DT], sm[DT];
+    __shared__ int sg[DT];
     const int k = blockIdx.x * DT + threadIdx.x;
     const int chunk = blockIdx.y;
     const int per = (n + NOALLOC_CHUNKS - 1) / NOALLOC_CHUNKS;
     const int j0 = chunk * per, j1 = min(n, j0 + per);
+    // A sample index outside [0, n) reads nothing: its row becomes NaN.
     const int i = (k < ns) ? idx[k] : -1;
-    const double xi = (i >= 0) ? x[i] : 0.0, yi = (i >= 0) ? y[i] : 0.0, zi = (i >= 0) ? z[i] : 0.0;
+    const bool valid = (unsigned)i < (unsigned)n;
+    const double xi = valid ? x[i] : 0.0, yi = valid ? y[i] : 0.0, zi = valid ? z[i] : 0.0;
+    const int gi = (valid && sys) ? sys[i] : 0; // only bodies of the same system attract
     double ax = 0.0, ay = 0.0, az = 0.0;
     for (int t = j0; t < j1; t += DT) {
         const int j = t + threadIdx.x;
@@ -350,12 +357,13 @@ __global__ void __launch_bounds__(DT) k_direct_noalloc(const double *__restrict_
             sy[threadIdx.x] = y[j];
             sz[threadIdx.x] = z[j];
             sm[threadIdx.x] = (m[j] <= 0.0) ? 0.0 : m[j];
+            sg[threadIdx.x] = sys ? sys[j] : 0;
         }
         __syncthreads();
         const int cnt = min(DT, j1 - t);
-        if (i >= 0) {
+        if (valid) {
             for (int q = 0; q < cnt; q++) {
-                if (t + q == i)
+                if (t + q == i || sg[q] != gi)
                     continue;
                 double dx = sx[q] - xi, dy = sy[q] - yi, dz = sz[q] - zi;
                 double r2 = dx * dx + dy * dy + dz * dz + eps2;
@@ -368,6 +376,8 @@ __global__ void __launch_bounds__(DT) k_direct_noalloc(const double *__restrict_
         }
     }
     if (k < ns) {
+        if (!valid)
+            ax = ay = az = __longlong_as_double(0x7ff8000000000000ll);
         double *p = part + ((size_t)chunk * ns + k) * 3;
         p[0] = ax;
         p[1] = ay;
@@ -393,7 +403,10 @@ __global__ void k_direct_noalloc_sum(const double *__restrict__ part, int ns,
 
 // The device address of the scratch array on the current device, looked up
 // once per device (the first call on a device does it, so that call should
-// come before any stream capture on that device).
+// come before any stream capture on that device). The address belongs to the
+// device's primary context: after a cudaDeviceReset the cached address is
+// stale, so a process that resets a device must not call the entry point on
+// it again.
 static int noalloc_scratch(double **ptr)
 {
     int dev = 0;
@@ -415,9 +428,10 @@ static int noalloc_scratch(double **ptr)
 }
 
 extern "C" CSG_EXPORT int csg_direct_forces_noalloc(const double *x, const double *y,
-                                                    const double *z, const double *mass, int n,
-                                                    const int *idx, int m, double G,
-                                                    double softening, double *out, void *stream)
+                                                    const double *z, const double *mass,
+                                                    const int *sys, int n, const int *idx, int m,
+                                                    double G, double softening, double *out,
+                                                    void *stream)
 {
     if (n < 0 || m < 0 || m > NOALLOC_MAX_SAMPLE)
         return CSG_ERR_BAD_ARG;
@@ -431,7 +445,7 @@ extern "C" CSG_EXPORT int csg_direct_forces_noalloc(const double *x, const doubl
         return rc;
     cudaStream_t s = (cudaStream_t)stream;
     dim3 grid((m + DT - 1) / DT, NOALLOC_CHUNKS);
-    k_direct_noalloc<<<grid, DT, 0, s>>>(x, y, z, mass, n, idx, m, G, softening * softening, part);
+    k_direct_noalloc<<<grid, DT, 0, s>>>(x, y, z, mass, sys, n, idx, m, G, softening * softening, part);
     k_direct_noalloc_sum<<<(m + 255) / 256, 256, 0, s>>>(part, m, out);
     if (cudaGetLastError() != cudaSuccess)
         return CSG_ERR_CUDA;

@@ -98,7 +98,7 @@ _SIGS = {
                             ctypes.POINTER(ctypes.c_int64)], _i),
     "csg_sort_keys": ([_vp, _i, _i, _vp, _vp], _i),
     "cosmosim_enable_graphs": ([_vp, _i], _i),
-    "csg_direct_forces_noalloc": ([_vp, _vp, _vp, _vp, _i, _vp, _i, _d, _d, _vp, _vp], _i),
+    "csg_direct_forces_noalloc": ([_vp, _vp, _vp, _vp, _vp, _i, _vp, _i, _d, _d, _vp, _vp], _i),
     "cosmosim_create_ensemble": ([_vp, _i, _i, _ip, ctypes.POINTER(CsgSimParams)], _vp),
     "cosmosim_system_count": ([_vp], _i),
     "cosmosim_set_walk_shape": ([_vp, ctypes.POINTER(CsgWalkShape)], _i),

@@ -181,8 +181,10 @@ CSG_EXPORT int cosmosim_set_precision(SimHandle handle, int precision);
 
 /* FP64 diagnostics on the handle's current bodies (blocking): direct-sum
    accelerations of the m bodies listed in idx into out[3*m] (the formula of
-   the reference's test helper, tests/test_physics.c:54-71), and kinetic /
-   softened potential energy (tests/test_physics.c:34-52, O(n^2)). */
+   the reference's test helper, tests/test_physics.c:54-71; in an ensemble
+   only bodies of the same system attract; every idx must lie in [0, count),
+   else CSG_ERR_BAD_ARG), and kinetic / softened potential energy
+   (tests/test_physics.c:34-52, O(n^2)). */
 CSG_EXPORT int cosmosim_direct_forces(SimHandle handle, const int *idx, int m, double *out);
 CSG_EXPORT int cosmosim_energy(SimHandle handle, double *kinetic, double *potential);
 
@@ -215,15 +217,21 @@ CSG_EXPORT int csg_sort_keys(const uint64_t *keys, int n, int bits, uint64_t *ou
    engine or renderer with a fixed GPU budget and its own allocator, a
    real-time thread that must not block on cudaMalloc/cudaFree): all pointers
    are device pointers the caller already owns — x, y, z, mass (n bodies, SoA),
-   idx (m sample indices) and out (3*m doubles); the work is queued on the
-   given cudaStream_t and not waited for. Scratch is a fixed 1.5 MiB array
-   inside the library, so m may be at most 4096 (larger m: CSG_ERR_BAD_ARG).
-   The first call on each device looks up that array's address, so make it
-   before any stream capture on that device. Calls share the array: calls
-   that overlap on the GPU race. Same formula as cosmosim_direct_forces. */
+   sys (n system ids, or NULL when all n bodies form one system), idx (m
+   sample indices) and out (3*m doubles); the work is queued on the given
+   cudaStream_t and not waited for. Body i is attracted by every other body j
+   with sys[j] == sys[i] (all bodies when sys is NULL), mass <= 0 counting as
+   0: the formula and system rule of cosmosim_direct_forces. A sample index
+   outside [0, n) reads no body; its row of out is NaN. Scratch is a fixed
+   1.5 MiB array inside the library, so m may be at most 4096 (larger m:
+   CSG_ERR_BAD_ARG). The first call on each device looks up that array's
+   address, so make it before any stream capture on that device; the address
+   is cached per device and does not survive a cudaDeviceReset. Calls share
+   the array: calls that overlap on the GPU race. */
 CSG_EXPORT int csg_direct_forces_noalloc(const double *x, const double *y, const double *z,
-                                         const double *mass, int n, const int *idx, int m,
-                                         double G, double softening, double *out, void *stream);
+                                         const double *mass, const int *sys, int n,
+                                         const int *idx, int m, double G, double softening,
+                                         double *out, void *stream);
 
 /* ---- Adjoint of the kick-drift-kick leapfrog -------------------------------
    No counterpart in the reference. Differentiates a T-substep FP64 run
