@@ -7,18 +7,28 @@ mass ratio 1:1.2, 50 deg tilt, 10% SPH gas, theta 0.5, softening 0.01,
 dt 1e-3 — seeded synthetic initial conditions of that shape (no dataset).
 A step is one kick-drift-kick substep: tree build, gravity walk, SPH density
 and forces, kicks, cooling. The headline `value` is the FP32-mixed walk; the
-FP64 plain walk is measured on the same workload beside it.
+FP64 plain walk is measured on the same workload beside it, over the same K
+substeps.
 
 Timing: W untimed warm-up substeps, then K substeps each bracketed by CUDA
 events on the library's stream (torch's current stream), with a 512 MB write
 between substeps to flush L2 (the 100k working set fits in L2). `e2e` is the
 same metric through the reference-facing C call integrator_step() with the
-Body array and pool in pinned host memory, host<->device copies included.
-Under torchrun (N > 1) every rank runs an independent replica (the path does
-not shard: replicas only); value = all ranks' body-substeps / max time.
+Body array and pool in pinned host memory, host<->device copies included
+(K calls). Under torchrun (N > 1) every rank runs an independent replica (the
+path does not shard: replicas only); value = all ranks' body-substeps / max
+time.
+
+At N = 1 the line also carries `targets_1m`: the 1,000,000-body bulge + disk
+at theta 0.3 and 0.5 (softening 0.005), FP32-mixed and FP64 plain over K
+substeps each, their force errors against an FP64 direct sum on a seeded
+4096-body sample, and the reference's CPU algorithm on the host cores at the
+same theta (bounded sample) — the FP32/FP64 and FP64/CPU ratios the targets
+are stated on.
 
 --impl reference times the reference's CPU algorithm (the oracle port in
-oracle/, OpenMP on all host cores) on the same workload.
+oracle/, OpenMP on all host cores) on the same workload; it draws its bodies
+with the oracle's generator and never loads the product library.
 """
 import argparse
 import json
@@ -58,6 +68,12 @@ FLOP_PER_INTERACTION = 20  # monopole body-cell interaction: 3 sub, 3 fma d2, rs
 WALK32_DRAM_BYTES_PER_BODY = 10.06e6 / 100_000
 # issue slots busy in the same capture (k_walk32, 100k merger): 57.8%
 WALK32_ISSUE_BUSY = 0.578
+WALK32_NOTE = ("20 flop per reference interaction / walk event time; peak = FP32 FMA throughput "
+               "measured live by csg_measure_fp_peaks (the walk is CUDA-core bound: no dense "
+               "contraction, tree resident in L2). What bounds it is instruction issue in the "
+               "traversal. traffic and issue_slots_busy_ncu are per-launch DRAM bytes and issue "
+               "activity from the committed ncu capture of k_walk32 on the 100k merger "
+               "(profiles/), traffic scaled by the body count")
 SEED = 0x5EED0000
 
 
@@ -80,9 +96,12 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+    """nvidia-smi samples (every 200 ms) of SM clock and throttle reasons over
+    the whole run of the GPU legs. Timed regions are marked with window();
+    the reported median is over the samples that fall inside them (all
+    samples of the run when fewer than 3 do), the reasons over every sample."""
 
-    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -90,6 +109,7 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.lines = []
+        self.windows = []
 
     def start(self):
         try:
@@ -104,32 +124,40 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.time(), line.strip()))
+
+    def window(self, t0, t1):
+        self.windows.append((t0, t1))
 
     def stop(self):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        sm, mx, reasons = [], [], set()
+        rows, reasons = [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for t, ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 8:
+            if len(parts) < 9:
                 continue
             try:
-                sm.append(float(parts[0]))
-                mx.append(float(parts[1]))
+                rows.append((t, float(parts[1]), float(parts[2])))
             except ValueError:
                 continue
-            for name, v in zip(names, parts[4:8]):
+            for name, v in zip(names, parts[5:9]):
                 if v.lower() == "active":
                     reasons.add(name)
-        return {"sm_mhz": float(np.median(sm)) if sm else None,
-                "sm_max_mhz": max(mx) if mx else None, "samples": len(sm),
+        # a sample read at t covers roughly [t - 0.2 s, t]
+        inside = [r for r in rows if any(a - 0.05 <= r[0] <= b + 0.25 for a, b in self.windows)]
+        use = inside if len(inside) >= 3 else rows
+        return {"sm_mhz": float(np.median([r[1] for r in use])) if use else None,
+                "sm_max_mhz": max(r[2] for r in rows) if rows else None,
+                "samples": len(rows), "samples_in_timed_regions": len(inside),
+                "median_over": "timed regions" if use is inside else "whole GPU run",
                 "reasons": sorted(reasons)}
 
 
@@ -137,17 +165,21 @@ def flush_buffer(torch):
     return torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
 
 
-def time_substeps(torch, sim, k, flush):
+def time_substeps(torch, sim, k, flush, sampler=None):
     """Sum of per-substep device times (events on the launching stream)."""
     st = torch.cuda.current_stream()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
            for _ in range(k)]
+    torch.cuda.synchronize()
+    t0 = time.time()
     for a, b in evs:
         flush.zero_()
         a.record(st)
         sim.substeps_async(1)
         b.record(st)
     torch.cuda.synchronize()
+    if sampler:
+        sampler.window(t0, time.time())
     return sum(a.elapsed_time(b) for a, b in evs) / 1e3
 
 
@@ -175,8 +207,10 @@ def acc(b):
     return np.stack([b["ax"], b["ay"], b["az"]], axis=1)
 
 
-def run_cuda(args, torch, lib, cfg, rank, world):
-    dev = torch.cuda.current_device()
+def run_cuda(args, torch, lib, cfg, rank, world, sampler):
+    """The headline workload: FP32-mixed and FP64 substeps timed on the
+    device (K substeps each), their phases and walk counters, the force
+    errors, and K end-to-end integrator_step calls on pinned host buffers."""
     stream = torch.cuda.current_stream()
     assert stream.cuda_stream != 0, "the library needs a non-default stream handle"
     flush = flush_buffer(torch)
@@ -184,7 +218,6 @@ def run_cuda(args, torch, lib, cfg, rank, world):
     n_alive = int((bodies["mass"] > 0).sum())
     common = dict(softening=cfg["eps"], theta=cfg["theta"], dt=cfg["dt"], sph=cfg["sph"])
     out = {}
-    clocks = None
     for prec, name in ((lib.PREC_FP32_MIXED, "fp32_mixed"), (lib.PREC_FP64, "fp64")):
         sim = lib.Sim.from_bodies(bodies, precision=prec, **common)
         sim.set_stream(stream.cuda_stream)
@@ -192,18 +225,13 @@ def run_cuda(args, torch, lib, cfg, rank, world):
             flush.zero_()
             sim.substeps_async(1)
         torch.cuda.synchronize()
-        k = args.steps if name == "fp32_mixed" else max(3, args.steps // args.fp64_divisor)
+        k = args.steps
         l0 = sim.launch_count()
-        sampler = ClockSampler(dev) if name == "fp32_mixed" else None
-        if sampler:
-            sampler.start()
         if world > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
-        secs = time_substeps(torch, sim, k, flush)
+        secs = time_substeps(torch, sim, k, flush, sampler)
         sim.sync()  # raises if any substep reported an error
-        if sampler:
-            clocks = sampler.stop()
         launches = sim.launch_count() - l0
         # phases on the state reached: tree build and gravity walk alone
         build_s = time_phase(torch, sim.build_tree_async, 5, flush)
@@ -242,19 +270,20 @@ def run_cuda(args, torch, lib, cfg, rank, world):
     pool = pool_t.numpy().view(NODE_DTYPE)
     lib.set_precision(lib.PREC_FP32_MIXED)
     lib.integrator_init_accelerations(hb, 1.0, cfg["eps"], cfg["theta"], pool)
-    for _ in range(2):
+    for _ in range(args.warmup):
         lib.integrator_step(hb, cfg["dt"], 1.0, cfg["eps"], cfg["theta"], pool, int(cfg["sph"]))
-    ke = max(3, args.steps // args.e2e_divisor)
+    ke = args.steps
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
+    t0w, t0 = time.time(), time.perf_counter()
     for _ in range(ke):
         lib.integrator_step(hb, cfg["dt"], 1.0, cfg["eps"], cfg["theta"], pool, int(cfg["sph"]))
     e2e_s = time.perf_counter() - t0
+    sampler.window(t0w, time.time())
     lib.set_precision(lib.PREC_FP64)
     _, nodes = lib.octree_build(hb, pool)
-    return dict(n_alive=n_alive, runs=out, errors=errors, clocks=clocks, e2e_s=e2e_s, e2e_steps=ke,
+    return dict(n_alive=n_alive, runs=out, errors=errors, e2e_s=e2e_s, e2e_steps=ke,
                 e2e_nodes=nodes)
 
 
@@ -264,11 +293,13 @@ def ensemble_sizes():
     return np.exp(r.uniform(lo, hi, ENSEMBLE["n_gal"])).astype(np.int64)
 
 
-def ensemble_bodies(lib, rank):
+def ensemble_bodies(gen, rank):
+    """The 64 galaxies, drawn by gen (the library's or the oracle's
+    generate_ics: byte-identical)."""
     from cosmosim_gb300.abi import BODY_DTYPE
 
     sizes = ensemble_sizes()
-    parts = [lib.generate_ics(3, int(n), SEED + 1000 * rank + g) for g, n in enumerate(sizes)]
+    parts = [gen(3, int(n), SEED + 1000 * rank + g) for g, n in enumerate(sizes)]
     return np.concatenate(parts).astype(BODY_DTYPE), parts
 
 
@@ -294,7 +325,7 @@ def run_ensemble(args, torch, lib, rank, world):
     stream = torch.cuda.current_stream()
     flush = flush_buffer(torch)
     t0 = time.perf_counter()
-    allb, parts = ensemble_bodies(lib, rank)
+    allb, parts = ensemble_bodies(lib.generate_ics, rank)
     t_host_ics = time.perf_counter() - t0
     sizes = [len(p) for p in parts]
     n_total = len(allb)
@@ -319,9 +350,8 @@ def run_ensemble(args, torch, lib, rank, world):
     if world > 1:
         torch.distributed.barrier()
     l0 = ens.launch_count()
-    secs = time_substeps(torch, ens, args.steps, flush)
+    secs = time_substeps(torch, ens, args.steps, flush, sampler)
     ens.sync()
-    clocks = sampler.stop()
     launches = ens.launch_count() - l0
     build_s = time_phase(torch, ens.build_tree_async, 5, flush)
     walk_s = time_phase(torch, ens.gravity_async, 5, flush)
@@ -336,29 +366,30 @@ def run_ensemble(args, torch, lib, rank, world):
     hin = pin_in.numpy().view(allb.dtype)
     hout = pin_out.numpy().view(allb.dtype)
     hin[:] = state
-    ke = max(3, args.steps // args.e2e_divisor)
+    ke = args.steps
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
+    t0w, t0 = time.time(), time.perf_counter()
     for _ in range(ke):
         ens.set_bodies(hin)
         ens.substeps_async(1)
         lib.load().cosmosim_copy_bodies(ens.h, hout.ctypes.data, n_total)
     e2e_s = time.perf_counter() - t0
+    sampler.window(t0w, time.time())
     ens.sync()
     ens.close()
     res["fp32"] = dict(secs=secs, steps=args.steps, launches=launches, build_s=build_s,
                        walk_s=walk_s, interactions=inter)
     # the batched handle, FP64 plain (default walk shape)
-    k64 = max(3, args.steps // args.fp64_divisor)
+    k64 = args.steps
     ens64 = lib.Sim.ensemble(allb, sizes, precision=lib.PREC_FP64, **common)
     ens64.set_stream(stream.cuda_stream)
     for _ in range(args.warmup):
         ens64.substeps_async(1)
-    res["fp64"] = dict(secs=time_substeps(torch, ens64, k64, flush), steps=k64)
+    res["fp64"] = dict(secs=time_substeps(torch, ens64, k64, flush, sampler), steps=k64)
     ens64.sync()
     ens64.close()
     # the same galaxies as 64 separate handles, stepped one after another
-    kseq = max(3, args.steps // args.fp64_divisor)
+    kseq = args.steps
     for prec, name in ((lib.PREC_FP64, "seq_fp64"), (lib.PREC_FP32_MIXED, "seq_fp32")):
         sims = [lib.Sim.from_bodies(p, precision=prec, **common) for p in parts]
         for sm in sims:
@@ -375,6 +406,7 @@ def run_ensemble(args, torch, lib, rank, world):
         for sm in sims:
             sm.sync()
             sm.close()
+    clocks = sampler.stop()
     # per-galaxy error of the FP32-mixed walk vs the FP64 walk, and of both
     # against an FP64 direct sum on 64 bodies per galaxy (4096 in all)
     g64 = lib.Sim.ensemble(state, sizes, precision=lib.PREC_FP64, **common)
@@ -460,7 +492,6 @@ def ensemble_line(args, torch, lib, rank, world, fp32_peak):
 def ensemble_reference(args, world):
     """The reference's CPU algorithm over the 64 galaxies (one system at a time,
     as the reference runs them), substep sweeps within --cpu-budget seconds."""
-    from cosmosim_gb300 import lib
     from cosmosim_gb300.abi import NODE_DTYPE
     from oracle import orc
 
@@ -468,7 +499,7 @@ def ensemble_reference(args, world):
     o = orc.Oracle()
     cores = o.set_threads(os.cpu_count() or 1)
     e = ENSEMBLE
-    _, parts = ensemble_bodies(lib, 0)
+    _, parts = ensemble_bodies(o.generate_ics, 0)
     pools = [np.zeros(8 * len(p), dtype=NODE_DTYPE) for p in parts]
     for p, pool in zip(parts, pools):
         o.integrator_init_accelerations(p, 1.0, e["eps"], e["theta"], pool)
@@ -582,9 +613,10 @@ def adjoint_line(args):
     }
 
 
-def theta_sweep(args, torch, lib, cfg, thetas, flush):
-    """Per opening angle: FP32-mixed and FP64 ms/substep, walk times, and the
-    force errors (FP32 vs FP64 walk; both vs FP64 direct sum on 4096 bodies)."""
+def theta_sweep(args, torch, lib, cfg, thetas, flush, k, sampler=None):
+    """Per opening angle: FP32-mixed and FP64 ms/substep over k timed
+    substeps, walk times, and the force errors of the initial state (FP32 vs
+    FP64 walk; both vs an FP64 direct sum on a seeded 4096-body sample)."""
     stream = torch.cuda.current_stream()
     bodies = lib.generate_ics(cfg["kind"], cfg["n"], SEED)
     alive = bodies["mass"] > 0
@@ -600,18 +632,19 @@ def theta_sweep(args, torch, lib, cfg, thetas, flush):
                                       sph=cfg["sph"], precision=prec)
             sim.set_stream(stream.cuda_stream)
             accs[name] = acc(sim.bodies())
-            for _ in range(3):
+            for _ in range(args.warmup):
                 sim.substeps_async(1)
-            k = max(3, args.steps // (4 if name == "fp32_mixed" else 4 * args.fp64_divisor))
-            secs = time_substeps(torch, sim, k, flush)
+            secs = time_substeps(torch, sim, k, flush, sampler)
+            sim.sync()
             walk_s = time_phase(torch, sim.gravity_async, 3, flush)
             sim.enable_stats(True)
             sim.gravity_async()
             inter = sim.interactions()
             sim.close()
             row[name] = {"body_substeps_per_s": n_alive * k / secs, "ms_per_substep": 1e3 * secs / k,
-                         "walk_ms": 1e3 * walk_s,
-                         "interactions_per_body": inter / n_alive}
+                         "steps": k, "walk_ms": 1e3 * walk_s,
+                         "interactions_per_body": inter / n_alive,
+                         "walk_tflops": FLOP_PER_INTERACTION * inter / walk_s / 1e12}
         g = lib.Sim.from_bodies(bodies, softening=cfg["eps"], theta=th)
         direct = g.direct_forces(sample)
         g.close()
@@ -622,6 +655,28 @@ def theta_sweep(args, torch, lib, cfg, thetas, flush):
                          "fp64_walk_vs_direct": rel_err_stats(accs["fp64"][sample], direct),
                          "fp32_walk_vs_direct": rel_err_stats(accs["fp32_mixed"][sample], direct)}
         out[str(th)] = row
+    return out
+
+
+def target_leg(args, torch, lib, flush, sampler):
+    """The stated targets, on the 1M bulge + disk at theta 0.3 and 0.5:
+    FP32-mixed >= 5x FP64 plain at force error <= 1e-3 against an FP64 direct
+    sum (4096-body sample; median), and FP64 plain >= 50x the reference's CPU
+    algorithm on the host cores (main() adds that CPU sample after every
+    GPU leg has run)."""
+    cfg = CONFIGS["bulge1m"]
+    thetas = (0.3, 0.5)
+    rows = theta_sweep(args, torch, lib, cfg, thetas, flush, args.steps, sampler)
+    out = {"workload": f"bulge1m: {cfg['desc']}", "n_bodies": cfg["n"], "softening": cfg["eps"],
+           "dt": cfg["dt"], "steps": args.steps, "thetas": {}}
+    for th in thetas:
+        row = rows[str(th)]
+        err = row["errors"]["fp32_walk_vs_direct"]["median"]
+        t = {"fp32_mixed": row["fp32_mixed"], "fp64_plain": row["fp64"],
+             "fp32_over_fp64": row["fp32_mixed_speedup"], "errors": row["errors"],
+             "fp32_err_vs_direct_median": err,
+             "target_5x_at_err_1e-3": bool(row["fp32_mixed_speedup"] >= 5.0 and err <= 1e-3)}
+        out["thetas"][str(th)] = t
     return out
 
 
@@ -652,15 +707,15 @@ def cpu_reference(cfg, steps, seed=SEED, time_budget=None, warmup=0, warmup_budg
     """The reference's CPU algorithm (oracle port, OpenMP on every host core):
     `warmup` untimed substeps (at most `warmup_budget` seconds of them), then
     `steps` timed ones (stopping early, after at least 2, once `time_budget`
-    seconds have passed)."""
-    from cosmosim_gb300 import lib
+    seconds have passed). The bodies come from the oracle's generator (equal
+    byte for byte to the library's): this leg never loads the library."""
     from cosmosim_gb300.abi import NODE_DTYPE
     from oracle import orc
 
     orc.build()
     o = orc.Oracle()
     cores = o.set_threads(os.cpu_count() or 1)
-    b = lib.generate_ics(cfg["kind"], cfg["n"], seed)
+    b = o.generate_ics(cfg["kind"], cfg["n"], seed)
     pool = np.zeros(8 * cfg["n"], dtype=NODE_DTYPE)
     o.integrator_init_accelerations(b, 1.0, cfg["eps"], cfg["theta"], pool)
     tw = time.perf_counter()
@@ -685,14 +740,13 @@ def cpu_reference(cfg, steps, seed=SEED, time_budget=None, warmup=0, warmup_budg
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="cuda", choices=["cuda", "reference"])
     ap.add_argument("--config", default="merger100k",
                     choices=sorted(CONFIGS) + ["ensemble64", "adjoint10k"])
-    ap.add_argument("--fp64-divisor", type=int, default=8,
-                    help="FP64 run times steps/divisor substeps")
-    ap.add_argument("--e2e-divisor", type=int, default=8)
+    ap.add_argument("--no-targets", action="store_true",
+                    help="skip the 1M-body target leg (theta 0.3 and 0.5) of the default line")
     ap.add_argument("--cpu-budget", type=float, default=20.0,
                     help="seconds of CPU work for the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -797,7 +851,13 @@ def main():
             sim.close()
         return
     fp32_peak, fp64_peak = lib.measure_fp_peaks()
-    r = run_cuda(args, torch, lib, cfg, rank, world)
+    sampler = ClockSampler(torch.cuda.current_device())
+    sampler.start()
+    r = run_cuda(args, torch, lib, cfg, rank, world, sampler)
+    targets = None
+    if rank == 0 and world == 1 and args.config == "merger100k" and not args.no_targets:
+        targets = target_leg(args, torch, lib, flush_buffer(torch), sampler)
+    clocks = sampler.stop()
     f32, f64 = r["runs"]["fp32_mixed"], r["runs"]["fp64"]
     # whole-job aggregation: max time over ranks
     t32, t64, te = f32["secs"], f64["secs"], r["e2e_s"]
@@ -830,25 +890,18 @@ def main():
                      "frac": achieved / fp32_peak,
                      "traffic": WALK32_DRAM_BYTES_PER_BODY * cfg["n"],
                      "issue_slots_busy_ncu": WALK32_ISSUE_BUSY,
-                     "note": "20 flop per reference interaction / walk event time; peak = FP32 "
-                             "FMA throughput measured live by csg_measure_fp_peaks (the walk is "
-                             "CUDA-core bound: no dense contraction, tree resident in L2). What "
-                             "bounds it is instruction issue: the traversal's opening decisions "
-                             "take ~68 warp instructions per warp step against ~9 for the pair "
-                             "term; issue_slots_busy_ncu is from the ncu capture of the 100k "
-                             "merger. traffic = DRAM bytes per launch from that capture scaled "
-                             "by the body count"},
+                     "note": WALK32_NOTE},
         "errors": r["errors"],
         "e2e": {"value": e2e_value, "unit": UNIT, "api": "integrator_step (pinned host Body[])",
                 "steps": r["e2e_steps"], "h2d_bytes_per_step": 168 * cfg["n"],
                 "d2h_bytes_per_step": (104 if cfg["sph"] else 72) * cfg["n"] + 104 * r["e2e_nodes"]},
         "gpu_launches": f32["launches"],
-        "clocks": r["clocks"],
+        "clocks": clocks,
     }
     if rank == 0 and args.thetas:
         line["theta_sweep"] = theta_sweep(args, torch, lib, cfg,
                                           [float(t) for t in args.thetas.split(",")],
-                                          flush_buffer(torch))
+                                          flush_buffer(torch), args.steps)
     if rank == 0 and args.drift > 0:
         line["energy_drift"] = energy_drift(torch, lib, cfg, args.drift, flush_buffer(torch))
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -856,6 +909,16 @@ def main():
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
         line["speedup_vs_cpu"] = {"fp32_mixed": value / cb["value"], "fp64_plain": v64 / cb["value"],
                                   "e2e": e2e_value / cb["value"]}
+        if targets is not None:
+            for th, t in targets["thetas"].items():
+                cbt = cpu_reference(dict(CONFIGS["bulge1m"], theta=float(th)), 10**9,
+                                    time_budget=args.cpu_budget)
+                t["cpu_baseline"] = {k: cbt[k] for k in ("value", "unit", "cores", "kind", "sample")}
+                t["fp64_over_cpu"] = t["fp64_plain"]["body_substeps_per_s"] / cbt["value"]
+                t["fp32_over_cpu"] = t["fp32_mixed"]["body_substeps_per_s"] / cbt["value"]
+                t["target_50x_cpu"] = bool(t["fp64_over_cpu"] >= 50.0)
+    if targets is not None:
+        line["targets_1m"] = targets
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

@@ -56,6 +56,11 @@ void orc_direct_forces(const Body *bodies, int n, const int32_t *idx, int m, dou
 /* Kinetic + softened potential energy, O(n^2). */
 double orc_total_energy(const Body *bodies, int n, double G, double softening);
 
+/* Seeded benchmark initial conditions (orc_ics.c): the kinds of the
+   library's csg_generate_ics, byte for byte, so that CPU-only runs need not
+   load the library. Returns n, or -1 for a bad kind or count. */
+int orc_generate_ics(int kind, int n, uint64_t seed, Body *out);
+
 /* Threads the OpenMP loops use (0 = runtime default). Returns the count in use. */
 int orc_set_threads(int nthreads);
 

@@ -23,12 +23,22 @@ _d = ctypes.c_double
 _i = ctypes.c_int
 
 
+def reference_dir():
+    """The cosmosim checkout named by CSG_REFERENCE_DIR, when it holds the
+    sources; None otherwise (there is no default location)."""
+    ref = os.environ.get("CSG_REFERENCE_DIR")
+    if ref and os.path.isdir(os.path.join(ref, "src")):
+        return ref
+    return None
+
+
 def build(quiet=True):
-    """Compile liborc.so (and the reference library when its sources exist)."""
+    """Compile liborc.so (and the reference library when CSG_REFERENCE_DIR
+    names a cosmosim checkout)."""
     out = subprocess.DEVNULL if quiet else None
     subprocess.run(["make", "-s", "-C", HERE, "liborc.so"], check=True, stdout=out)
-    if os.path.isdir(os.environ.get("CSG_REFERENCE_DIR", "/root/reference") + "/src"):
-        ref = os.environ.get("CSG_REFERENCE_DIR", "/root/reference")
+    ref = reference_dir()
+    if ref:
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref}"], check=True, stdout=out)
 
 
@@ -130,6 +140,16 @@ class Oracle(CpuPhysics):
         lib.orc_set_threads.restype = _i
         lib.orc_quasar_seed.argtypes = [ctypes.c_uint64, _i]
         lib.orc_quasar_seed.restype = None
+        lib.orc_generate_ics.argtypes = [_i, _i, ctypes.c_uint64, _vp]
+        lib.orc_generate_ics.restype = _i
+
+    def generate_ics(self, kind, n, seed):
+        """The library's csg_generate_ics(kind, n, seed) restated on the CPU
+        (byte-identical Body[]), so CPU-only runs need not load the library."""
+        out = np.zeros(n, dtype=BODY_DTYPE)
+        if self.lib.orc_generate_ics(kind, n, seed, ptr(out) if n else None) != n:
+            raise ValueError(f"orc_generate_ics: bad kind {kind} or count {n}")
+        return out
 
     def quasar_seed(self, rng_state=1, knot_phase=0):
         self.lib.orc_quasar_seed(rng_state, knot_phase)

@@ -1,10 +1,11 @@
 """Generates the golden fixtures in tests/golden/ from cosmosim's own code.
 
-Run in a checkout where the reference sources exist (it compiles them with
-`make -C oracle ref`, i.e. cosmosim's src/*.c built where they lie, into
-oracle/_ref/libcosmosim_ref.so) and commit the .npz files it writes:
+Run with CSG_REFERENCE_DIR naming a cosmosim checkout (it compiles its
+sources with `make -C oracle ref REF=$CSG_REFERENCE_DIR`, i.e. cosmosim's
+src/*.c built where they lie, into oracle/_ref/libcosmosim_ref.so) and commit
+the .npz files it writes:
 
-    python tests/golden/make_golden.py
+    CSG_REFERENCE_DIR=<cosmosim checkout> python tests/golden/make_golden.py
 
 Every output below is what the reference library itself returned on the
 stored seeded inputs. Inputs are drawn with numpy's PCG64 from fixed seeds.

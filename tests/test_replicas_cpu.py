@@ -33,7 +33,7 @@ def rank_main(rank, world, port, out):
     times = bench.max_over_ranks(torch, [1.0 + rank, 5.0 - rank, 0.5], "cpu")
     rate = bench.job_rate(1000, w, times[0])
     # each rank's ensemble is its own (rank-dependent seeds)
-    bodies, parts = bench.ensemble_bodies(lib, r)
+    bodies, parts = bench.ensemble_bodies(lib.generate_ics, r)
     out.put((rank, r, w, local, times, rate, float(bodies["x"][:100].sum()), len(bodies)))
     dist.barrier()
     dist.destroy_process_group()
