@@ -113,6 +113,17 @@ int csgd_upload_device_bodies(csgd_t *d, const Body *device_bodies, int n);
 int csgd_quasar_step(csgd_t *d, const QuasarConfig *cfg, int n_alloc, double dt,
                      int *jet_count, int *n_out);
 int csgd_quasar_state(csgd_t *d, unsigned long long rng, int knot_phase);
+/* 1 when a CUDA device is visible (tells allocation failures from a missing GPU). */
+int csgd_has_device(void);
+/* Limit of the walks' bounded producer/consumer waits, in polls (<= 0: the
+   default 2^22). Drops the captured substep. */
+void csgd_set_wait_limit(csgd_t *d, int polls);
+/* Runs the radix sort's look-back wait on a status word that nothing
+   publishes, with the given poll limit: *status receives the error the wait
+   reported (CSG_ERR_DEVICE_WAIT when it gave up, as it must). */
+int csgd_check_device_wait(csgd_t *d, int polls, int *status);
+/* Frees the quasar step's device scratch (state destruction). */
+void csgd_quasar_free(csgd_t *d);
 
 /* Drops bodies whose mass is not > 0, keeping the order of the rest
    (reference src/quasar.c:511-523); *new_n is the new count. Blocks. */

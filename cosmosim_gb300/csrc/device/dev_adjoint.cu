@@ -363,7 +363,7 @@ template <typename T>
 cudaError_t alloc(T **p, size_t count)
 {
     *p = nullptr;
-    return cudaMalloc((void **)p, sizeof(T) * (count ? count : 1));
+    return csgd_malloc((void **)p, sizeof(T) * (count ? count : 1));
 }
 
 } // namespace
@@ -653,7 +653,7 @@ CSG_EXPORT csg_adjoint *csg_adjoint_create(int n, const CsgSimParams *params, in
         if (e == cudaSuccess) e = alloc(&a->xm, ncap);
         if (e == cudaSuccess) e = alloc(&a->sb, (size_t)n);
         if (e == cudaSuccess) e = alloc(&a->counts, (size_t)n);
-        if (e == cudaSuccess) e = cudaMallocHost((void **)&a->h_total, sizeof(int));
+        if (e == cudaSuccess) e = csgd_malloc_host((void **)&a->h_total, sizeof(int));
         rc = cuda_rc(a, e);
     }
     if (!rc) {

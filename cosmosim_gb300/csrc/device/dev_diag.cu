@@ -200,11 +200,11 @@ extern "C" int csgd_direct_forces(csgd_t *d, const int *host_idx, int ns, double
             return CSG_ERR_BAD_ARG;
     int *didx = nullptr;
     double *part = nullptr, *out = nullptr;
-    cudaError_t e = cudaMalloc((void **)&didx, sizeof(int) * (size_t)ns);
+    cudaError_t e = csgd_malloc((void **)&didx, sizeof(int) * (size_t)ns);
     if (e == cudaSuccess)
-        e = cudaMalloc((void **)&part, sizeof(double) * 3 * (size_t)ns * JCHUNKS);
+        e = csgd_malloc((void **)&part, sizeof(double) * 3 * (size_t)ns * JCHUNKS);
     if (e == cudaSuccess)
-        e = cudaMalloc((void **)&out, sizeof(double) * 3 * (size_t)ns);
+        e = csgd_malloc((void **)&out, sizeof(double) * 3 * (size_t)ns);
     int rc = CSG_OK;
     if (e == cudaSuccess) {
         cudaMemcpyAsync(didx, host_idx, sizeof(int) * (size_t)ns, cudaMemcpyHostToDevice, d->stream);
@@ -227,9 +227,9 @@ extern "C" int csgd_energy(csgd_t *d, double G, double softening, double *ke, do
 {
     const int n = d->n;
     double *row = nullptr, *out = nullptr;
-    cudaError_t e = cudaMalloc((void **)&row, sizeof(double) * (size_t)(n > 0 ? n : 1));
+    cudaError_t e = csgd_malloc((void **)&row, sizeof(double) * (size_t)(n > 0 ? n : 1));
     if (e == cudaSuccess)
-        e = cudaMalloc((void **)&out, 2 * sizeof(double));
+        e = csgd_malloc((void **)&out, 2 * sizeof(double));
     int rc = CSG_OK;
     if (e == cudaSuccess && n > 0) {
         { k_potential_rows<<<csgd_grid(n, DT), DT, 0, d->stream>>>(d->x, d->y, d->z, d->m, d->gid, n, G, softening * softening, row); d->launches++; }
@@ -270,8 +270,8 @@ extern "C" CSG_EXPORT int csg_measure_fp_peaks(double *fp32_tflops, double *fp64
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     int rc = CSG_OK;
-    if (cudaMalloc((void **)&o32, nthr * sizeof(float)) != cudaSuccess ||
-        cudaMalloc((void **)&o64, nthr * sizeof(double)) != cudaSuccess) {
+    if (csgd_malloc((void **)&o32, nthr * sizeof(float)) != cudaSuccess ||
+        csgd_malloc((void **)&o64, nthr * sizeof(double)) != cudaSuccess) {
         rc = CSG_ERR_NOMEM;
     } else {
         const int it32 = 8192, it64 = 512;
@@ -552,7 +552,7 @@ extern "C" CSG_EXPORT int csg_check_div_sqrt(int64_t n, uint64_t seed, int64_t *
         return CSG_ERR_NO_DEVICE;
     }
     unsigned long long *out = nullptr;
-    if (cudaMalloc((void **)&out, 2 * sizeof(unsigned long long)) != cudaSuccess) {
+    if (csgd_malloc((void **)&out, 2 * sizeof(unsigned long long)) != cudaSuccess) {
         cudaGetLastError();
         return CSG_ERR_NOMEM;
     }

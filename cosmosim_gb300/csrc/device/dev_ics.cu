@@ -16,7 +16,6 @@
 
 namespace {
 
-constexpr int JUMP_LEVELS = 40; // runs start below 10 * 2^36 draws
 constexpr int RUN = 16;         // bodies per thread
 constexpr double IPI = 3.14159265358979323846;
 
@@ -26,35 +25,6 @@ unsigned long long xs_step(unsigned long long x)
     x ^= x >> 7;
     x ^= x << 17;
     return x;
-}
-
-// columns of M^(2^b): col[b][j] = M^(2^b) e_j
-struct JumpTable {
-    unsigned long long col[JUMP_LEVELS][64];
-};
-
-__host__ __device__ inline unsigned long long apply(const unsigned long long *col,
-                                                    unsigned long long s)
-{
-    unsigned long long r = 0;
-    for (int j = 0; j < 64; j++)
-        if ((s >> j) & 1ull)
-            r ^= col[j];
-    return r;
-}
-
-const JumpTable &host_table()
-{
-    static JumpTable t;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        for (int j = 0; j < 64; j++)
-            t.col[0][j] = xs_step(1ull << j);
-        for (int b = 1; b < JUMP_LEVELS; b++)
-            for (int j = 0; j < 64; j++) // M^(2^b) = M^(2^(b-1)) o M^(2^(b-1))
-                t.col[b][j] = apply(t.col[b - 1], t.col[b - 1][j]);
-    });
-    return t;
 }
 
 struct Gen {
@@ -88,7 +58,7 @@ __device__ double plummer_menc(double m, double a, double r)
 // chunk c -> (system, first body of the run)
 __global__ void k_disks(const csgd_disk_plan *__restrict__ plans, const int *__restrict__ counts,
                         const int *__restrict__ body_off, const int *__restrict__ chunk_off,
-                        int n_sys, const JumpTable *__restrict__ jt, Body *__restrict__ out)
+                        int n_sys, const XsJumpTable *__restrict__ jt, Body *__restrict__ out)
 {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= chunk_off[n_sys])
@@ -115,10 +85,7 @@ __global__ void k_disks(const csgd_disk_plan *__restrict__ plans, const int *__r
         i = first;
     }
     Gen r{p.seed ? p.seed : 1ull};
-    unsigned long long e = 10ull * (unsigned long long)(i - first);
-    for (int lv = 0; e; lv++, e >>= 1)
-        if (e & 1ull)
-            r.s = apply(jt->col[lv], r.s);
+    r.s = xs_jump(jt, r.s, 10ull * (unsigned long long)(i - first));
     for (; i < i0 + RUN && i < n; i++) {
         Body &b = o[i];
         b = Body{};
@@ -157,6 +124,21 @@ __global__ void k_disks(const csgd_disk_plan *__restrict__ plans, const int *__r
 
 } // namespace
 
+// Runs start below 10 * 2^36 draws; the quasar step's offsets are far smaller.
+const XsJumpTable &xs_jump_table_host()
+{
+    static XsJumpTable t;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        for (int j = 0; j < 64; j++)
+            t.col[0][j] = xs_step(1ull << j);
+        for (int b = 1; b < XS_JUMP_LEVELS; b++)
+            for (int j = 0; j < 64; j++) // M^(2^b) = M^(2^(b-1)) o M^(2^(b-1))
+                t.col[b][j] = xs_apply(t.col[b - 1], t.col[b - 1][j]);
+    });
+    return t;
+}
+
 extern "C" int csgd_generate_disks(void *stream, const csgd_disk_plan *plans, const int *counts,
                                    int n_sys, Body *out)
 {
@@ -180,18 +162,18 @@ extern "C" int csgd_generate_disks(void *stream, const csgd_disk_plan *plans, co
     }
     const int chunks = coff[n_sys];
     void *dmem = nullptr;
-    const size_t bytes = sizeof(JumpTable) + sizeof(csgd_disk_plan) * n_sys +
+    const size_t bytes = sizeof(XsJumpTable) + sizeof(csgd_disk_plan) * n_sys +
                          sizeof(int) * (words + n_sys);
-    if (cudaMalloc(&dmem, bytes) != cudaSuccess) {
+    if (csgd_malloc(&dmem, bytes) != cudaSuccess) {
         cudaGetLastError();
         free(h);
         return CSG_ERR_NOMEM;
     }
     char *p = (char *)dmem;
-    JumpTable *djt = (JumpTable *)p;
-    csgd_disk_plan *dplans = (csgd_disk_plan *)(p + sizeof(JumpTable));
-    int *dints = (int *)(p + sizeof(JumpTable) + sizeof(csgd_disk_plan) * n_sys);
-    cudaMemcpyAsync(djt, &host_table(), sizeof(JumpTable), cudaMemcpyHostToDevice, s);
+    XsJumpTable *djt = (XsJumpTable *)p;
+    csgd_disk_plan *dplans = (csgd_disk_plan *)(p + sizeof(XsJumpTable));
+    int *dints = (int *)(p + sizeof(XsJumpTable) + sizeof(csgd_disk_plan) * n_sys);
+    cudaMemcpyAsync(djt, &xs_jump_table_host(), sizeof(XsJumpTable), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(dplans, plans, sizeof(csgd_disk_plan) * n_sys, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(dints, counts, sizeof(int) * n_sys, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(dints + n_sys, h, sizeof(int) * words, cudaMemcpyHostToDevice, s);

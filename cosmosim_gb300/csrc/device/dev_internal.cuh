@@ -103,14 +103,51 @@ struct DevScalars {
 
 // Quasar step state kept on the device between steps (the reference keeps
 // the generator state and the knot phase in file statics, src/quasar.c:11
-// and :224; the live jet count in its QuasarConfig).
+// and :224; the live jet count in its QuasarConfig), and the counters one
+// step passes between its stages.
 struct QuasarState {
     unsigned long long rng;
     int knot_phase;
     int jet_count;
     int n;      // bodies in use (the step appends jets and lobes)
     int n_smbh; // bodies of type SMBH found by the current step
+    double swallowed; // mass accreted this step, summed in accretion order
+    int expired;      // jets whose lifetime ran out this step
+    int n_events;     // accretion events of the current SMBH
+    int spawns;       // jet spawns that happen this step
+    int spawned;      // bodies they add
+    int err;          // CSG_* code; the step changed nothing when set
 };
+
+// ---- xorshift64 jump-ahead ----------------------------------------------------
+// The generator (Marsaglia xorshift, shifts 13/7/17) is linear over GF(2): one
+// step is a 64x64 bit matrix M, so the state k draws ahead is M^k s. The table
+// holds M^(2^b) by columns (col[b][j] = M^(2^b) e_j); a jump applies one
+// column sum per set bit of k.
+constexpr int XS_JUMP_LEVELS = 40;
+struct XsJumpTable {
+    unsigned long long col[XS_JUMP_LEVELS][64];
+};
+const XsJumpTable &xs_jump_table_host(); // built once per process (dev_ics.cu)
+
+__host__ __device__ inline unsigned long long xs_apply(const unsigned long long *col,
+                                                       unsigned long long s)
+{
+    unsigned long long r = 0;
+    for (int j = 0; j < 64; j++)
+        if ((s >> j) & 1ull)
+            r ^= col[j];
+    return r;
+}
+
+__device__ inline unsigned long long xs_jump(const XsJumpTable *t, unsigned long long s,
+                                             unsigned long long k)
+{
+    for (int lv = 0; k; lv++, k >>= 1)
+        if (k & 1ull)
+            s = xs_apply(t->col[lv], s);
+    return s;
+}
 
 struct csgd {
     cudaStream_t stream;
@@ -126,6 +163,7 @@ struct csgd {
     int node_cap; // node capacity (8*cap + 64)
     int stats;
     int host_err; // first error seen on the host side (launch, allocation)
+    int wait_polls; // limit of the bounded device waits (0: the default, 2^22 polls)
     unsigned long long launches; // kernels launched on this state (measurement)
 
     // bodies, caller index order
@@ -188,6 +226,8 @@ struct csgd {
     DevScalars *sc_host; // pinned mirror
     int *h_int;          // pinned scratch for single values read back (4 ints)
     QuasarState *qs;     // device, allocated by the first quasar step
+    void *q_scratch;     // device scratch of the quasar step (dev_quasar.cu)
+    int q_scratch_cap;   // bodies it is sized for
     int geometry_valid;
     // captured substep (cosmosim_substeps_async path)
     cudaGraphExec_t graph;
@@ -203,6 +243,12 @@ struct csgd {
 };
 
 // ---- helpers shared by the .cu files ----
+// Every device and pinned-host allocation of the library goes through these
+// two. Fault injection (csg_inject_alloc_failure) can make them fail: the
+// next `k` allocations succeed, every later one returns
+// cudaErrorMemoryAllocation until the injection is cleared.
+cudaError_t csgd_malloc(void **p, size_t bytes);
+cudaError_t csgd_malloc_host(void **p, size_t bytes);
 int csgd_check(csgd_t *d, cudaError_t e);
 void csgd_drop_graph(csgd_t *d); // destroys the captured substep (after a sync)
 // allocates the cell geometry (geo, s32) and/or the pool staging on first use
@@ -220,6 +266,13 @@ int csg_radix_sort(csgd_t *d, unsigned long long *key, int *val, unsigned long l
 // Exclusive scan of in[0..n) into out[0..n], out[n] = total. count_limit, when
 // non-NULL, is a device int: items at positions >= *count_limit count as 0.
 int csg_scan_exclusive(csgd_t *d, const int *in, int *out, int n, const int *count_limit);
+
+// Polls a bounded device wait makes before it gives up (csgd::wait_polls).
+constexpr int CSG_WAIT_POLLS_DEFAULT = 1 << 22;
+inline int csgd_wait_polls(const csgd_t *d)
+{
+    return d->wait_polls > 0 ? d->wait_polls : CSG_WAIT_POLLS_DEFAULT;
+}
 
 // ---- device error codes written to DevScalars::err ----
 __device__ __forceinline__ void dev_fail(DevScalars *sc, int code) { atomicCAS(&sc->err, 0, code); }

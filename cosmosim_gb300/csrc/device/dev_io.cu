@@ -102,7 +102,7 @@ extern "C" int csgd_snapshot_f32(csgd_t *d, int format, float *out, int out_is_d
     float *dst = out;
     float *tmp = nullptr;
     if (!out_is_device) {
-        if (cudaMalloc((void **)&tmp, sizeof(float) * stride * (size_t)(k > 0 ? k : 1)) !=
+        if (csgd_malloc((void **)&tmp, sizeof(float) * stride * (size_t)(k > 0 ? k : 1)) !=
             cudaSuccess) {
             cudaGetLastError();
             csgd_set_err(d, CSG_ERR_NOMEM);
@@ -141,7 +141,7 @@ extern "C" int csgd_compact(csgd_t *d, int *new_n)
     if (rc)
         return rc;
     void *tmp = nullptr;
-    if (cudaMalloc(&tmp, sizeof(Body) * (size_t)n) != cudaSuccess) {
+    if (csgd_malloc(&tmp, sizeof(Body) * (size_t)n) != cudaSuccess) {
         cudaGetLastError();
         csgd_set_err(d, CSG_ERR_NOMEM);
         return CSG_ERR_NOMEM;

@@ -1,34 +1,56 @@
-// dev_quasar.cu — the quasar/AGN step (reference src/quasar.c:477-509) on
-// the device: accretion onto SMBHs, accretion rate and luminosity, radiation
-// feedback, jet decay into lobes, recycling of distant jets, jet spawning.
+// dev_quasar.cu — the quasar/AGN step (reference src/quasar.c:477-509) on the
+// device, as one cooperative launch over the whole GPU.
 //
-// The reference runs these loops in index order with a sequential random
-// number stream (xorshift64, src/quasar.c:11-35) and state kept across calls
-// (the generator state and the jet knot phase, :11 and :224); bodies spawned
-// in a step are appended. The device version keeps that order:
-//   - wide passes find the bodies a stage touches (candidates within the
-//     accretion radius of an SMBH, expiring jets, distant jets) and compact
-//     them in index order;
-//   - one thread then processes them in that order, exactly as the
-//     reference's loop would (the SMBH's mass, velocity and spin evolve
-//     victim by victim; random numbers are drawn in the same sequence);
-//   - independent per-body updates (feedback kicks, lifetime countdowns) run
-//     on every thread.
-// The serial parts touch the few bodies near SMBHs and the jets; the O(N)
-// scans are parallel. Compiled with -fmad=false and the reference's
-// operation order; sin, cos and log are CUDA's (within 2 ulp of the C
-// library's), so spawned jets agree to ~1e-15, everything else exactly.
+// What the step reproduces (the reference's semantics are the specification):
+// accretion onto each SMBH in index order and, per SMBH, of its victims in
+// index order, the SMBH's mass, velocity and spin evolving victim by victim;
+// accretion rates and luminosities; radiation feedback; jet countdown, with a
+// lobe appended for every expiring heavy jet; lobe countdown; recycling of
+// jets far from the first live SMBH as infalling gas; jet spawning. Random
+// numbers come from one xorshift64 stream (src/quasar.c:11-35) consumed in
+// that order — 3 draws per lobe, 2 per recycled jet, 3 per jet spawn — and
+// the jet knot phase advances once per step (:224).
 //
-// Field layout: positions, velocities, accelerations, mass, type, density,
+// How the GPU does it:
+//  * Each stage is a grid-wide pass; stages are separated by grid barriers of
+//    one cooperative launch, so the step has no host round trip inside.
+//  * Where index order matters, a pass sets one bit per selected body in a
+//    bitmap, and an ordered compaction (per-block bit counts, prefix over
+//    blocks, in-block scan) turns the bits into an ascending list and clears
+//    them.
+//  * Accretion: only candidates inside the swallow radius or the ISCO can be
+//    accreted ("inner"), so only they form a sequential chain: one thread
+//    walks them in index order, updating the SMBH and recording its mass and
+//    velocity after every accretion event. Every other candidate ("outer":
+//    possibly turned into gas and dragged, never accreted) runs in parallel
+//    with the SMBH state that holds at its index, found by binary search in
+//    that event table.
+//  * Appended and recycled bodies: each one knows its slot from a prefix
+//    count and its random numbers from its draw offset; the generator is
+//    jumped ahead to that offset (xs_jump), so all of them are written at
+//    once.
+// Arithmetic keeps the reference's operation order (the file is compiled
+// without fused multiply-add); sin, cos and log are CUDA's, within 2 ulp of
+// the C library's, so spawned and recycled jets agree to ~1e-15 and all other
+// fields exactly.
+//
+// Fields: positions, velocities, accelerations, mass, type, density,
 // pressure, internal energy and smoothing length live in the SoA arrays;
 // spin, accretion rate, luminosity and lifetime in the device Body staging
-// (csgd::aos), which is their authoritative copy while the state is resident.
+// (csgd::aos), their authoritative copy while the state is resident.
+#include <cooperative_groups.h>
+
 #include "dev_internal.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace {
 
 constexpr double QPI = 3.14159265358979323846;
-constexpr int QT = 1024; // threads of the single-block stages
+constexpr int QB = 256;              // threads per block
+constexpr int QMAX_SMBH = 1024;      // SMBHs one step handles
+constexpr int QMAX_SPAWNS = 12;      // spawns per SMBH: up to 8 plus 4 burst knots
+constexpr unsigned FULL = 0xffffffffu;
 
 struct QCfg {
     double acc_r, swallow_r, isco_r, alpha, jet_speed, jet_mass, jet_life, fb, eta, edd_k,
@@ -42,454 +64,606 @@ struct Bodies {
     Body *aos;
 };
 
-__device__ __forceinline__ unsigned long long q_next(QuasarState *q)
-{
-    unsigned long long x = q->rng;
-    x ^= x << 13;
-    x ^= x >> 7;
-    x ^= x << 17;
-    q->rng = x;
-    return x;
-}
+// Device scratch, one allocation sized for `cap` bodies (layout in qscratch_layout).
+struct QScratch {
+    unsigned *bits;  // cap bits, all zero between uses
+    int *list;       // ordered compaction output, cap
+    int *blockcnt;   // per-block counts of a compaction
+    int *smbh;       // SMBH indices as found (unordered)
+    int *ev_idx;     // accretion event table: victim index (row 0: -1 = initial state)
+    double *ev_m, *ev_vx, *ev_vy, *ev_vz; // SMBH mass and velocity after the event
+    int *sp_k, *sp_j, *sp_first, *sp_ring, *sp_norm; // jet spawn plan
+    double *frame;   // per SMBH: jet frame (perp, perp2, helix offset), 9 doubles
+    XsJumpTable *jump;
+};
 
-__device__ __forceinline__ double q_uniform(QuasarState *q)
-{
-    return (double)(q_next(q) >> 11) * (1.0 / 9007199254740992.0);
-}
+struct Hole { // an SMBH while its victims are processed
+    double x, y, z, vx, vy, vz, m, sx, sy, sz;
+};
 
-__device__ __forceinline__ double q_gaussian(QuasarState *q)
-{
-    double u1 = q_uniform(q);
-    double u2 = q_uniform(q);
-    if (u1 < 1e-15)
-        u1 = 1e-15;
-    return sqrt(-2.0 * log(u1)) * cos(2.0 * QPI * u2);
-}
+struct Draws { // the step's random stream from a given offset
+    unsigned long long s;
+    __device__ double uniform()
+    {
+        s ^= s << 13;
+        s ^= s >> 7;
+        s ^= s << 17;
+        return (double)(s >> 11) * (1.0 / 9007199254740992.0);
+    }
+    __device__ double gaussian() // Box-Muller, first output (src/quasar.c:29-35)
+    {
+        double a = uniform();
+        const double b = uniform();
+        if (a < 1e-15)
+            a = 1e-15;
+        return sqrt(-2.0 * log(a)) * cos(2.0 * QPI * b);
+    }
+};
 
-// Ordered compaction of {i < n : pred(i)} into out[] by one block; returns
-// the count (every thread gets it).
-template <typename Pred>
-__device__ int block_compact(int n, Pred pred, int *out)
+// Exclusive prefix sum of v over the block; *total receives the block's sum.
+__device__ int block_exscan(int v, int *total)
 {
-    __shared__ int s_warp[QT / 32];
-    __shared__ int s_base;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int total = 0;
-    for (int base = 0; base < n; base += QT) {
-        const int i = base + threadIdx.x;
-        const bool f = i < n && pred(i);
-        const unsigned bal = __ballot_sync(0xffffffffu, f);
-        if (lane == 0)
-            s_warp[warp] = __popc(bal);
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int acc = 0;
-            for (int w = 0; w < QT / 32; w++) {
-                int c = s_warp[w];
-                s_warp[w] = acc;
-                acc += c;
-            }
-            s_base = acc;
+    __shared__ int s_w[QB / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL, x, o);
+        if (lane >= o)
+            x += y;
+    }
+    if (lane == 31)
+        s_w[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int t = lane < QB / 32 ? s_w[lane] : 0;
+        for (int o = 1; o < QB / 32; o <<= 1) {
+            const int y = __shfl_up_sync(FULL, t, o);
+            if (lane >= o)
+                t += y;
         }
-        __syncthreads();
-        if (f)
-            out[total + s_warp[warp] + __popc(bal & ((1u << lane) - 1u))] = i;
-        total += s_base;
-        __syncthreads();
+        if (lane < QB / 32)
+            s_w[lane] = t;
+    }
+    __syncthreads();
+    const int before = wid ? s_w[wid - 1] : 0;
+    *total = s_w[QB / 32 - 1];
+    __syncthreads(); // s_w is reused by the next call
+    return before + x - v;
+}
+
+// The positions of the bits set in bits[0, nwords), ascending, into out[];
+// the words are cleared. Returns the count (in every block). Holds one grid
+// barrier; out[] may be read after the caller's next barrier.
+__device__ int grid_compact(cg::grid_group &grid, unsigned *bits, int nwords, int *out,
+                            int *blockcnt)
+{
+    const int per = (nwords + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int w0 = min(nwords, (int)blockIdx.x * per), w1 = min(nwords, w0 + per);
+    int mine = 0;
+    for (int w = w0 + threadIdx.x; w < w1; w += QB)
+        mine += __popc(bits[w]);
+    int tot;
+    block_exscan(mine, &tot);
+    if (threadIdx.x == 0)
+        blockcnt[blockIdx.x] = tot;
+    grid.sync();
+    int before = 0, all = 0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += QB) {
+        const int v = blockcnt[b];
+        all += v;
+        if (b < (int)blockIdx.x)
+            before += v;
+    }
+    int base, total;
+    block_exscan(before, &base);
+    block_exscan(all, &total);
+    for (int c0 = w0; c0 < w1; c0 += QB) {
+        const int w = c0 + threadIdx.x;
+        unsigned word = w < w1 ? bits[w] : 0u;
+        int chunk;
+        int at = base + block_exscan(__popc(word), &chunk);
+        while (word) {
+            out[at++] = w * 32 + (__ffs(word) - 1);
+            word &= word - 1u;
+        }
+        if (w < w1)
+            bits[w] = 0u;
+        base += chunk;
     }
     return total;
 }
 
-__device__ void zero_body(const Bodies &b, int i)
+__device__ __forceinline__ void mark(unsigned *bits, int i)
+{
+    atomicOr(&bits[i >> 5], 1u << (i & 31));
+}
+
+// A body stops: no mass, no velocity, no acceleration.
+__device__ __forceinline__ void stop_body(const Bodies &b, int i)
+{
+    b.m[i] = 0.0;
+    b.vx[i] = b.vy[i] = b.vz[i] = 0.0;
+    b.ax[i] = b.ay[i] = b.az[i] = 0.0;
+}
+
+// A fresh body record at slot i: every field zero, then the given type.
+__device__ void fresh_body(const Bodies &b, int i, int type)
 {
     b.x[i] = b.y[i] = b.z[i] = 0.0;
     b.vx[i] = b.vy[i] = b.vz[i] = 0.0;
     b.ax[i] = b.ay[i] = b.az[i] = 0.0;
     b.m[i] = 0.0;
     b.rho[i] = b.P[i] = b.u[i] = b.h[i] = 0.0;
-    b.type[i] = BODY_STAR;
-    Body &a = b.aos[i];
-    a = Body{};
+    b.type[i] = type;
+    b.aos[i] = Body{};
+    b.aos[i].type = (BodyType)type;
 }
 
-// src/quasar.c:63-101 (s: the SMBH, v: the victim)
-__device__ void accrete_body(const Bodies &b, int s, int v)
+// Hole H takes victim v (src/quasar.c:63-101): momentum-conserving merge,
+// spin nudged toward the victim's orbital angular momentum (relative to the
+// merged velocity), victim stopped.
+__device__ void swallow(Hole &H, const Bodies &b, int v)
 {
-    Body &S = b.aos[s];
-    double new_mass = b.m[s] + b.m[v];
-    b.vx[s] = (b.m[s] * b.vx[s] + b.m[v] * b.vx[v]) / new_mass;
-    b.vy[s] = (b.m[s] * b.vy[s] + b.m[v] * b.vy[v]) / new_mass;
-    b.vz[s] = (b.m[s] * b.vz[s] + b.m[v] * b.vz[v]) / new_mass;
-    double rx = b.x[v] - b.x[s];
-    double ry = b.y[v] - b.y[s];
-    double rz = b.z[v] - b.z[s];
-    double rvx = b.vx[v] - b.vx[s];
-    double rvy = b.vy[v] - b.vy[s];
-    double rvz = b.vz[v] - b.vz[s];
-    double lx = ry * rvz - rz * rvy;
-    double ly = rz * rvx - rx * rvz;
-    double lz = rx * rvy - ry * rvx;
-    double l_mag = sqrt(lx * lx + ly * ly + lz * lz);
-    if (l_mag > 1e-15) {
-        double weight = b.m[v] / new_mass * 0.01;
-        S.spin_x += weight * lx / l_mag;
-        S.spin_y += weight * ly / l_mag;
-        S.spin_z += weight * lz / l_mag;
-        double s_mag = sqrt(S.spin_x * S.spin_x + S.spin_y * S.spin_y + S.spin_z * S.spin_z);
-        if (s_mag > 1e-15) {
-            S.spin_x /= s_mag;
-            S.spin_y /= s_mag;
-            S.spin_z /= s_mag;
+    const double mv = b.m[v], mt = H.m + mv;
+    H.vx = (H.m * H.vx + mv * b.vx[v]) / mt;
+    H.vy = (H.m * H.vy + mv * b.vy[v]) / mt;
+    H.vz = (H.m * H.vz + mv * b.vz[v]) / mt;
+    const double px = b.x[v] - H.x, py = b.y[v] - H.y, pz = b.z[v] - H.z;
+    const double qx = b.vx[v] - H.vx, qy = b.vy[v] - H.vy, qz = b.vz[v] - H.vz;
+    const double jx = py * qz - pz * qy, jy = pz * qx - px * qz, jz = px * qy - py * qx;
+    const double j = sqrt(jx * jx + jy * jy + jz * jz);
+    if (j > 1e-15) {
+        const double f = mv / mt * 0.01;
+        H.sx += f * jx / j;
+        H.sy += f * jy / j;
+        H.sz += f * jz / j;
+        const double sn = sqrt(H.sx * H.sx + H.sy * H.sy + H.sz * H.sz);
+        if (sn > 1e-15) {
+            H.sx /= sn;
+            H.sy /= sn;
+            H.sz /= sn;
         }
     }
-    b.m[s] = new_mass;
-    b.m[v] = 0.0;
-    b.vx[v] = b.vy[v] = b.vz[v] = 0.0;
-    b.ax[v] = b.ay[v] = b.az[v] = 0.0;
+    H.m = mt;
+    stop_body(b, v);
 }
 
-// src/quasar.c:103-123
-__device__ void disk_drag(const Bodies &b, int s, int g, double alpha)
+// A candidate at offset (dx, dy, dz), distance r from hole H that is not
+// swallowed outright (src/quasar.c:156-183): it turns into gas when the
+// circularisation radius of its orbit lies outside the ISCO (SPH fields
+// seeded if unset); gas feels the accretion disk's radial drag
+// (src/quasar.c:103-123). Returns whether the body is gas.
+__device__ bool settle(const Bodies &b, const QCfg &c, const Hole &H, int i, double dx, double dy,
+                       double dz, double r)
 {
-    double rx = b.x[g] - b.x[s];
-    double ry = b.y[g] - b.y[s];
-    double rz = b.z[g] - b.z[s];
-    double r = sqrt(rx * rx + ry * ry + rz * rz);
-    if (r < 1e-15)
-        return;
-    double rvx = b.vx[g] - b.vx[s];
-    double rvy = b.vy[g] - b.vy[s];
-    double rvz = b.vz[g] - b.vz[s];
-    double v_dot_r = (rvx * rx + rvy * ry + rvz * rz) / r;
-    double vr_x = v_dot_r * rx / r;
-    double vr_y = v_dot_r * ry / r;
-    double vr_z = v_dot_r * rz / r;
-    b.ax[g] -= alpha * vr_x;
-    b.ay[g] -= alpha * vr_y;
-    b.az[g] -= alpha * vr_z;
-}
-
-// Stage 1-2 (src/quasar.c:125-190 and :482-494): accretion, then accretion
-// rate and luminosity of every SMBH. One block. smbh[]: all bodies of type
-// SMBH in index order (count in q->n_smbh); cand[]: scratch.
-__global__ void __launch_bounds__(QT) k_q_accretion(Bodies b, QCfg c, QuasarState *q, double dt,
-                                                    int *smbh, int *cand)
-{
-    const int n = q->n;
-    const int ns = block_compact(n, [&](int i) { return b.type[i] == BODY_SMBH; }, smbh);
-    __shared__ double s_swallowed;
-    if (threadIdx.x == 0) {
-        q->n_smbh = ns;
-        s_swallowed = 0.0;
+    const double qx = b.vx[i] - H.vx, qy = b.vy[i] - H.vy, qz = b.vz[i] - H.vz;
+    const double jx = dy * qz - dz * qy, jy = dz * qx - dx * qz, jz = dx * qy - dy * qx;
+    const double r_circ = (jx * jx + jy * jy + jz * jz) / (H.m * r);
+    if (r_circ > c.isco_r && b.type[i] != BODY_GAS) {
+        b.type[i] = BODY_GAS;
+        if (b.h[i] < 1e-10)
+            b.h[i] = c.acc_r * 0.3;
+        if (b.u[i] < 1e-10) {
+            const double v2 = b.vx[i] * b.vx[i] + b.vy[i] * b.vy[i] + b.vz[i] * b.vz[i];
+            b.u[i] = 0.001 * v2 + 0.01;
+        }
     }
+    if (b.type[i] != BODY_GAS)
+        return false;
+    const double rx = b.x[i] - H.x, ry = b.y[i] - H.y, rz = b.z[i] - H.z;
+    const double rr = sqrt(rx * rx + ry * ry + rz * rz);
+    if (rr < 1e-15)
+        return true;
+    const double wx = b.vx[i] - H.vx, wy = b.vy[i] - H.vy, wz = b.vz[i] - H.vz;
+    const double radial = (wx * rx + wy * ry + wz * rz) / rr;
+    b.ax[i] -= c.alpha * (radial * rx / rr);
+    b.ay[i] -= c.alpha * (radial * ry / rr);
+    b.az[i] -= c.alpha * (radial * rz / rr);
+    return true;
+}
+
+// Row e of the event table: the largest e with ev_idx[e] < i (row 0 holds
+// index -1, the state before any event).
+__device__ int state_at(const QScratch &w, int n_events, int i)
+{
+    int lo = 0, hi = n_events; // ev_idx[lo] < i <= ev_idx[hi + 1]
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (w.ev_idx[mid] < i)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(QB) k_quasar_step(Bodies b, QCfg c, QuasarState *q,
+                                                    QScratch w, double dt)
+{
+    cg::grid_group grid = cg::this_grid();
+    __shared__ int s_smbh[QMAX_SMBH];
+    const int tid = threadIdx.x;
+    const long long gtid = (long long)blockIdx.x * QB + tid;
+    const long long gsz = (long long)gridDim.x * QB;
+    const bool lead = gtid == 0;
+    const int n0 = q->n, jc0 = q->jet_count, knot0 = q->knot_phase;
+    const unsigned long long rng0 = q->rng;
+    const int nwords = (c.n_alloc + 31) >> 5;
+    grid.sync(); // every thread has read the inputs before they change
+    if (lead) {
+        q->n_smbh = 0;
+        q->swallowed = 0.0;
+        q->expired = 0;
+        q->err = 0;
+    }
+    grid.sync();
+
+    // ---- the SMBHs, sorted by index in every block ----
+    for (long long i = gtid; i < n0; i += gsz)
+        if (b.type[i] == BODY_SMBH) {
+            const int k = atomicAdd(&q->n_smbh, 1);
+            if (k < QMAX_SMBH)
+                w.smbh[k] = (int)i;
+        }
+    grid.sync();
+    const int ns = q->n_smbh;
+    if (ns > QMAX_SMBH) { // uniform over the grid: nothing has changed yet
+        if (lead)
+            q->err = CSG_ERR_UNSUPPORTED;
+        return;
+    }
+    int span = 1;
+    while (span < ns)
+        span <<= 1;
+    for (int k = tid; k < span; k += QB)
+        s_smbh[k] = k < ns ? w.smbh[k] : 0x7fffffff;
     __syncthreads();
-    const double r_acc_sq = c.acc_r * c.acc_r;
-    const double r_swallow_sq = c.swallow_r * c.swallow_r;
-    for (int k = 0; k < ns; k++) {
-        const int s = smbh[k];
-        if (!(b.m[s] > 0.0)) // reference: mass <= 0.0 skips this SMBH
-            continue;
-        const double sx = b.x[s], sy = b.y[s], sz = b.z[s]; // positions do not change here
-        const int nc = block_compact(n, [&](int i) {
-            if (i == s || b.m[i] <= 0.0 || b.type[i] == BODY_SMBH)
-                return false;
-            const double dx = b.x[i] - sx, dy = b.y[i] - sy, dz = b.z[i] - sz;
-            return !(dx * dx + dy * dy + dz * dz > r_acc_sq);
-        }, cand);
-        if (threadIdx.x == 0) {
-            for (int j = 0; j < nc; j++) {
-                const int i = cand[j];
-                double dx = b.x[i] - b.x[s];
-                double dy = b.y[i] - b.y[s];
-                double dz = b.z[i] - b.z[s];
-                double dist_sq = dx * dx + dy * dy + dz * dz;
-                if (dist_sq < r_swallow_sq) {
-                    s_swallowed += b.m[i];
-                    accrete_body(b, s, i);
-                    continue;
-                }
-                double r = sqrt(dist_sq);
-                double rvx = b.vx[i] - b.vx[s];
-                double rvy = b.vy[i] - b.vy[s];
-                double rvz = b.vz[i] - b.vz[s];
-                double lx = dy * rvz - dz * rvy;
-                double ly = dz * rvx - dx * rvz;
-                double lz = dx * rvy - dy * rvx;
-                double l_sq = lx * lx + ly * ly + lz * lz;
-                double r_circ = l_sq / (b.m[s] * r);
-                if (r_circ > c.isco_r && b.type[i] != BODY_GAS) {
-                    b.type[i] = BODY_GAS;
-                    if (b.h[i] < 1e-10)
-                        b.h[i] = c.acc_r * 0.3;
-                    if (b.u[i] < 1e-10) {
-                        double v2 = b.vx[i] * b.vx[i] + b.vy[i] * b.vy[i] + b.vz[i] * b.vz[i];
-                        b.u[i] = 0.001 * v2 + 0.01;
-                    }
-                }
-                if (b.type[i] == BODY_GAS) {
-                    disk_drag(b, s, i, c.alpha);
-                    if (r < c.isco_r) {
-                        s_swallowed += b.m[i];
-                        accrete_body(b, s, i);
+    for (int size = 2; size <= span; size <<= 1) // bitonic sort
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int k = tid; k < span; k += QB) {
+                const int o = k ^ stride;
+                if (o > k) {
+                    const int a = s_smbh[k], v = s_smbh[o];
+                    if ((a > v) == ((k & size) == 0)) {
+                        s_smbh[k] = v;
+                        s_smbh[o] = a;
                     }
                 }
             }
+            __syncthreads();
         }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        const double mdot_instant = s_swallowed / dt;
-        for (int k = 0; k < ns; k++) {
-            Body &S = b.aos[smbh[k]];
-            S.accretion_rate = c.smoothing * S.accretion_rate + (1.0 - c.smoothing) * mdot_instant;
-            double l_edd = c.edd_k * b.m[smbh[k]];
-            S.luminosity = c.eta * S.accretion_rate;
-            if (S.luminosity > l_edd)
-                S.luminosity = l_edd;
-        }
-    }
-}
 
-// Stage 3 (src/quasar.c:192-220): radiation pressure of every luminous SMBH
-// on the bodies within 3 accretion radii, added in SMBH index order.
-__global__ void k_q_feedback(Bodies b, QCfg c, const QuasarState *q, const int *smbh)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int n = q->n, ns = q->n_smbh;
-    if (i >= n || b.m[i] <= 0.0 || b.type[i] == BODY_SMBH)
-        return;
-    const double r_fb_sq = (c.acc_r * 3.0) * (c.acc_r * 3.0);
+    // ---- 1. accretion (src/quasar.c:125-190), SMBH by SMBH ----
+    const double r_acc_sq = c.acc_r * c.acc_r, r_sw_sq = c.swallow_r * c.swallow_r;
     for (int k = 0; k < ns; k++) {
-        const int s = smbh[k];
-        const double lum = b.aos[s].luminosity;
-        if (lum <= 0.0)
-            continue;
-        double dx = b.x[i] - b.x[s];
-        double dy = b.y[i] - b.y[s];
-        double dz = b.z[i] - b.z[s];
-        double dist_sq = dx * dx + dy * dy + dz * dz;
-        if (dist_sq > r_fb_sq || dist_sq < 1e-10)
-            continue;
-        double r = sqrt(dist_sq);
-        double f_mag = c.fb * lum / (4.0 * QPI * dist_sq);
-        b.ax[i] += f_mag * dx / r;
-        b.ay[i] += f_mag * dy / r;
-        b.az[i] += f_mag * dz / r;
+        const int s = s_smbh[k];
+        if (!(b.m[s] > 0.0))
+            continue; // the same decision in every block: SMBH masses only grow here
+        const double hx = b.x[s], hy = b.y[s], hz = b.z[s];
+        // inner candidates -> bitmap
+        for (long long i = gtid; i < n0; i += gsz) {
+            if (i == s || b.m[i] <= 0.0 || b.type[i] == BODY_SMBH)
+                continue;
+            const double dx = b.x[i] - hx, dy = b.y[i] - hy, dz = b.z[i] - hz;
+            const double d2 = dx * dx + dy * dy + dz * dz;
+            if (!(d2 > r_acc_sq) && (d2 < r_sw_sq || sqrt(d2) < c.isco_r))
+                mark(w.bits, (int)i);
+        }
+        grid.sync();
+        const int n_inner = grid_compact(grid, w.bits, nwords, w.list, w.blockcnt);
+        grid.sync();
+        if (lead) { // the chain of possible accretions, in index order
+            Hole H{hx, hy, hz, b.vx[s], b.vy[s], b.vz[s], b.m[s], b.aos[s].spin_x,
+                   b.aos[s].spin_y, b.aos[s].spin_z};
+            double swallowed = q->swallowed;
+            int e = 0;
+            w.ev_idx[0] = -1;
+            w.ev_m[0] = H.m;
+            w.ev_vx[0] = H.vx;
+            w.ev_vy[0] = H.vy;
+            w.ev_vz[0] = H.vz;
+            for (int t = 0; t < n_inner; t++) {
+                const int i = w.list[t];
+                const double dx = b.x[i] - hx, dy = b.y[i] - hy, dz = b.z[i] - hz;
+                const double d2 = dx * dx + dy * dy + dz * dz;
+                bool eaten = d2 < r_sw_sq;
+                if (!eaten) {
+                    const double r = sqrt(d2);
+                    eaten = settle(b, c, H, i, dx, dy, dz, r) && r < c.isco_r;
+                }
+                if (eaten) {
+                    swallowed += b.m[i];
+                    swallow(H, b, i);
+                    e++;
+                    w.ev_idx[e] = i;
+                    w.ev_m[e] = H.m;
+                    w.ev_vx[e] = H.vx;
+                    w.ev_vy[e] = H.vy;
+                    w.ev_vz[e] = H.vz;
+                }
+            }
+            q->n_events = e;
+            q->swallowed = swallowed;
+            b.m[s] = H.m;
+            b.vx[s] = H.vx;
+            b.vy[s] = H.vy;
+            b.vz[s] = H.vz;
+            b.aos[s].spin_x = H.sx;
+            b.aos[s].spin_y = H.sy;
+            b.aos[s].spin_z = H.sz;
+        }
+        grid.sync();
+        // outer candidates, each with the SMBH state at its index
+        const int n_events = q->n_events;
+        for (long long i = gtid; i < n0; i += gsz) {
+            if (i == s || b.m[i] <= 0.0 || b.type[i] == BODY_SMBH)
+                continue;
+            const double dx = b.x[i] - hx, dy = b.y[i] - hy, dz = b.z[i] - hz;
+            const double d2 = dx * dx + dy * dy + dz * dz;
+            if (d2 > r_acc_sq || d2 < r_sw_sq)
+                continue;
+            const double r = sqrt(d2);
+            if (r < c.isco_r)
+                continue; // inner: done by the chain
+            const int e = state_at(w, n_events, (int)i);
+            const Hole H{hx, hy, hz, w.ev_vx[e], w.ev_vy[e], w.ev_vz[e], w.ev_m[e], 0.0, 0.0, 0.0};
+            settle(b, c, H, (int)i, dx, dy, dz, r);
+        }
+        grid.sync();
     }
-}
 
-__device__ void spawn_jets(const Bodies &b, const QCfg &c, QuasarState *q, const int *smbh,
-                           int ns)
-{
-    q->knot_phase++;
-    const int knot_phase = q->knot_phase;
-    double phase_rad = knot_phase * 0.10;
-    double phase_rad2 = knot_phase * 0.057;
-    double speed_mod = 1.0 + 0.6 * sin(phase_rad);
+    // ---- 2. accretion rate and luminosity of every SMBH (src/quasar.c:482-494) ----
+    if (gtid < ns) {
+        const int s = s_smbh[gtid];
+        Body &A = b.aos[s];
+        const double mdot = q->swallowed / dt;
+        A.accretion_rate = c.smoothing * A.accretion_rate + (1.0 - c.smoothing) * mdot;
+        const double l_edd = c.edd_k * b.m[s];
+        A.luminosity = c.eta * A.accretion_rate;
+        if (A.luminosity > l_edd)
+            A.luminosity = l_edd;
+    }
+    grid.sync();
+
+    // ---- 3. feedback (src/quasar.c:192-220), 4. jet countdown (:375-382) ----
+    const double r_fb_sq = (c.acc_r * 3.0) * (c.acc_r * 3.0);
+    for (long long i = gtid; i < n0; i += gsz) {
+        if (b.m[i] <= 0.0 || b.type[i] == BODY_SMBH)
+            continue;
+        for (int k = 0; k < ns; k++) {
+            const int s = s_smbh[k];
+            const double lum = b.aos[s].luminosity;
+            if (lum <= 0.0)
+                continue;
+            const double dx = b.x[i] - b.x[s], dy = b.y[i] - b.y[s], dz = b.z[i] - b.z[s];
+            const double d2 = dx * dx + dy * dy + dz * dz;
+            if (d2 > r_fb_sq || d2 < 1e-10)
+                continue;
+            const double r = sqrt(d2);
+            const double f = c.fb * lum / (4.0 * QPI * d2);
+            b.ax[i] += f * dx / r;
+            b.ay[i] += f * dy / r;
+            b.az[i] += f * dz / r;
+        }
+        if (b.type[i] == BODY_JET) {
+            double &life = b.aos[i].lifetime;
+            life -= dt;
+            if (life <= 0.0) {
+                atomicAdd(&q->expired, 1);
+                if (b.m[i] > 0.2)
+                    mark(w.bits, (int)i); // leaves a lobe, if there is room
+            }
+        }
+    }
+    grid.sync();
+
+    // lobes: the k-th heavy expiring jet (index order) fills slot n0 + k
+    const int heavy = grid_compact(grid, w.bits, nwords, w.list, w.blockcnt);
+    const int lobes = max(0, min(heavy, c.n_alloc - n0));
+    grid.sync();
+    for (long long k = gtid; k < lobes; k += gsz) {
+        const int j = w.list[k], t = n0 + (int)k;
+        Draws g{xs_jump(w.jump, rng0, 3ull * (unsigned long long)k)};
+        const double mj = b.m[j], xj = b.x[j], yj = b.y[j], zj = b.z[j];
+        const double vxj = b.vx[j], vyj = b.vy[j], vzj = b.vz[j];
+        fresh_body(b, t, BODY_LOBE);
+        b.m[t] = mj * 0.5;
+        b.x[t] = xj;
+        b.y[t] = yj;
+        b.z[t] = zj;
+        const double spread = 0.5;
+        b.vx[t] = vxj * 0.15 + (g.uniform() - 0.5) * spread;
+        b.vy[t] = vyj * 0.15 + (g.uniform() - 0.5) * spread;
+        b.vz[t] = vzj * 0.15 + (g.uniform() - 0.5) * spread;
+        b.aos[t].lifetime = c.jet_life * 3.0;
+    }
+    grid.sync();
+    // expired jets stop; lobes (the new ones too) count down (src/quasar.c:404-421)
+    const int n1 = n0 + lobes;
+    for (long long i = gtid; i < n1; i += gsz) {
+        if (b.m[i] <= 0.0)
+            continue;
+        if (b.type[i] == BODY_JET && i < n0 && b.aos[i].lifetime <= 0.0) {
+            stop_body(b, (int)i);
+        } else if (b.type[i] == BODY_LOBE) {
+            double &life = b.aos[i].lifetime;
+            life -= dt;
+            if (life <= 0.0)
+                stop_body(b, (int)i);
+        }
+    }
+    grid.sync();
+
+    // ---- 4b. recycling around the first live SMBH (src/quasar.c:424-475) ----
+    int first = -1;
+    for (int k = 0; k < ns && first < 0; k++)
+        if (b.m[s_smbh[k]] > 0.0)
+            first = s_smbh[k];
+    int recycled = 0;
+    if (first >= 0) {
+        const double rr = c.acc_r * 10.0, rr_sq = rr * rr;
+        const double fx = b.x[first], fy = b.y[first], fz = b.z[first];
+        for (long long i = gtid; i < n1; i += gsz) {
+            if (b.type[i] != BODY_JET || b.m[i] <= 0.0)
+                continue;
+            const double dx = b.x[i] - fx, dy = b.y[i] - fy, dz = b.z[i] - fz;
+            if (!(dx * dx + dy * dy + dz * dz < rr_sq))
+                mark(w.bits, (int)i);
+        }
+        grid.sync();
+        recycled = grid_compact(grid, w.bits, nwords, w.list, w.blockcnt);
+        grid.sync();
+        const double fm = b.m[first], fvx = b.vx[first], fvy = b.vy[first], fvz = b.vz[first];
+        for (long long k = gtid; k < recycled; k += gsz) {
+            const int i = w.list[k];
+            Draws g{xs_jump(w.jump, rng0, 3ull * (unsigned long long)lobes + 2ull * (unsigned long long)k)};
+            const double phi = 2.0 * QPI * g.uniform();
+            const double ct = 2.0 * g.uniform() - 1.0;
+            const double st = sqrt(1.0 - ct * ct);
+            const double rp = c.acc_r;
+            b.x[i] = fx + rp * st * cos(phi);
+            b.y[i] = fy + rp * st * sin(phi);
+            b.z[i] = fz + rp * ct;
+            const double v_in = 0.5 * sqrt(fm / rp);
+            const double nx = (b.x[i] - fx) / rp, ny = (b.y[i] - fy) / rp, nz = (b.z[i] - fz) / rp;
+            b.vx[i] = fvx - v_in * nx;
+            b.vy[i] = fvy - v_in * ny;
+            b.vz[i] = fvz - v_in * nz;
+            b.ax[i] = b.ay[i] = b.az[i] = 0.0;
+            b.type[i] = BODY_GAS;
+            b.aos[i].type = BODY_GAS;
+            b.aos[i].lifetime = 0.0;
+            b.h[i] = c.acc_r * 0.3;
+            const double v2 = b.vx[i] * b.vx[i] + b.vy[i] * b.vy[i] + b.vz[i] * b.vz[i];
+            b.u[i] = 0.001 * v2 + 0.01;
+            b.rho[i] = 0.0;
+            b.P[i] = 0.0;
+        }
+    }
+
+    // ---- 5. jet spawning (src/quasar.c:221-366) ----
+    // The plan: spawns in (SMBH, j) order, each with its ring of bodies; a
+    // spawn happens while there is room (jet cap and body capacity), and
+    // all spawns that happen form a prefix of the plan.
+    const int knot = knot0 + 1;
+    double speed_mod = 1.0 + 0.6 * sin(knot * 0.10);
     if (speed_mod < 0.5)
         speed_mod = 0.5;
-    double cone_angle = 0.05 + 0.13 * (0.5 + 0.5 * sin(phase_rad2));
-    double helix_phase = knot_phase * 0.04;
-    for (int k = 0; k < ns; k++) {
-        const int s = smbh[k];
-        const Body &S = b.aos[s];
-        if (S.luminosity <= 0.0)
-            continue;
-        double jet_energy = 0.5 * c.jet_mass * c.jet_speed * c.jet_speed;
-        if (jet_energy < 1e-15)
-            continue;
-        int n_spawn = (int)(S.luminosity / jet_energy);
-        if (n_spawn < 2)
-            n_spawn = 2;
-        if (n_spawn > 8)
-            n_spawn = 8;
-        double perp_x, perp_y, perp_z;
-        if (fabs(S.spin_z) < 0.9) {
-            perp_x = -S.spin_y;
-            perp_y = S.spin_x;
-            perp_z = 0.0;
-        } else {
-            perp_x = 0.0;
-            perp_y = -S.spin_z;
-            perp_z = S.spin_y;
-        }
-        double pmag = sqrt(perp_x * perp_x + perp_y * perp_y + perp_z * perp_z);
-        if (pmag > 1e-15) {
-            perp_x /= pmag;
-            perp_y /= pmag;
-            perp_z /= pmag;
-        }
-        double perp2_x = S.spin_y * perp_z - S.spin_z * perp_y;
-        double perp2_y = S.spin_z * perp_x - S.spin_x * perp_z;
-        double perp2_z = S.spin_x * perp_y - S.spin_y * perp_x;
-        double pmag2 = sqrt(perp2_x * perp2_x + perp2_y * perp2_y + perp2_z * perp2_z);
-        if (pmag2 > 1e-15) {
-            perp2_x /= pmag2;
-            perp2_y /= pmag2;
-            perp2_z /= pmag2;
-        }
-        double helix_amp = c.swallow_r * 0.35;
-        double hx = helix_amp * (cos(helix_phase) * perp_x + sin(helix_phase) * perp2_x);
-        double hy = helix_amp * (cos(helix_phase) * perp_y + sin(helix_phase) * perp2_y);
-        double hz = helix_amp * (cos(helix_phase) * perp_z + sin(helix_phase) * perp2_z);
-        double actual_speed = c.jet_speed * speed_mod;
-        int burst_extra = (speed_mod > 1.35) ? 4 : 0;
-        int total_spawn = n_spawn + burst_extra;
-        for (int j = 0; j < total_spawn && q->jet_count < c.jet_cap; j++) {
-            if (q->n >= c.n_alloc)
-                break;
-            int is_burst = (j >= n_spawn);
-            double sign = (j % 2 == 0) ? 1.0 : -1.0;
-            double this_cone = is_burst ? 0.012 : cone_angle;
-            double this_speed = is_burst ? actual_speed * 1.28 : actual_speed;
-            double this_mass = is_burst ? c.jet_mass * 1.9 : c.jet_mass;
-            double this_life = is_burst ? c.jet_life * 1.4 : c.jet_life;
-            double axial_fwd = is_burst ? c.swallow_r * 0.6 : 0.0;
-            double angle = q_uniform(q) * 2.0 * QPI;
-            double offset = q_gaussian(q) * this_cone;
-            int ring_n = c.ring_count;
-            if (is_burst)
-                ring_n = 1;
-            for (int r = 0; r < ring_n; r++) {
-                if (q->n >= c.n_alloc || q->jet_count >= c.jet_cap)
-                    break;
-                const int jt = q->n;
-                zero_body(b, jt);
-                b.type[jt] = BODY_JET;
-                b.aos[jt].type = BODY_JET;
-                b.aos[jt].lifetime = this_life;
-                double ring_angle = (ring_n > 1) ? 2.0 * QPI * r / ring_n + angle : angle;
-                double ring_r = (ring_n > 1) ? c.swallow_r * 0.15 : 0.0;
-                double rx = ring_r * (cos(ring_angle) * perp_x + sin(ring_angle) * perp2_x);
-                double ry = ring_r * (cos(ring_angle) * perp_y + sin(ring_angle) * perp2_y);
-                double rz = ring_r * (cos(ring_angle) * perp_z + sin(ring_angle) * perp2_z);
-                b.m[jt] = (ring_n > 1) ? this_mass * 0.6 : this_mass;
-                b.x[jt] = b.x[s] + sign * S.spin_x * (c.swallow_r + axial_fwd) +
-                          offset * (perp_x * cos(angle)) + sign * hx + rx;
-                b.y[jt] = b.y[s] + sign * S.spin_y * (c.swallow_r + axial_fwd) +
-                          offset * (perp_y * cos(angle)) + sign * hy + ry;
-                b.z[jt] = b.z[s] + sign * S.spin_z * (c.swallow_r + axial_fwd) +
-                          offset * (perp_z * sin(angle)) + sign * hz + rz;
-                double expand_v = this_speed * 0.04 * (1.0 + b.aos[jt].lifetime * 0.1);
-                b.vx[jt] = b.vx[s] + sign * S.spin_x * this_speed + rx * expand_v / (ring_r + 1e-15);
-                b.vy[jt] = b.vy[s] + sign * S.spin_y * this_speed + ry * expand_v / (ring_r + 1e-15);
-                b.vz[jt] = b.vz[s] + sign * S.spin_z * this_speed + rz * expand_v / (ring_r + 1e-15);
-                q->n++;
-                q->jet_count++;
+    const double cone = 0.05 + 0.13 * (0.5 + 0.5 * sin(knot * 0.057));
+    const double helix = knot * 0.04;
+    const int jc1 = jc0 - q->expired - recycled;
+    if (blockIdx.x == 0 && tid == 0) {
+        const long long room = min((long long)c.jet_cap - jc1, (long long)c.n_alloc - n1);
+        long long made = 0;
+        int p = 0;
+        const double jet_energy = 0.5 * c.jet_mass * c.jet_speed * c.jet_speed;
+        for (int k = 0; k < ns && made < room; k++) {
+            const int s = s_smbh[k];
+            const Body &A = b.aos[s];
+            if (A.luminosity <= 0.0 || jet_energy < 1e-15)
+                continue;
+            int n_norm = (int)(A.luminosity / jet_energy);
+            n_norm = n_norm < 2 ? 2 : (n_norm > 8 ? 8 : n_norm);
+            // jet frame: perp to the spin axis, perp2 = spin x perp, helical offset
+            double px, py, pz;
+            if (fabs(A.spin_z) < 0.9) {
+                px = -A.spin_y;
+                py = A.spin_x;
+                pz = 0.0;
+            } else {
+                px = 0.0;
+                py = -A.spin_z;
+                pz = A.spin_y;
+            }
+            const double pm = sqrt(px * px + py * py + pz * pz);
+            if (pm > 1e-15) {
+                px /= pm;
+                py /= pm;
+                pz /= pm;
+            }
+            double qx = A.spin_y * pz - A.spin_z * py;
+            double qy = A.spin_z * px - A.spin_x * pz;
+            double qz = A.spin_x * py - A.spin_y * px;
+            const double qm = sqrt(qx * qx + qy * qy + qz * qz);
+            if (qm > 1e-15) {
+                qx /= qm;
+                qy /= qm;
+                qz /= qm;
+            }
+            const double amp = c.swallow_r * 0.35;
+            double *f = w.frame + 9 * k;
+            f[0] = px;
+            f[1] = py;
+            f[2] = pz;
+            f[3] = qx;
+            f[4] = qy;
+            f[5] = qz;
+            f[6] = amp * (cos(helix) * px + sin(helix) * qx);
+            f[7] = amp * (cos(helix) * py + sin(helix) * qy);
+            f[8] = amp * (cos(helix) * pz + sin(helix) * qz);
+            const int spawns = n_norm + ((speed_mod > 1.35) ? 4 : 0);
+            for (int j = 0; j < spawns && made < room; j++, p++) {
+                const int ring = (j >= n_norm) ? 1 : c.ring_count;
+                w.sp_k[p] = k;
+                w.sp_j[p] = j;
+                w.sp_first[p] = (int)made;
+                w.sp_ring[p] = ring;
+                w.sp_norm[p] = n_norm;
+                made += min((long long)max(ring, 0), room - made);
             }
         }
+        q->rng = xs_jump(w.jump, rng0, 3ull * lobes + 2ull * recycled + 3ull * p);
+        q->knot_phase = knot;
+        q->n = n1 + (int)made;
+        q->jet_count = jc1 + (int)made;
+        q->spawns = p;
+        q->spawned = (int)made;
     }
-}
-
-// Stages 4, 4b and 5 (src/quasar.c:375-475 and :301-373): jet decay into
-// lobes, lobe decay, recycling of distant jets, jet spawning. One block.
-__global__ void __launch_bounds__(QT) k_q_jets(Bodies b, QCfg c, QuasarState *q, double dt,
-                                               const int *smbh, int *list)
-{
-    const int n0 = q->n, ns = q->n_smbh;
-    // 4. jets: count down; expiring ones (in index order) spawn lobes
-    for (int i = threadIdx.x; i < n0; i += QT)
-        if (b.type[i] == BODY_JET && b.m[i] > 0.0)
-            b.aos[i].lifetime -= dt;
-    __syncthreads();
-    const int ne = block_compact(n0, [&](int i) {
-        return b.type[i] == BODY_JET && b.m[i] > 0.0 && b.aos[i].lifetime <= 0.0;
-    }, list);
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < ne; k++) {
-            const int i = list[k];
-            if (q->n < c.n_alloc && b.m[i] > 0.2) {
-                const int lb = q->n;
-                zero_body(b, lb);
-                b.type[lb] = BODY_LOBE;
-                b.aos[lb].type = BODY_LOBE;
-                b.m[lb] = b.m[i] * 0.5;
-                b.x[lb] = b.x[i];
-                b.y[lb] = b.y[i];
-                b.z[lb] = b.z[i];
-                double spread = 0.5;
-                b.vx[lb] = b.vx[i] * 0.15 + (q_uniform(q) - 0.5) * spread;
-                b.vy[lb] = b.vy[i] * 0.15 + (q_uniform(q) - 0.5) * spread;
-                b.vz[lb] = b.vz[i] * 0.15 + (q_uniform(q) - 0.5) * spread;
-                b.aos[lb].lifetime = c.jet_life * 3.0;
-                q->n++;
-            }
-            b.m[i] = 0.0;
-            b.vx[i] = b.vy[i] = b.vz[i] = 0.0;
-            b.ax[i] = b.ay[i] = b.az[i] = 0.0;
-            q->jet_count--;
+    grid.sync();
+    const int spawns = q->spawns, made = q->spawned;
+    const unsigned long long base = 3ull * lobes + 2ull * recycled;
+    for (long long t = gtid; t < made; t += gsz) {
+        int lo = 0, hi = spawns - 1; // the last spawn whose first body is <= t
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (w.sp_first[mid] <= t)
+                lo = mid;
+            else
+                hi = mid - 1;
         }
+        const int p = lo, k = w.sp_k[p], j = w.sp_j[p], ring_n = w.sp_ring[p];
+        const int r = (int)t - w.sp_first[p];
+        const int s = s_smbh[k];
+        const Body &A = b.aos[s];
+        const double *f = w.frame + 9 * k;
+        const bool burst = j >= w.sp_norm[p];
+        const double sign = (j % 2 == 0) ? 1.0 : -1.0;
+        const double this_cone = burst ? 0.012 : cone;
+        const double this_speed = burst ? c.jet_speed * speed_mod * 1.28 : c.jet_speed * speed_mod;
+        const double this_mass = burst ? c.jet_mass * 1.9 : c.jet_mass;
+        const double this_life = burst ? c.jet_life * 1.4 : c.jet_life;
+        const double fwd = burst ? c.swallow_r * 0.6 : 0.0;
+        Draws g{xs_jump(w.jump, rng0, base + 3ull * (unsigned long long)p)};
+        const double angle = g.uniform() * 2.0 * QPI;
+        const double offset = g.gaussian() * this_cone;
+        const double ra = (ring_n > 1) ? 2.0 * QPI * r / ring_n + angle : angle;
+        const double rr = (ring_n > 1) ? c.swallow_r * 0.15 : 0.0;
+        const double ox = rr * (cos(ra) * f[0] + sin(ra) * f[3]);
+        const double oy = rr * (cos(ra) * f[1] + sin(ra) * f[4]);
+        const double oz = rr * (cos(ra) * f[2] + sin(ra) * f[5]);
+        const int o = n1 + (int)t;
+        fresh_body(b, o, BODY_JET);
+        b.aos[o].lifetime = this_life;
+        b.m[o] = (ring_n > 1) ? this_mass * 0.6 : this_mass;
+        const double lift = c.swallow_r + fwd;
+        b.x[o] = b.x[s] + sign * A.spin_x * lift + offset * (f[0] * cos(angle)) + sign * f[6] + ox;
+        b.y[o] = b.y[s] + sign * A.spin_y * lift + offset * (f[1] * cos(angle)) + sign * f[7] + oy;
+        b.z[o] = b.z[s] + sign * A.spin_z * lift + offset * (f[2] * sin(angle)) + sign * f[8] + oz;
+        const double widen = this_speed * 0.04 * (1.0 + this_life * 0.1);
+        b.vx[o] = b.vx[s] + sign * A.spin_x * this_speed + ox * widen / (rr + 1e-15);
+        b.vy[o] = b.vy[s] + sign * A.spin_y * this_speed + oy * widen / (rr + 1e-15);
+        b.vz[o] = b.vz[s] + sign * A.spin_z * this_speed + oz * widen / (rr + 1e-15);
     }
-    __syncthreads();
-    const int n1 = q->n;
-    // lobes (those spawned just now too)
-    for (int i = threadIdx.x; i < n1; i += QT) {
-        if (b.type[i] != BODY_LOBE || b.m[i] <= 0.0)
-            continue;
-        b.aos[i].lifetime -= dt;
-        if (b.aos[i].lifetime <= 0.0) {
-            b.m[i] = 0.0;
-            b.vx[i] = b.vy[i] = b.vz[i] = 0.0;
-            b.ax[i] = b.ay[i] = b.az[i] = 0.0;
-        }
-    }
-    __syncthreads();
-    // 4b. jets beyond 10 accretion radii of the first live SMBH come back as gas
-    __shared__ int s_first;
-    if (threadIdx.x == 0) {
-        s_first = -1;
-        for (int k = 0; k < ns; k++)
-            if (b.m[smbh[k]] > 0.0) {
-                s_first = smbh[k];
-                break;
-            }
-    }
-    __syncthreads();
-    const int s = s_first;
-    if (s >= 0) {
-        const double recycle_r = c.acc_r * 10.0;
-        const double recycle_r_sq = recycle_r * recycle_r;
-        const double sx = b.x[s], sy = b.y[s], sz = b.z[s];
-        const int nr = block_compact(n1, [&](int i) {
-            if (b.type[i] != BODY_JET || b.m[i] <= 0.0)
-                return false;
-            const double dx = b.x[i] - sx, dy = b.y[i] - sy, dz = b.z[i] - sz;
-            return !(dx * dx + dy * dy + dz * dz < recycle_r_sq);
-        }, list);
-        if (threadIdx.x == 0) {
-            for (int k = 0; k < nr; k++) {
-                const int i = list[k];
-                double angle = 2.0 * QPI * q_uniform(q);
-                double cos_phi = 2.0 * q_uniform(q) - 1.0;
-                double sin_phi = sqrt(1.0 - cos_phi * cos_phi);
-                double r_place = c.acc_r;
-                b.x[i] = b.x[s] + r_place * sin_phi * cos(angle);
-                b.y[i] = b.y[s] + r_place * sin_phi * sin(angle);
-                b.z[i] = b.z[s] + r_place * cos_phi;
-                double v_inward = 0.5 * sqrt(b.m[s] / r_place);
-                double nx = (b.x[i] - b.x[s]) / r_place;
-                double ny = (b.y[i] - b.y[s]) / r_place;
-                double nz = (b.z[i] - b.z[s]) / r_place;
-                b.vx[i] = b.vx[s] - v_inward * nx;
-                b.vy[i] = b.vy[s] - v_inward * ny;
-                b.vz[i] = b.vz[s] - v_inward * nz;
-                b.ax[i] = b.ay[i] = b.az[i] = 0.0;
-                b.type[i] = BODY_GAS;
-                b.aos[i].type = BODY_GAS;
-                b.aos[i].lifetime = 0.0;
-                b.h[i] = c.acc_r * 0.3;
-                double v2 = b.vx[i] * b.vx[i] + b.vy[i] * b.vy[i] + b.vz[i] * b.vz[i];
-                b.u[i] = 0.001 * v2 + 0.01;
-                b.rho[i] = 0.0;
-                b.P[i] = 0.0;
-                q->jet_count--;
-            }
-        }
-        __syncthreads();
-    }
-    // 5. spawning
-    if (threadIdx.x == 0)
-        spawn_jets(b, c, q, smbh, ns);
 }
 
 QCfg qcfg(const QuasarConfig *cfg, int n_alloc)
@@ -513,13 +687,90 @@ QCfg qcfg(const QuasarConfig *cfg, int n_alloc)
     return c;
 }
 
+size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+// Lays out the scratch for cap bodies and grid blocks; returns its size.
+size_t qscratch_layout(char *base, int cap, int blocks, QScratch *w)
+{
+    const size_t words = ((size_t)cap + 31) / 32 + 1;
+    const size_t plan = (size_t)QMAX_SMBH * QMAX_SPAWNS;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char *p = base ? base + off : nullptr;
+        off += align256(bytes);
+        return p;
+    };
+    w->jump = (XsJumpTable *)take(sizeof(XsJumpTable));
+    w->bits = (unsigned *)take(words * sizeof(unsigned));
+    w->list = (int *)take((size_t)cap * sizeof(int));
+    w->blockcnt = (int *)take((size_t)blocks * sizeof(int));
+    w->smbh = (int *)take(QMAX_SMBH * sizeof(int));
+    w->ev_idx = (int *)take(((size_t)cap + 1) * sizeof(int));
+    w->ev_m = (double *)take(((size_t)cap + 1) * sizeof(double));
+    w->ev_vx = (double *)take(((size_t)cap + 1) * sizeof(double));
+    w->ev_vy = (double *)take(((size_t)cap + 1) * sizeof(double));
+    w->ev_vz = (double *)take(((size_t)cap + 1) * sizeof(double));
+    w->sp_k = (int *)take(plan * sizeof(int));
+    w->sp_j = (int *)take(plan * sizeof(int));
+    w->sp_first = (int *)take(plan * sizeof(int));
+    w->sp_ring = (int *)take(plan * sizeof(int));
+    w->sp_norm = (int *)take(plan * sizeof(int));
+    w->frame = (double *)take((size_t)QMAX_SMBH * 9 * sizeof(double));
+    return off;
+}
+
+// Grid of the cooperative launch: every block resident at once.
+int quasar_blocks(csgd_t *d)
+{
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_quasar_step, QB, 0) != cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    return (d->num_sms > 0 ? d->num_sms : 1) * min(per_sm, 4);
+}
+
+int ensure_scratch(csgd_t *d, int cap, QScratch *w)
+{
+    const int blocks = quasar_blocks(d);
+    if (d->q_scratch && d->q_scratch_cap >= cap) {
+        qscratch_layout((char *)d->q_scratch, d->q_scratch_cap, blocks, w);
+        return CSG_OK;
+    }
+    cudaStreamSynchronize(d->stream);
+    if (d->q_scratch)
+        cudaFree(d->q_scratch);
+    d->q_scratch = nullptr;
+    d->q_scratch_cap = 0;
+    const size_t bytes = qscratch_layout(nullptr, cap, blocks, w);
+    if (csgd_malloc(&d->q_scratch, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        d->q_scratch = nullptr;
+        return CSG_ERR_NOMEM;
+    }
+    qscratch_layout((char *)d->q_scratch, cap, blocks, w);
+    cudaMemsetAsync(w->bits, 0, (((size_t)cap + 31) / 32 + 1) * sizeof(unsigned), d->stream);
+    cudaMemcpyAsync(w->jump, &xs_jump_table_host(), sizeof(XsJumpTable), cudaMemcpyHostToDevice,
+                    d->stream);
+    d->q_scratch_cap = cap;
+    return csgd_check(d, cudaGetLastError());
+}
+
 } // namespace
+
+extern "C" void csgd_quasar_free(csgd_t *d)
+{
+    if (d->q_scratch)
+        cudaFree(d->q_scratch);
+    d->q_scratch = nullptr;
+    d->q_scratch_cap = 0;
+}
 
 extern "C" int csgd_quasar_state(csgd_t *d, unsigned long long rng, int knot_phase)
 {
-    if (!d->qs && cudaMalloc((void **)&d->qs, sizeof(QuasarState)) != cudaSuccess) {
+    if (!d->qs && csgd_malloc((void **)&d->qs, sizeof(QuasarState)) != cudaSuccess) {
         cudaGetLastError();
-        csgd_set_err(d, CSG_ERR_NOMEM);
         return CSG_ERR_NOMEM;
     }
     QuasarState h{};
@@ -537,12 +788,15 @@ extern "C" int csgd_quasar_step(csgd_t *d, const QuasarConfig *cfg, int n_alloc,
         if (rc)
             return rc;
     }
-    if (n_alloc > d->cap || d->n_gal > 1) {
-        csgd_set_err(d, d->n_gal > 1 ? CSG_ERR_UNSUPPORTED : CSG_ERR_BAD_ARG);
+    // errors are returned at once and leave nothing for a later sync to report
+    if (n_alloc > d->cap || n_alloc < d->n || d->n_gal > 1)
         return d->n_gal > 1 ? CSG_ERR_UNSUPPORTED : CSG_ERR_BAD_ARG;
-    }
+    QScratch w;
+    int rc = ensure_scratch(d, d->cap, &w);
+    if (rc)
+        return rc;
     cudaStream_t s = d->stream;
-    // body count and jet count in, the step may append bodies
+    // body count and jet count in; the step may append bodies
     int *hi = d->h_int;
     hi[0] = d->n;
     hi[1] = *jet_count;
@@ -551,18 +805,25 @@ extern "C" int csgd_quasar_step(csgd_t *d, const QuasarConfig *cfg, int n_alloc,
     Bodies b{d->x, d->y, d->z, d->vx, d->vy, d->vz, d->ax, d->ay, d->az, d->m,
              d->rho, d->P, d->u, d->h, d->type, d->aos};
     QCfg c = qcfg(cfg, n_alloc);
-    int *smbh = d->cnt, *list = d->base; // tree scratch: free between builds
-    { k_q_accretion<<<1, QT, 0, s>>>(b, c, d->qs, dt, smbh, list); d->launches++; }
-    { k_q_feedback<<<csgd_grid(n_alloc > 0 ? n_alloc : 1, 256), 256, 0, s>>>(b, c, d->qs, smbh); d->launches++; }
-    { k_q_jets<<<1, QT, 0, s>>>(b, c, d->qs, dt, smbh, list); d->launches++; }
-    cudaMemcpyAsync(&hi[2], &d->qs->n, sizeof(int), cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(&hi[3], &d->qs->jet_count, sizeof(int), cudaMemcpyDeviceToHost, s);
-    int rc = csgd_sync(d);
+    QuasarState *q = d->qs;
+    void *args[] = {&b, &c, &q, &w, &dt};
+    const int blocks = quasar_blocks(d);
+    rc = csgd_check(d, cudaLaunchCooperativeKernel((const void *)k_quasar_step, dim3(blocks),
+                                                   dim3(QB), args, 0, s));
+    d->launches++;
     if (rc)
         return rc;
-    d->n = hi[2];
-    *jet_count = hi[3];
-    *n_out = hi[2];
+    cudaMemcpyAsync(&hi[0], &d->qs->n, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&hi[1], &d->qs->jet_count, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&hi[2], &d->qs->err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    rc = csgd_sync(d);
+    if (rc)
+        return rc;
+    if (hi[2])
+        return hi[2];
+    d->n = hi[0];
+    *jet_count = hi[1];
+    *n_out = hi[0];
     d->geometry_valid = 0;
     d->gas_valid = 0;
     return CSG_OK;

@@ -169,7 +169,6 @@ __global__ void k_scan_total(int *__restrict__ out, int n, const int *__restrict
 constexpr unsigned long long LB_AGG = 1ull << 62; // tile count published
 constexpr unsigned long long LB_PRE = 1ull << 63; // inclusive prefix published
 constexpr unsigned long long LB_VAL = LB_AGG - 1;
-constexpr int LB_SPIN_LIMIT = 1 << 22; // polls of one status word before giving up
 
 // layout of the sort scratch (32-bit words): digit counts [8][256], tile
 // counters [8], padding to an 8-byte boundary, then two status buffers of
@@ -187,6 +186,22 @@ __device__ __forceinline__ unsigned long long lb_load(const unsigned long long *
 {
     unsigned long long v;
     asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Waits (at most `limit` polls) until the status word q carries a published
+// count or prefix; returns it, or 0 after giving up (CSG_ERR_DEVICE_WAIT
+// recorded). The look-back's only wait.
+__device__ unsigned long long lb_wait(const unsigned long long *q, int limit, DevScalars *sc)
+{
+    unsigned long long v = lb_load(q);
+    int spins = 0;
+    while (!(v & (LB_AGG | LB_PRE)) && ++spins < limit)
+        v = lb_load(q);
+    if (!(v & (LB_AGG | LB_PRE))) {
+        dev_fail(sc, CSG_ERR_DEVICE_WAIT);
+        return 0ull;
+    }
     return v;
 }
 
@@ -234,7 +249,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_onesweep(
     unsigned long long *__restrict__ key_out, int *__restrict__ val_out, int n, int shift,
     const unsigned int *__restrict__ counts, int *__restrict__ tile_ctr,
     unsigned long long *status, unsigned long long *__restrict__ status_next, int nblocks,
-    const int *__restrict__ n_dev, DevScalars *sc)
+    const int *__restrict__ n_dev, DevScalars *sc, int wait_polls)
 {
     if (n_dev) { // key count known on the device only: the grid covers the bound
         n = max(0, min(n, *n_dev));
@@ -285,15 +300,9 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_onesweep(
     long long excl = 0;
     if (tile > 0) {
         for (int j = tile - 1; j >= 0; j--) {
-            const unsigned long long *q = status + (size_t)j * RADIX + dg;
-            unsigned long long v = lb_load(q);
-            int spins = 0;
-            while (!(v & (LB_AGG | LB_PRE)) && ++spins < LB_SPIN_LIMIT)
-                v = lb_load(q);
-            if (!(v & (LB_AGG | LB_PRE))) { // gave up: record it, leave the wait
-                dev_fail(sc, CSG_ERR_DEVICE_WAIT);
+            const unsigned long long v = lb_wait(status + (size_t)j * RADIX + dg, wait_polls, sc);
+            if (!v) // gave up (recorded): leave the wait
                 break;
-            }
             excl += (long long)(v & LB_VAL);
             if (v & LB_PRE)
                 break;
@@ -333,7 +342,37 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_onesweep(
     }
 }
 
+// A look-back wait on a status word that nothing publishes: it must give up
+// after `limit` polls and record CSG_ERR_DEVICE_WAIT (the failure path of
+// the sort's only wait, without a sort around it).
+__global__ void k_wait_probe(const unsigned long long *word, int limit, DevScalars *sc)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0)
+        lb_wait(word, limit, sc);
+}
+
 } // namespace
+
+// The real sort keeps the default limit: there a wait only ever waits on a
+// tile whose block is already running, and a tile that gave up would leave
+// holes in the permutation later kernels index with.
+extern "C" int csgd_check_device_wait(csgd_t *d, int polls, int *status)
+{
+    if (polls < 1 || !status)
+        return CSG_ERR_BAD_ARG;
+    unsigned long long *word = nullptr;
+    if (csgd_malloc((void **)&word, sizeof(unsigned long long)) != cudaSuccess) {
+        cudaGetLastError();
+        return CSG_ERR_NOMEM;
+    }
+    cudaMemsetAsync(word, 0, sizeof(unsigned long long), d->stream);
+    { k_wait_probe<<<1, 32, 0, d->stream>>>(word, polls, d->sc); d->launches++; }
+    int rc = csgd_check(d, cudaGetLastError());
+    const int got = rc ? rc : csgd_sync(d); // collects (and clears) the device error
+    cudaFree(word);
+    *status = got;
+    return rc;
+}
 
 int csg_scan_exclusive(csgd_t *d, const int *in, int *out, int n, const int *count_limit)
 {
@@ -411,9 +450,9 @@ int csg_radix_sort(csgd_t *d, unsigned long long *key, int *val, unsigned long l
         unsigned long long *st = status + (size_t)(p & 1) * status_words;
         unsigned long long *st_next = status + (size_t)((p + 1) & 1) * status_words;
         if (small)
-            { k_radix_onesweep<4><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, n_dev, d->sc); d->launches++; }
+            { k_radix_onesweep<4><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, n_dev, d->sc, CSG_WAIT_POLLS_DEFAULT); d->launches++; }
         else
-            { k_radix_onesweep<16><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, n_dev, d->sc); d->launches++; }
+            { k_radix_onesweep<16><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, n_dev, d->sc, CSG_WAIT_POLLS_DEFAULT); d->launches++; }
         unsigned long long *tk = ki;
         ki = ko;
         ko = tk;

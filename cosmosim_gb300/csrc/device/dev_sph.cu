@@ -591,12 +591,12 @@ static int ensure_lists(csgd_t *d)
     d->nb_count = d->sph_relist = nullptr;
     d->pr2 = d->cs = d->sph_term = nullptr;
     size_t c = (size_t)(d->cap > 0 ? d->cap : 1);
-    if (cudaMalloc((void **)&d->nb, sizeof(int) * CSG_SPH_MAX_NEIGHBORS * c) != cudaSuccess ||
-        cudaMalloc((void **)&d->nb_count, sizeof(int) * c) != cudaSuccess ||
-        cudaMalloc((void **)&d->sph_relist, sizeof(int) * c) != cudaSuccess ||
-        cudaMalloc((void **)&d->pr2, sizeof(double) * c) != cudaSuccess ||
-        cudaMalloc((void **)&d->cs, sizeof(double) * c) != cudaSuccess ||
-        cudaMalloc((void **)&d->sph_term, sizeof(double) * 3 * CSG_SPH_MAX_NEIGHBORS * c) !=
+    if (csgd_malloc((void **)&d->nb, sizeof(int) * CSG_SPH_MAX_NEIGHBORS * c) != cudaSuccess ||
+        csgd_malloc((void **)&d->nb_count, sizeof(int) * c) != cudaSuccess ||
+        csgd_malloc((void **)&d->sph_relist, sizeof(int) * c) != cudaSuccess ||
+        csgd_malloc((void **)&d->pr2, sizeof(double) * c) != cudaSuccess ||
+        csgd_malloc((void **)&d->cs, sizeof(double) * c) != cudaSuccess ||
+        csgd_malloc((void **)&d->sph_term, sizeof(double) * 3 * CSG_SPH_MAX_NEIGHBORS * c) !=
             cudaSuccess) {
         cudaGetLastError();
         csgd_set_err(d, CSG_ERR_NOMEM);

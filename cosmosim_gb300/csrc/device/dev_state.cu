@@ -5,6 +5,8 @@
 // src/sph.c:200-231), so given equal accelerations they agree bit for bit.
 #include "dev_internal.cuh"
 
+#include <atomic>
+
 #include <stdlib.h>
 #include <string.h>
 
@@ -136,8 +138,68 @@ cudaError_t dalloc(T **p, size_t count)
     *p = nullptr;
     if (count == 0)
         count = 1;
-    return cudaMalloc((void **)p, sizeof(T) * count);
+    return csgd_malloc((void **)p, sizeof(T) * count);
 }
+
+} // namespace
+
+// Allocations still allowed before injected failures begin; < 0: no injection.
+static std::atomic<long long> g_alloc_allowance{-1};
+
+static bool alloc_injected_failure()
+{
+    long long a = g_alloc_allowance.load();
+    while (a >= 0) {
+        if (a == 0)
+            return true;
+        if (g_alloc_allowance.compare_exchange_weak(a, a - 1))
+            return false;
+    }
+    return false;
+}
+
+cudaError_t csgd_malloc(void **p, size_t bytes)
+{
+    *p = nullptr;
+    if (alloc_injected_failure())
+        return cudaErrorMemoryAllocation;
+    return cudaMalloc(p, bytes);
+}
+
+cudaError_t csgd_malloc_host(void **p, size_t bytes)
+{
+    *p = nullptr;
+    if (alloc_injected_failure())
+        return cudaErrorMemoryAllocation;
+    return cudaMallocHost(p, bytes);
+}
+
+extern "C" int csgd_has_device(void)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n > 0;
+}
+
+extern "C" void csgd_set_wait_limit(csgd_t *d, int polls)
+{
+    cudaStreamSynchronize(d->stream);
+    csgd_drop_graph(d); // captured walks carry the limit in their arguments
+    d->wait_polls = polls > 0 ? polls : 0;
+}
+
+// Fault injection for tests: the next `allow` device or pinned allocations
+// of the library succeed, every later one fails (as an out-of-memory GPU
+// would) until csg_inject_alloc_failure(-1) clears it.
+extern "C" CSG_EXPORT void csg_inject_alloc_failure(long long allow)
+{
+    g_alloc_allowance.store(allow < 0 ? -1 : allow);
+}
+
+namespace {
 
 void free_bodies(csgd_t *d)
 {
@@ -279,21 +341,12 @@ extern "C" csgd_t *csgd_create(void)
     else
         d->num_sms = 152;
     d->gal_cap = 1;
-    if (cudaMalloc((void **)&d->roots, sizeof(DevRoot)) != cudaSuccess) {
-        cudaStreamDestroy(d->own_stream);
-        free(d);
-        return nullptr;
-    }
-    if (cudaMalloc((void **)&d->sc, sizeof(DevScalars)) != cudaSuccess ||
-        cudaMallocHost((void **)&d->sc_host, sizeof(DevScalars)) != cudaSuccess ||
-        cudaMallocHost((void **)&d->h_int, 4 * sizeof(int)) != cudaSuccess) {
-        if (d->sc)
-            cudaFree(d->sc);
-        if (d->sc_host)
-            cudaFreeHost(d->sc_host);
-        cudaFree(d->roots);
-        cudaStreamDestroy(d->own_stream);
-        free(d);
+    if (csgd_malloc((void **)&d->roots, sizeof(DevRoot)) != cudaSuccess ||
+        csgd_malloc((void **)&d->sc, sizeof(DevScalars)) != cudaSuccess ||
+        csgd_malloc_host((void **)&d->sc_host, sizeof(DevScalars)) != cudaSuccess ||
+        csgd_malloc_host((void **)&d->h_int, 4 * sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        csgd_destroy(d); // frees what was made, streams and events included
         return nullptr;
     }
     memset(d->sc_host, 0, sizeof(DevScalars));
@@ -331,6 +384,7 @@ extern "C" void csgd_destroy(csgd_t *d)
         cudaFreeHost(d->h_int);
     if (d->qs)
         cudaFree(d->qs);
+    csgd_quasar_free(d);
     if (d->aux) {
         cudaStreamSynchronize(d->aux);
         cudaStreamDestroy(d->aux);
@@ -397,6 +451,7 @@ extern "C" int csgd_reserve(csgd_t *d, int n)
     cudaStreamSynchronize(d->stream);
     csgd_drop_graph(d); // captured pointers are about to change
     free_bodies(d);
+    d->cap = d->node_cap = d->task_cap = 0; // nothing is held until every buffer is
     const size_t cap = (size_t)(n > 0 ? n : 1);
     const size_t ncap = 8 * cap + 64; // the reference's pool contract
     bool ok = true;
@@ -682,7 +737,15 @@ extern "C" int csgd_sph_cooling(csgd_t *d, double dt)
 // captured substep the fork and join become graph edges.
 extern "C" int csgd_substep(csgd_t *d, double dt, const csgd_force_params *p, int sph)
 {
-    int rc = csgd_kick_drift(d, dt);
+    // what a substep allocates on first use, before its first kernel: an
+    // allocation failure then leaves the bodies as they were (no-ops inside a
+    // capture, which allocates them beforehand)
+    int rc = sph ? csgd_prepare_sph(d) : CSG_OK;
+    if (!rc && d->export_dst)
+        rc = csgd_ensure_tree_extras(d, 1, 1);
+    if (rc)
+        return rc;
+    rc = csgd_kick_drift(d, dt);
     if (!rc)
         rc = csgd_build_tree(d, sph);
     // the pool export reads the finished tree only: it runs beside the walk
@@ -893,8 +956,11 @@ extern "C" int csgd_substeps(csgd_t *d, int k, double dt, const csgd_force_param
 {
     if (k <= 0)
         return CSG_OK;
-    if (d->use_graphs && d->n > 0 && d->stream != nullptr) {
-        if (!graph_matches(d, dt, p, sph) && capture_substep(d, dt, p, sph) != CSG_OK)
+    if (d->use_graphs && d->n > 0 && d->stream != nullptr && !graph_matches(d, dt, p, sph)) {
+        const int crc = capture_substep(d, dt, p, sph);
+        if (crc == CSG_ERR_NOMEM) // nothing ran; a later call captures again
+            return crc;
+        if (crc != CSG_OK)
             d->use_graphs = 0; // run without graphs from now on
     }
     if (d->use_graphs && d->graph) {

@@ -198,15 +198,21 @@ __device__ __forceinline__ void bbox_flush(DevRoot *roots, int g, unsigned long 
 
 __global__ void k_bbox(const double *__restrict__ x, const double *__restrict__ y,
                        const double *__restrict__ z, const double *__restrict__ m,
-                       const int *__restrict__ gid, int n, DevRoot *roots)
+                       const int *__restrict__ gid, int n, DevRoot *roots, DevScalars *gsc)
 {
     unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
     int cnt = 0;
     int cur_g = -1; // warp-uniform: the system the running box belongs to
+    bool bad = false; // a non-finite mass, or a non-finite position of a live body
     for (long long base = (long long)blockIdx.x * blockDim.x; base < n;
          base += (long long)gridDim.x * blockDim.x) {
         const long long i = base + threadIdx.x;
         const int g = (i < n) ? gid[i] : -1;
+        if (g >= 0) {
+            const double mi = m[i];
+            bad |= !isfinite(mi) ||
+                   (is_alive(mi) && !(isfinite(x[i]) && isfinite(y[i]) && isfinite(z[i])));
+        }
         const int g0 = __shfl_sync(0xffffffffu, g, 0);
         if (!__all_sync(0xffffffffu, g == g0 || g < 0)) { // straddles systems
             if (g >= 0 && is_alive(m[i])) {
@@ -241,6 +247,8 @@ __global__ void k_bbox(const double *__restrict__ x, const double *__restrict__ 
     }
     if (cur_g >= 0)
         bbox_flush(roots, cur_g, lo, hi, cnt);
+    if (bad)
+        dev_fail(gsc, CSG_ERR_BAD_ARG);
 }
 
 // Root cube, reference src/octree.c:141-159, plus the fast-key parameters.
@@ -293,8 +301,15 @@ __device__ void root_cube(DevRoot *sc)
 // the sorted order (systems sort in id order) and the total alive count.
 __global__ void k_root(DevScalars *sc, DevRoot *roots, int n_gal)
 {
-    for (int g = threadIdx.x; g < n_gal; g += blockDim.x)
+    // After an error (non-finite input found by k_bbox, or an earlier failure
+    // not yet collected) the tree is built empty: no key is formed from the
+    // bodies and nothing downstream walks them.
+    const bool failed = sc->err != 0;
+    for (int g = threadIdx.x; g < n_gal; g += blockDim.x) {
+        if (failed)
+            roots[g].n_alive = 0;
         root_cube(&roots[g]);
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
         int off = 0;
@@ -336,7 +351,7 @@ __global__ void k_keys(const double *__restrict__ x, const double *__restrict__ 
     if (i >= n)
         return;
     perm[i] = i;
-    if (!is_alive(m[i])) {
+    if (!is_alive(m[i]) || gsc->err != 0) { // see k_root: after an error no body is keyed
         key[i] = CSG_DEAD_KEY;
         return;
     }
@@ -1137,7 +1152,7 @@ static int order_bodies(csgd_t *d)
     // few blocks: each warp flushes its running box with atomics on the same
     // words, so fewer warps contend less (4 blocks per SM keep HBM busy)
     int gb = min(csgd_grid(n, B), 4 * d->num_sms);
-    { k_bbox<<<gb > 0 ? gb : 1, B, 0, s>>>(d->x, d->y, d->z, d->m, d->gid, n, d->roots); d->launches++; }
+    { k_bbox<<<gb > 0 ? gb : 1, B, 0, s>>>(d->x, d->y, d->z, d->m, d->gid, n, d->roots, sc); d->launches++; }
     { k_root<<<1, 256, 0, s>>>(sc, d->roots, G); d->launches++; }
     if (n > 0)
         { k_keys<<<csgd_grid(n, B), B, 0, s>>>(d->x, d->y, d->z, d->m, d->gid, n, sc, d->roots, d->key, d->perm); d->launches++; }

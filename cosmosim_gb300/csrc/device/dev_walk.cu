@@ -47,6 +47,7 @@ struct WalkArgs {
     float acc_k, opn_k;
     int node_cap;
     int group; // 0: one warp per task; g > 0: take g tasks at a time from a counter
+    int wait_polls; // producer/consumer waits give up after this many polls
 };
 
 // Work distribution shared by the walks. A task is up to 32 consecutive
@@ -637,12 +638,12 @@ __global__ void __launch_bounds__(WARPS * CSG_WARP, w64q_min_blocks(WARPS, PERSI
 // the queued walk's bit for bit. The traversal (FP32/ALU pipes) and the
 // evaluation (FP64 pipe) then overlap on every SM instead of alternating in
 // one warp. The warps hand over through per-lane head and tail counters in
-// shared memory; every wait polls with a sleep and gives up after WS_POLLS
-// polls (recording CSG_ERR_DEVICE_WAIT, then both warps leave the task).
+// shared memory; every wait polls with a sleep and gives up after
+// a.wait_polls polls (recording CSG_ERR_DEVICE_WAIT, then both warps leave
+// the task).
 constexpr int WS_RING = 128;   // ring slots per lane (power of two)
 constexpr int WS_BATCH = 8;    // dense batch the consumer waits for
 constexpr int WS_PUBLISH = 4;  // the producer publishes its tails every few steps
-constexpr int WS_POLLS = 1 << 22;
 
 struct WsShared {
     int ring[WS_RING * CSG_WARP]; // slot-major: ring[slot * 32 + lane]
@@ -674,7 +675,7 @@ __device__ __forceinline__ void ws_produce(const WalkArgs &a, NodeW32 *win, WsSh
             bool full = take && tail - head_seen >= WS_RING;
             if (__any_sync(0xffffffffu, full)) {
                 publish();
-                for (int k = 0; k < WS_POLLS; k++) {
+                for (int k = 0; k < a.wait_polls; k++) {
                     head_seen = ws_load(&sh.head[lane]);
                     full = take && tail - head_seen >= WS_RING;
                     if (!__any_sync(0xffffffffu, full) || ws_load(&sh.broken))
@@ -747,7 +748,7 @@ __device__ __forceinline__ void ws_consume(const WalkArgs &a, WsShared &sh, cons
         }
         if (ws_load(&sh.broken))
             return;
-        if (++polls >= WS_POLLS) {
+        if (++polls >= a.wait_polls) {
             if (lane == 0) {
                 dev_fail(a.sc, CSG_ERR_DEVICE_WAIT);
                 ((volatile int *)&sh.broken)[0] = 1;
@@ -878,6 +879,7 @@ WalkArgs walk_args(csgd_t *d, const csgd_force_params *p)
     a.tasks = d->tasks;
     a.roots = d->roots;
     a.sc = d->sc;
+    a.wait_polls = csgd_wait_polls(d);
     a.ax = d->ax;
     a.ay = d->ay;
     a.az = d->az;

@@ -18,9 +18,35 @@ csgd_t *csg_thread_dev(void)
         if (tl_dev) /* the free functions export the tree into the caller's pool */
             csgd_set_export_order(tl_dev, 1);
         if (!tl_dev)
-            tl_error = CSG_ERR_NO_DEVICE;
+            tl_error = csgd_has_device() ? CSG_ERR_NOMEM : CSG_ERR_NO_DEVICE;
     }
     return tl_dev;
+}
+
+CSG_EXPORT void csg_release_thread_state(void)
+{
+    if (tl_dev)
+        csgd_destroy(tl_dev);
+    tl_dev = NULL;
+    tl_error = CSG_OK;
+}
+
+CSG_EXPORT void csg_set_wait_limit(int polls)
+{
+    csgd_t *d = csg_thread_dev();
+    if (!d)
+        return;
+    csgd_set_wait_limit(d, polls);
+    tl_error = CSG_OK;
+}
+
+CSG_EXPORT int csg_check_device_wait(int polls, int *status)
+{
+    csgd_t *d = csg_thread_dev();
+    if (!d)
+        return tl_error;
+    tl_error = csgd_check_device_wait(d, polls, status);
+    return tl_error;
 }
 
 void csg_thread_set_error(int code) { tl_error = code; }

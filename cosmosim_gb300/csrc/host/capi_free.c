@@ -53,6 +53,16 @@ static int store_pool(csgd_t *d, OctreeNode *pool, int *pool_size, int n)
     return CSG_OK;
 }
 
+/* Records a free function's status for csg_last_error. A failed call also
+   waits for its queued work and discards what it left for a later sync (a
+   device error flag, a parked host error), so the next call starts clean. */
+static void finish(csgd_t *d, int rc)
+{
+    if (rc)
+        (void)csgd_sync(d);
+    csg_thread_set_error(rc);
+}
+
 CSG_EXPORT void octree_build(OctreeNode *pool, int *pool_size, const Body *bodies, int n)
 {
     csgd_t *d = csg_thread_dev();
@@ -67,7 +77,7 @@ CSG_EXPORT void octree_build(OctreeNode *pool, int *pool_size, const Body *bodie
         rc = csgd_build_tree(d, 1);
     if (!rc)
         rc = store_pool(d, pool, pool_size, n);
-    csg_thread_set_error(rc);
+    finish(d, rc);
 }
 
 static void compute_forces(const OctreeNode *pool, int root, Body *bodies, int n, double G,
@@ -92,7 +102,7 @@ static void compute_forces(const OctreeNode *pool, int root, Body *bodies, int n
         rc = csgd_download_bodies(d, bodies, n);
     if (!rc)
         rc = csgd_sync(d);
-    csg_thread_set_error(rc);
+    finish(d, rc);
 }
 
 CSG_EXPORT void octree_compute_forces(const OctreeNode *pool, int root, Body *bodies, int n,
@@ -122,7 +132,7 @@ CSG_EXPORT int octree_find_neighbors(const OctreeNode *pool, int root, const Bod
     int rc = load_pool(d, pool, root, bodies, n);
     if (!rc)
         rc = csgd_find_neighbors(d, cx, cy, cz, radius, neighbor_buf, buf_capacity, &count);
-    csg_thread_set_error(rc);
+    finish(d, rc);
     return rc ? 0 : count;
 }
 
@@ -148,7 +158,7 @@ CSG_EXPORT void integrator_init_accelerations(Body *bodies, int n, double G, dou
         rc = csgd_download_bodies(d, bodies, n);
     if (!rc)
         rc = csgd_sync(d);
-    csg_thread_set_error(rc);
+    finish(d, rc);
 }
 
 CSG_EXPORT void integrator_step(Body *bodies, int n, double dt, double G, double softening,
@@ -179,7 +189,7 @@ CSG_EXPORT void integrator_step(Body *bodies, int n, double dt, double G, double
         rc = csgd_download_step_fields(d, bodies, n, sph_enabled ? 1 : 0);
     if (!rc)
         rc = csgd_sync(d);
-    csg_thread_set_error(rc);
+    finish(d, rc);
 }
 
 static void sph_pass(Body *bodies, int n, const OctreeNode *tree, int which)
@@ -202,7 +212,7 @@ static void sph_pass(Body *bodies, int n, const OctreeNode *tree, int which)
         rc = csgd_download_bodies(d, bodies, n);
     if (!rc)
         rc = csgd_sync(d);
-    csg_thread_set_error(rc);
+    finish(d, rc);
 }
 
 CSG_EXPORT void sph_compute_density(Body *bodies, int n, const OctreeNode *tree)
@@ -231,7 +241,7 @@ CSG_EXPORT void sph_apply_cooling(Body *bodies, int n, double dt)
         rc = csgd_download_bodies(d, bodies, n);
     if (!rc)
         rc = csgd_sync(d);
-    csg_thread_set_error(rc);
+    finish(d, rc);
 }
 
 /* ---- quasar step (reference src/quasar.c:477-509) on the GPU ---------------- */
@@ -259,7 +269,7 @@ CSG_EXPORT void csg_quasar_step(Body *bodies, int *n, int n_alloc, QuasarConfig 
         *n = new_n;
         cfg->jet_count = jets;
     }
-    csg_thread_set_error(rc);
+    finish(d, rc);
 }
 
 CSG_EXPORT int csg_sort_keys(const uint64_t *keys, int n, int bits, uint64_t *out_keys,
@@ -270,7 +280,7 @@ CSG_EXPORT int csg_sort_keys(const uint64_t *keys, int n, int bits, uint64_t *ou
         return CSG_ERR_NO_DEVICE;
     int rc = csgd_sort_keys(d, (const unsigned long long *)keys, n, bits,
                             (unsigned long long *)out_keys, out_index);
-    csg_thread_set_error(rc);
+    finish(d, rc);
     return rc;
 }
 

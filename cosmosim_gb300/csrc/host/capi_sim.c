@@ -90,7 +90,7 @@ static SimState *start_systems(SimState *s, int n_sys, const int *counts)
 {
     s->dev = csgd_create();
     if (!s->dev) {
-        csg_thread_set_error(CSG_ERR_NO_DEVICE);
+        csg_thread_set_error(csgd_has_device() ? CSG_ERR_NOMEM : CSG_ERR_NO_DEVICE);
         destroy_state(s);
         return NULL;
     }
@@ -321,7 +321,8 @@ CSG_EXPORT SimHandle cosmosim_create_ensemble_ics(int kind, int n_sys, const int
     SimState *s = (SimState *)calloc(1, sizeof(SimState));
     Body *host = (Body *)calloc((size_t)n, sizeof(Body));
     csgd_t *d = csgd_create();
-    int rc = (!s || !host) ? CSG_ERR_NOMEM : (!d ? CSG_ERR_NO_DEVICE : CSG_OK);
+    int rc = (!s || !host) ? CSG_ERR_NOMEM
+             : (!d ? (csgd_has_device() ? CSG_ERR_NOMEM : CSG_ERR_NO_DEVICE) : CSG_OK);
     if (!rc)
         rc = csgd_reserve(d, n);
     if (!rc) /* generated straight into the device Body staging */
@@ -601,6 +602,15 @@ CSG_EXPORT int cosmosim_set_stream(SimHandle handle, void *cuda_stream)
     int rc = csgd_sync(s->dev);
     csgd_set_stream(s->dev, cuda_stream);
     return set_err(s, rc);
+}
+
+CSG_EXPORT int cosmosim_set_wait_limit(SimHandle handle, int polls)
+{
+    if (!handle)
+        return CSG_ERR_BAD_ARG;
+    SimState *s = (SimState *)handle;
+    csgd_set_wait_limit(s->dev, polls);
+    return set_err(s, CSG_OK);
 }
 
 CSG_EXPORT int cosmosim_build_tree_async(SimHandle handle)

@@ -89,6 +89,11 @@ _SIGS = {
     "csg_last_error": ([], _i),
     "csg_error_string": ([_i], ctypes.c_char_p),
     "csg_set_precision": ([_i], None),
+    "csg_release_thread_state": ([], None),
+    "cosmosim_set_wait_limit": ([_vp, _i], _i),
+    "csg_set_wait_limit": ([_i], None),
+    "csg_check_device_wait": ([_i, _ip], _i),
+    "csg_inject_alloc_failure": ([ctypes.c_longlong], None),
     "csg_generate_ics": ([_i, _i, ctypes.c_uint64, _vp], _i),
     "cosmosim_direct_forces": ([_vp, _vp, _i, _vp], _i),
     "cosmosim_energy": ([_vp, ctypes.POINTER(_d), ctypes.POINTER(_d)], _i),

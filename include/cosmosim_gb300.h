@@ -67,6 +67,36 @@ CSG_EXPORT const char *csg_error_string(int code);
 /* Precision the calling thread's free functions use (default FP64). */
 CSG_EXPORT void csg_set_precision(int precision);
 
+/* Frees the calling thread's device state (the free functions create one per
+   thread on first use; a thread pool can release it before a thread ends).
+   The next free-function call on the thread creates a new one. */
+CSG_EXPORT void csg_release_thread_state(void);
+
+/* ---- Failure handling and fault injection ----------------------------------
+   No counterpart in the reference (its API has no error channel). Every device
+   wait in the library is bounded; the walks' producer/consumer waits give up
+   after `polls` polls (default 2^22, about 0.3 s) and report
+   CSG_ERR_DEVICE_WAIT at the next sync, with the context still usable.
+   cosmosim_set_wait_limit / csg_set_wait_limit lower that limit for a handle /
+   the calling thread's free functions (polls <= 0 restores the default) — for
+   tests that make a wait run out. */
+CSG_EXPORT int cosmosim_set_wait_limit(SimHandle handle, int polls);
+CSG_EXPORT void csg_set_wait_limit(int polls);
+
+/* Self-check of the tree sort's look-back wait: runs it, on the calling
+   thread's GPU state, on a status word that nothing publishes, with the given
+   poll limit (>= 1). *status receives what the wait reported:
+   CSG_ERR_DEVICE_WAIT when it gave up, as it must. Returns CSG_OK when the
+   check ran. */
+CSG_EXPORT int csg_check_device_wait(int polls, int *status);
+
+/* Allocation-failure injection: the next `allow` device or pinned-host
+   allocations of the library succeed and every later one fails, as on a GPU
+   out of memory, until csg_inject_alloc_failure(-1). Calls that need memory
+   then fail with CSG_ERR_NOMEM (cosmosim_create* return NULL) and leave the
+   caller's arrays unchanged. Process-wide; for tests. */
+CSG_EXPORT void csg_inject_alloc_failure(long long allow);
+
 /* Status of the handle's last call; 0 = success. The reference API has no
    error channel; this is an additive one. */
 CSG_EXPORT int cosmosim_last_error(SimHandle handle);
