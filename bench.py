@@ -68,7 +68,8 @@ FLOP_PER_INTERACTION = 20  # monopole body-cell interaction: 3 sub, 3 fma d2, rs
 WALK32_DRAM_BYTES_PER_BODY = 10.06e6 / 100_000
 # issue slots busy in the same capture (k_walk32, 100k merger): 57.8%
 WALK32_ISSUE_BUSY = 0.578
-WALK32_NOTE = ("20 flop per reference interaction / walk event time; peak = FP32 FMA throughput "
+WALK32_NOTE = ("20 flop per reference interaction / the walk's time inside the substep (CUDA "
+               "events around it, SPH running beside it); peak = FP32 FMA throughput "
                "measured live by csg_measure_fp_peaks (the walk is CUDA-core bound: no dense "
                "contraction, tree resident in L2). What bounds it is instruction issue in the "
                "traversal. traffic and issue_slots_busy_ncu are per-launch DRAM bytes and issue "
@@ -233,15 +234,27 @@ def run_cuda(args, torch, lib, cfg, rank, world, sampler):
         secs = time_substeps(torch, sim, k, flush, sampler)
         sim.sync()  # raises if any substep reported an error
         launches = sim.launch_count() - l0
-        # phases on the state reached: tree build and gravity walk alone
-        build_s = time_phase(torch, sim.build_tree_async, 5, flush)
-        walk_s = time_phase(torch, sim.gravity_async, 5, flush)
+        # phases inside the real substep: the same kernels, direct launches
+        # with CUDA events between the phases (cosmosim_phase_times)
+        sim.enable_phase_timing(True)
+        for _ in range(k):
+            flush.zero_()
+            sim.substeps_async(1)
+        sim.sync()
+        ph = sim.phase_times()
+        sim.enable_phase_timing(False)
+        phases = {key[:-3]: ph[key] / ph["substeps"] for key in ph if key.endswith("_ms")}
+        walk_s = phases["gravity"] / 1e3
+        build_s = phases["build"] / 1e3
+        # the walk launched alone on the state reached (no SPH beside it)
+        walk_alone_s = time_phase(torch, sim.gravity_async, 5, flush)
         sim.sync()
         sim.enable_stats(True)
         sim.gravity_async()
         inter, wsteps, wactive = sim.walk_stats()
         sim.enable_stats(False)
         out[name] = dict(secs=secs, steps=k, launches=launches, build_s=build_s, walk_s=walk_s,
+                         walk_alone_s=walk_alone_s, phases=phases,
                          interactions=inter, warp_steps=wsteps, active_lane_steps=wactive,
                          state=sim.bodies() if name == "fp32_mixed" else None)
         sim.close()
@@ -879,8 +892,12 @@ def main():
                        "walk_ms": 1e3 * f64["walk_s"],
                        "walk_tflops": achieved64, "fp64_peak_tflops": fp64_peak,
                        "walk_frac_of_fp64_peak": achieved64 / fp64_peak},
-        "phases_ms": {"build": 1e3 * f32["build_s"], "walk_fp32": 1e3 * f32["walk_s"],
-                      "walk_fp64": 1e3 * f64["walk_s"]},
+        "phases_ms": {"fp32_mixed": f32["phases"], "fp64": f64["phases"],
+                      "walk_alone_fp32": 1e3 * f32["walk_alone_s"],
+                      "walk_alone_fp64": 1e3 * f64["walk_alone_s"],
+                      "how": "per substep, CUDA events between the phases of the real substep "
+                             "(cosmosim_phase_times, direct launches, L2 flushed between "
+                             "substeps); walk_alone = the walk launched by itself"},
         "interactions_per_substep": f32["interactions"],
         "walk_traversal": {"warp_steps": f32["warp_steps"],
                            "lane_utilisation": f32["active_lane_steps"] / max(32 * f32["warp_steps"], 1),

@@ -164,6 +164,13 @@ struct csgd {
     int stats;
     int host_err; // first error seen on the host side (launch, allocation)
     int wait_polls; // limit of the bounded device waits (0: the default, 2^22 polls)
+    // phase timing (csgd_set_phase_timing): events between the phases of a
+    // substep on the main stream (tev); around SPH on its stream and at the
+    // main stream's rejoin (taux); sums of the phase times so far
+    int timing;
+    cudaEvent_t tev[7], taux[3];
+    double phase_ms[7]; // kick+drift, build, gravity, SPH, kick, cooling, substep
+    long long timed_substeps;
     unsigned long long launches; // kernels launched on this state (measurement)
 
     // bodies, caller index order

@@ -7,6 +7,8 @@
 
 #include <atomic>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <stdlib.h>
 #include <string.h>
 
@@ -397,6 +399,12 @@ extern "C" void csgd_destroy(csgd_t *d)
         cudaEventDestroy(d->ev_fork2);
         cudaEventDestroy(d->ev_join2);
     }
+    for (int k = 0; k < 7; k++)
+        if (d->tev[k])
+            cudaEventDestroy(d->tev[k]);
+    for (int k = 0; k < 3; k++)
+        if (d->taux[k])
+            cudaEventDestroy(d->taux[k]);
     if (d->own_stream)
         cudaStreamDestroy(d->own_stream);
     free(d);
@@ -735,6 +743,20 @@ extern "C" int csgd_sph_cooling(csgd_t *d, double dt)
 // pressure, smoothing lengths and its pair terms), so they run on two streams
 // and the force sums, which add to the accelerations, wait for both. In a
 // captured substep the fork and join become graph edges.
+// Phase k of a substep starts: an NVTX range named for the phase (k = 6 only
+// closes the last one) and, when timing, event tev[k] on the main stream.
+static void phase_mark(csgd_t *d, int k)
+{
+    static const char *const names[6] = {"csg.kick_drift", "csg.build", "csg.gravity",
+                                         "csg.sph", "csg.kick", "csg.cooling"};
+    if (k > 0)
+        nvtxRangePop();
+    if (k < 6)
+        nvtxRangePushA(names[k]);
+    if (d->timing)
+        cudaEventRecord(d->tev[k], d->stream);
+}
+
 extern "C" int csgd_substep(csgd_t *d, double dt, const csgd_force_params *p, int sph)
 {
     // what a substep allocates on first use, before its first kernel: an
@@ -745,9 +767,12 @@ extern "C" int csgd_substep(csgd_t *d, double dt, const csgd_force_params *p, in
         rc = csgd_ensure_tree_extras(d, 1, 1);
     if (rc)
         return rc;
+    phase_mark(d, 0);
     rc = csgd_kick_drift(d, dt);
+    phase_mark(d, 1);
     if (!rc)
         rc = csgd_build_tree(d, sph);
+    phase_mark(d, 2);
     // the pool export reads the finished tree only: it runs beside the walk
     bool exported = false;
     if (!rc && d->export_dst && d->aux2) {
@@ -765,13 +790,20 @@ extern "C" int csgd_substep(csgd_t *d, double dt, const csgd_force_params *p, in
         cudaEventRecord(d->ev_fork, main);
         cudaStreamWaitEvent(d->aux, d->ev_fork, 0);
         d->stream = d->aux;
+        if (d->timing)
+            cudaEventRecord(d->taux[0], d->aux);
         rc = csgd_sph_density(d);
         if (!rc)
             rc = csgd_sph_force_terms(d, 1);
+        if (d->timing)
+            cudaEventRecord(d->taux[1], d->aux);
         d->stream = main;
         cudaEventRecord(d->ev_join, d->aux);
         const int rg = csgd_gravity(d, p);
+        phase_mark(d, 3); // the SPH sums on this stream count as SPH
         cudaStreamWaitEvent(main, d->ev_join, 0); // always rejoin (a capture needs it)
+        if (d->timing)
+            cudaEventRecord(d->taux[2], main);
         if (!rc)
             rc = rg;
         if (!rc)
@@ -779,19 +811,75 @@ extern "C" int csgd_substep(csgd_t *d, double dt, const csgd_force_params *p, in
     } else {
         if (!rc)
             rc = csgd_gravity(d, p);
+        phase_mark(d, 3);
         if (!rc && sph) {
             rc = csgd_sph_density(d);
             if (!rc)
                 rc = csgd_sph_forces(d, 1);
         }
     }
+    phase_mark(d, 4);
     if (!rc)
         rc = csgd_kick(d, dt);
+    phase_mark(d, 5);
     if (!rc && sph)
         rc = csgd_sph_cooling(d, dt);
     if (exported)
         cudaStreamWaitEvent(d->stream, d->ev_join2, 0); // always rejoin (a capture needs it)
+    phase_mark(d, 6);
     return rc;
+}
+
+// Adds the phase times of the substep just queued (waits for it). SPH that
+// overlapped the walk on its own stream counts its own span plus the sums
+// after the rejoin (the main stream's wait for it is in neither phase, only
+// in the substep's total); the gravity phase is then the walk alone.
+static int add_phase_times(csgd_t *d, int sph_overlapped)
+{
+    if (cudaEventSynchronize(d->tev[6]) != cudaSuccess)
+        return csgd_check(d, cudaGetLastError());
+    float t[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, whole = 0.f, aux = 0.f;
+    for (int k = 0; k < 6; k++)
+        if (cudaEventElapsedTime(&t[k], d->tev[k], d->tev[k + 1]) != cudaSuccess)
+            return csgd_check(d, cudaGetLastError());
+    if (cudaEventElapsedTime(&whole, d->tev[0], d->tev[6]) != cudaSuccess)
+        return csgd_check(d, cudaGetLastError());
+    if (sph_overlapped && (cudaEventElapsedTime(&aux, d->taux[0], d->taux[1]) != cudaSuccess ||
+                           cudaEventElapsedTime(&t[3], d->taux[2], d->tev[4]) != cudaSuccess))
+        return csgd_check(d, cudaGetLastError());
+    for (int k = 0; k < 6; k++)
+        d->phase_ms[k] += t[k];
+    d->phase_ms[3] += aux;
+    d->phase_ms[6] += whole;
+    d->timed_substeps++;
+    return CSG_OK;
+}
+
+extern "C" int csgd_set_phase_timing(csgd_t *d, int on)
+{
+    if (on && !d->tev[0]) {
+        for (int k = 0; k < 7; k++)
+            if (cudaEventCreate(&d->tev[k]) != cudaSuccess)
+                return csgd_check(d, cudaGetLastError());
+        for (int k = 0; k < 3; k++)
+            if (cudaEventCreate(&d->taux[k]) != cudaSuccess)
+                return csgd_check(d, cudaGetLastError());
+    }
+    d->timing = on ? 1 : 0;
+    if (on) { // a new measurement; turning it off keeps the sums for reading
+        for (int k = 0; k < 7; k++)
+            d->phase_ms[k] = 0.0;
+        d->timed_substeps = 0;
+    }
+    return CSG_OK;
+}
+
+extern "C" int csgd_phase_times(const csgd_t *d, double ms[7], long long *substeps)
+{
+    for (int k = 0; k < 7; k++)
+        ms[k] = d->phase_ms[k];
+    *substeps = d->timed_substeps;
+    return CSG_OK;
 }
 
 // ---- synchronisation and queries ---------------------------------------
@@ -956,6 +1044,16 @@ extern "C" int csgd_substeps(csgd_t *d, int k, double dt, const csgd_force_param
 {
     if (k <= 0)
         return CSG_OK;
+    if (d->timing) { // direct launches, each substep's phase events read back
+        const int overlapped = sph && d->aux && d->n_gal == 1;
+        int rc = CSG_OK;
+        for (int i = 0; i < k && !rc; i++) {
+            rc = csgd_substep(d, dt, p, sph);
+            if (!rc)
+                rc = add_phase_times(d, overlapped);
+        }
+        return rc;
+    }
     if (d->use_graphs && d->n > 0 && d->stream != nullptr && !graph_matches(d, dt, p, sph)) {
         const int crc = capture_substep(d, dt, p, sph);
         if (crc == CSG_ERR_NOMEM) // nothing ran; a later call captures again

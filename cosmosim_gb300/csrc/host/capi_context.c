@@ -131,3 +131,38 @@ int csg_pool_extent(const OctreeNode *pool, int root, int *n_nodes)
         *n_nodes = hi + 1;
     return rc;
 }
+
+int csg_fill_phase_times(const csgd_t *d, CsgPhaseTimes *out)
+{
+    double ms[7];
+    long long k = 0;
+    if (!out)
+        return CSG_ERR_BAD_ARG;
+    csgd_phase_times(d, ms, &k);
+    out->kick_drift_ms = ms[0];
+    out->build_ms = ms[1];
+    out->gravity_ms = ms[2];
+    out->sph_ms = ms[3];
+    out->kick_ms = ms[4];
+    out->cooling_ms = ms[5];
+    out->substep_ms = ms[6];
+    out->substeps = k;
+    return CSG_OK;
+}
+
+CSG_EXPORT int csg_enable_phase_timing(int on)
+{
+    csgd_t *d = csg_thread_dev();
+    if (!d)
+        return tl_error;
+    tl_error = csgd_set_phase_timing(d, on);
+    return tl_error;
+}
+
+CSG_EXPORT int csg_phase_times(CsgPhaseTimes *out)
+{
+    csgd_t *d = csg_thread_dev();
+    if (!d)
+        return tl_error;
+    return csg_fill_phase_times(d, out);
+}

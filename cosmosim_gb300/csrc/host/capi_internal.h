@@ -36,5 +36,7 @@ void csg_ref_quasar_merger(Body *bodies, int n, double separation, double approa
 void csg_ref_merger_dust(Body *bodies, int start_idx, int n_dust, double separation,
                          uint64_t seed);
 int csg_disk_plan(int kind, uint64_t seed, csgd_disk_plan *plan);
+/* Copies a device state's phase sums into the C-ABI record. */
+int csg_fill_phase_times(const csgd_t *d, CsgPhaseTimes *out);
 
 #endif

@@ -604,6 +604,25 @@ CSG_EXPORT int cosmosim_set_stream(SimHandle handle, void *cuda_stream)
     return set_err(s, rc);
 }
 
+CSG_EXPORT int cosmosim_enable_phase_timing(SimHandle handle, int on)
+{
+    if (!handle)
+        return CSG_ERR_BAD_ARG;
+    SimState *s = (SimState *)handle;
+    int rc = csgd_sync(s->dev);
+    if (!rc)
+        rc = csgd_set_phase_timing(s->dev, on);
+    return set_err(s, rc);
+}
+
+CSG_EXPORT int cosmosim_phase_times(SimHandle handle, CsgPhaseTimes *out)
+{
+    if (!handle)
+        return CSG_ERR_BAD_ARG;
+    SimState *s = (SimState *)handle;
+    return set_err(s, csg_fill_phase_times(s->dev, out));
+}
+
 CSG_EXPORT int cosmosim_set_wait_limit(SimHandle handle, int polls)
 {
     if (!handle)

@@ -40,6 +40,14 @@ class CsgWalkShape(ctypes.Structure):
                 "blocks_per_sm": self.blocks_per_sm, "ms": round(float(self.ms), 4)}
 
 
+class CsgPhaseTimes(ctypes.Structure):
+    _fields_ = [(f, _d) for f in ("kick_drift_ms", "build_ms", "gravity_ms", "sph_ms", "kick_ms",
+                                  "cooling_ms", "substep_ms")] + [("substeps", ctypes.c_longlong)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class CudaError(RuntimeError):
     pass
 
@@ -90,6 +98,10 @@ _SIGS = {
     "csg_error_string": ([_i], ctypes.c_char_p),
     "csg_set_precision": ([_i], None),
     "csg_release_thread_state": ([], None),
+    "cosmosim_enable_phase_timing": ([_vp, _i], _i),
+    "cosmosim_phase_times": ([_vp, ctypes.POINTER(CsgPhaseTimes)], _i),
+    "csg_enable_phase_timing": ([_i], _i),
+    "csg_phase_times": ([ctypes.POINTER(CsgPhaseTimes)], _i),
     "cosmosim_set_wait_limit": ([_vp, _i], _i),
     "csg_set_wait_limit": ([_i], None),
     "csg_check_device_wait": ([_i, _ip], _i),
@@ -359,6 +371,17 @@ class Sim:
 
     def sync(self):
         self._rc(self.lib.cosmosim_sync(self.h), "sync")
+
+    def enable_phase_timing(self, on=True):
+        """Substeps run as direct launches with CUDA events between phases
+        (cosmosim_enable_phase_timing); enabling resets the sums."""
+        self._rc(self.lib.cosmosim_enable_phase_timing(self.h, int(on)), "phase_timing")
+
+    def phase_times(self):
+        """Summed phase times (ms) and the substeps timed (cosmosim_phase_times)."""
+        t = CsgPhaseTimes()
+        self._rc(self.lib.cosmosim_phase_times(self.h, ctypes.byref(t)), "phase_times")
+        return t.as_dict()
 
     def set_stream(self, stream_ptr):
         self._rc(self.lib.cosmosim_set_stream(self.h, ctypes.c_void_p(stream_ptr)), "set_stream")

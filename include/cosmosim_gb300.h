@@ -198,6 +198,31 @@ CSG_EXPORT int cosmosim_set_bodies(SimHandle handle, const Body *bodies, int n);
 CSG_EXPORT int cosmosim_build_tree_async(SimHandle handle);
 CSG_EXPORT int cosmosim_gravity_async(SimHandle handle);
 
+/* Per-phase timing of the real substep — no counterpart in the reference,
+   which has no tracing. With timing on, a handle's substeps run as direct
+   launches (not the captured graph) with CUDA events between their phases
+   and NVTX ranges ("csg.kick_drift", "csg.build", "csg.gravity", "csg.sph",
+   "csg.kick", "csg.cooling") around them; each substep waits for its events,
+   and the phase times add up until read. SPH that overlaps the gravity walk
+   on its own stream counts its own span plus its sums after the walk; the
+   substep total is the elapsed time of the whole substep. Enabling resets
+   the sums; disabling keeps them for reading and returns to graph replays. */
+typedef struct {
+    double kick_drift_ms; /* first half kick + drift */
+    double build_ms;      /* bounding box, keys, sort, cells, moments */
+    double gravity_ms;    /* the Barnes-Hut walk */
+    double sph_ms;        /* neighbour lists, density, pressure and viscosity forces */
+    double kick_ms;       /* second half kick */
+    double cooling_ms;    /* SPH cooling */
+    double substep_ms;    /* whole substeps */
+    long long substeps;   /* substeps timed */
+} CsgPhaseTimes;
+CSG_EXPORT int cosmosim_enable_phase_timing(SimHandle handle, int on);
+CSG_EXPORT int cosmosim_phase_times(SimHandle handle, CsgPhaseTimes *out);
+/* The same for the calling thread's free functions (integrator_step). */
+CSG_EXPORT int csg_enable_phase_timing(int on);
+CSG_EXPORT int csg_phase_times(CsgPhaseTimes *out);
+
 /* Interaction counting (accepted cells + leaves, the reference walk's unit). */
 CSG_EXPORT int cosmosim_enable_stats(SimHandle handle, int on);
 CSG_EXPORT int cosmosim_interactions(SimHandle handle, int64_t *total);
