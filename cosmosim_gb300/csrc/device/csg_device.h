@@ -116,10 +116,11 @@ int csgd_quasar_state(csgd_t *d, unsigned long long rng, int knot_phase);
 /* Phase timing: on = 1 makes every later substep run as direct launches with
    CUDA events between its phases (and NVTX ranges around them), waiting for
    each substep's events; the phase times add up in ms[7] (kick+drift, tree
-   build, gravity walk, SPH, second kick, cooling, whole substep). Turning it
-   on resets the sums; turning it off keeps them for reading. */
+   build, gravity walk, SPH, second kick, cooling, whole substep), then in
+   ms[7..11] the build's parts (keys, sort, cells, moments, the rest). Turning
+   it on resets the sums; turning it off keeps them for reading. */
 int csgd_set_phase_timing(csgd_t *d, int on);
-int csgd_phase_times(const csgd_t *d, double ms[7], long long *substeps);
+int csgd_phase_times(const csgd_t *d, double ms[12], long long *substeps);
 /* 1 when a CUDA device is visible (tells allocation failures from a missing GPU). */
 int csgd_has_device(void);
 /* Limit of the walks' bounded producer/consumer waits, in polls (<= 0: the

@@ -171,6 +171,10 @@ struct csgd {
     cudaEvent_t tev[7], taux[3];
     double phase_ms[7]; // kick+drift, build, gravity, SPH, kick, cooling, substep
     long long timed_substeps;
+    // the build's own parts (keys, sort, cells, moments, the rest), between
+    // events bev[0..5] recorded by csgd_build_tree while timing
+    cudaEvent_t bev[6];
+    double build_ms[5];
     unsigned long long launches; // kernels launched on this state (measurement)
 
     // bodies, caller index order
@@ -250,6 +254,8 @@ struct csgd {
 };
 
 // ---- helpers shared by the .cu files ----
+// Event k of the build's parts (timing only; see csgd::bev).
+void csgd_build_mark(csgd_t *d, int k);
 // Every device and pinned-host allocation of the library goes through these
 // two. Fault injection (csg_inject_alloc_failure) can make them fail: the
 // next `k` allocations succeed, every later one returns

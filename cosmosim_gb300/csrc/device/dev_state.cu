@@ -405,6 +405,9 @@ extern "C" void csgd_destroy(csgd_t *d)
     for (int k = 0; k < 3; k++)
         if (d->taux[k])
             cudaEventDestroy(d->taux[k]);
+    for (int k = 0; k < 6; k++)
+        if (d->bev[k])
+            cudaEventDestroy(d->bev[k]);
     if (d->own_stream)
         cudaStreamDestroy(d->own_stream);
     free(d);
@@ -830,6 +833,12 @@ extern "C" int csgd_substep(csgd_t *d, double dt, const csgd_force_params *p, in
     return rc;
 }
 
+void csgd_build_mark(csgd_t *d, int k)
+{
+    if (d->timing && d->bev[k])
+        cudaEventRecord(d->bev[k], d->stream);
+}
+
 // Adds the phase times of the substep just queued (waits for it). SPH that
 // overlapped the walk on its own stream counts its own span plus the sums
 // after the rejoin (the main stream's wait for it is in neither phase, only
@@ -847,6 +856,12 @@ static int add_phase_times(csgd_t *d, int sph_overlapped)
     if (sph_overlapped && (cudaEventElapsedTime(&aux, d->taux[0], d->taux[1]) != cudaSuccess ||
                            cudaEventElapsedTime(&t[3], d->taux[2], d->tev[4]) != cudaSuccess))
         return csgd_check(d, cudaGetLastError());
+    for (int k = 0; k < 5; k++) {
+        float b = 0.f;
+        if (cudaEventElapsedTime(&b, d->bev[k], d->bev[k + 1]) != cudaSuccess)
+            return csgd_check(d, cudaGetLastError());
+        d->build_ms[k] += b;
+    }
     for (int k = 0; k < 6; k++)
         d->phase_ms[k] += t[k];
     d->phase_ms[3] += aux;
@@ -864,9 +879,14 @@ extern "C" int csgd_set_phase_timing(csgd_t *d, int on)
         for (int k = 0; k < 3; k++)
             if (cudaEventCreate(&d->taux[k]) != cudaSuccess)
                 return csgd_check(d, cudaGetLastError());
+        for (int k = 0; k < 6; k++)
+            if (cudaEventCreate(&d->bev[k]) != cudaSuccess)
+                return csgd_check(d, cudaGetLastError());
     }
     d->timing = on ? 1 : 0;
     if (on) { // a new measurement; turning it off keeps the sums for reading
+        for (int k = 0; k < 5; k++)
+            d->build_ms[k] = 0.0;
         for (int k = 0; k < 7; k++)
             d->phase_ms[k] = 0.0;
         d->timed_substeps = 0;
@@ -874,10 +894,12 @@ extern "C" int csgd_set_phase_timing(csgd_t *d, int on)
     return CSG_OK;
 }
 
-extern "C" int csgd_phase_times(const csgd_t *d, double ms[7], long long *substeps)
+extern "C" int csgd_phase_times(const csgd_t *d, double ms[12], long long *substeps)
 {
     for (int k = 0; k < 7; k++)
         ms[k] = d->phase_ms[k];
+    for (int k = 0; k < 5; k++)
+        ms[7 + k] = d->build_ms[k];
     *substeps = d->timed_substeps;
     return CSG_OK;
 }

@@ -1148,6 +1148,7 @@ static int order_bodies(csgd_t *d)
     DevScalars *sc = d->sc;
     const int B = 256;
     const int G = d->n_gal;
+    csgd_build_mark(d, 0);
     { k_reset<<<1, 256, 0, s>>>(sc, d->roots, G); d->launches++; }
     // few blocks: each warp flushes its running box with atomics on the same
     // words, so fewer warps contend less (4 blocks per SM keep HBM busy)
@@ -1156,6 +1157,7 @@ static int order_bodies(csgd_t *d)
     { k_root<<<1, 256, 0, s>>>(sc, d->roots, G); d->launches++; }
     if (n > 0)
         { k_keys<<<csgd_grid(n, B), B, 0, s>>>(d->x, d->y, d->z, d->m, d->gid, n, sc, d->roots, d->key, d->perm); d->launches++; }
+    csgd_build_mark(d, 1);
     int rc = csg_radix_sort(d, d->key, d->perm, d->key_alt, d->perm_alt, n, 64);
     if (rc)
         return rc;
@@ -1199,6 +1201,7 @@ extern "C" int csgd_build_tree(csgd_t *d, int geometry)
     if (rc)
         return rc;
     const int g = csgd_grid(n > 0 ? n : 1, B);
+    csgd_build_mark(d, 2);
     { k_deep_mark<<<g, B, 0, s>>>(d->x, d->y, d->z, sc, d->roots, d->key, d->sgid, d->perm, d->ext); d->launches++; }
     { k_deep_sort<<<g, B, 0, s>>>(sc, d->key, d->sgid, d->perm, d->ext); d->launches++; }
     { k_count<<<g, B, 0, s>>>(sc, d->key, d->ext, d->sgid, d->lcp, d->cnt); d->launches++; }
@@ -1209,11 +1212,13 @@ extern "C" int csgd_build_tree(csgd_t *d, int geometry)
     { k_nodes<<<g, B, 0, s>>>(*d, sc, d->roots, d->key, d->ext, d->sgid, d->lcp, d->base, d->perm, d->cnt); d->launches++; }
     const int gn = csgd_grid(cell_threads(d), B);
     { k_link<<<gn, B, 0, s>>>(*d, sc, d->key, d->ext); d->launches++; }
+    csgd_build_mark(d, 3);
     if (d->export_order)
         { k_moments<true><<<gn, B, 0, s>>>(*d, sc, d->x, d->y, d->z, d->m, d->perm); d->launches++; }
     else
         { k_moments<false><<<gn, B, 0, s>>>(*d, sc, d->x, d->y, d->z, d->m, d->perm); d->launches++; }
     d->minidx_valid = d->export_order;
+    csgd_build_mark(d, 4);
     { k_tasks<<<min(d->n_gal, 152), 256, 0, s>>>(sc, d->roots, d->n_gal, d->base, d->tasks, d->task_cap, 0); d->launches++; }
     d->geometry_valid = 0;
     d->imported = 0;
@@ -1222,6 +1227,7 @@ extern "C" int csgd_build_tree(csgd_t *d, int geometry)
         { k_geometry<<<gn, B, 0, s>>>(*d, sc, d->roots, d->key, d->ext, d->sgid); d->launches++; }
         d->geometry_valid = 1;
     }
+    csgd_build_mark(d, 5);
     return csgd_check(d, cudaGetLastError());
 }
 

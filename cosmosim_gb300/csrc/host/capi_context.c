@@ -134,7 +134,7 @@ int csg_pool_extent(const OctreeNode *pool, int root, int *n_nodes)
 
 int csg_fill_phase_times(const csgd_t *d, CsgPhaseTimes *out)
 {
-    double ms[7];
+    double ms[12];
     long long k = 0;
     if (!out)
         return CSG_ERR_BAD_ARG;
@@ -147,6 +147,11 @@ int csg_fill_phase_times(const csgd_t *d, CsgPhaseTimes *out)
     out->cooling_ms = ms[5];
     out->substep_ms = ms[6];
     out->substeps = k;
+    out->build_keys_ms = ms[7];
+    out->build_sort_ms = ms[8];
+    out->build_cells_ms = ms[9];
+    out->build_moments_ms = ms[10];
+    out->build_rest_ms = ms[11];
     return CSG_OK;
 }
 

@@ -42,7 +42,9 @@ class CsgWalkShape(ctypes.Structure):
 
 class CsgPhaseTimes(ctypes.Structure):
     _fields_ = [(f, _d) for f in ("kick_drift_ms", "build_ms", "gravity_ms", "sph_ms", "kick_ms",
-                                  "cooling_ms", "substep_ms")] + [("substeps", ctypes.c_longlong)]
+                                  "cooling_ms", "substep_ms")] + [("substeps", ctypes.c_longlong)] + [
+        (f, _d) for f in ("build_keys_ms", "build_sort_ms", "build_cells_ms", "build_moments_ms",
+                          "build_rest_ms")]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -216,6 +216,12 @@ typedef struct {
     double cooling_ms;    /* SPH cooling */
     double substep_ms;    /* whole substeps */
     long long substeps;   /* substeps timed */
+    /* the build's parts (sum to build_ms): */
+    double build_keys_ms;    /* bounding box, root cube, keys */
+    double build_sort_ms;    /* radix sort of the keys */
+    double build_cells_ms;   /* shared keys, cell counts and scan, cells, links */
+    double build_moments_ms; /* masses and centres of mass */
+    double build_rest_ms;    /* walk tasks; SPH cell geometry */
 } CsgPhaseTimes;
 CSG_EXPORT int cosmosim_enable_phase_timing(SimHandle handle, int on);
 CSG_EXPORT int cosmosim_phase_times(SimHandle handle, CsgPhaseTimes *out);

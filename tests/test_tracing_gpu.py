@@ -34,6 +34,11 @@ def test_phase_times_cover_the_substep_and_change_nothing(lib, sph, prec):
     # without SPH those phases hold no kernel: only the events' own overhead
     assert (t["sph_ms"] > 0.05 * t["gravity_ms"]) == sph
     assert (t["cooling_ms"] > 0.0) and (t["cooling_ms"] < 0.05 * t["substep_ms"])
+    # the build's parts follow one another inside the build
+    parts = sum(t[k] for k in ("build_keys_ms", "build_sort_ms", "build_cells_ms",
+                               "build_moments_ms", "build_rest_ms"))
+    assert 0.9 * t["build_ms"] <= parts <= 1.001 * t["build_ms"]
+    assert min(t["build_sort_ms"], t["build_moments_ms"]) > 0.0
     # the phases on the main stream follow one another inside the substep
     assert sum(t[k] for k in MAIN) <= t["substep_ms"] * 1.001
     if not sph:
