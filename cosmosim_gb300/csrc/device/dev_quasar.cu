@@ -20,8 +20,9 @@
 //    them.
 //  * Accretion: only candidates inside the swallow radius or the ISCO can be
 //    accreted ("inner"), so only they form a sequential chain: one thread
-//    walks them in index order, updating the SMBH and recording its mass and
-//    velocity after every accretion event. Every other candidate ("outer":
+//    walks them in index order (staged a block-wide chunk at a time in shared
+//    memory), updating the SMBH and recording its mass and velocity after
+//    every accretion event. Every other candidate ("outer":
 //    possibly turned into gas and dragged, never accreted) runs in parallel
 //    with the SMBH state that holds at its index, found by binary search in
 //    that event table.
@@ -30,9 +31,11 @@
 //    jumped ahead to that offset (xs_jump), so all of them are written at
 //    once.
 // Arithmetic keeps the reference's operation order (the file is compiled
-// without fused multiply-add); sin, cos and log are CUDA's, within 2 ulp of
-// the C library's, so spawned and recycled jets agree to ~1e-15 and all other
-// fields exactly.
+// without fused multiply-add); the accretion chain's divisions and square
+// roots are the correctly rounded integer-pipe ones of dev_fpint.cuh (same
+// bits as the compiler's, at a fraction of a lone thread's FP64 latency);
+// sin, cos and log are CUDA's, within 2 ulp of the C library's, so spawned
+// and recycled jets agree to ~1e-15 and all other fields exactly.
 //
 // Fields: positions, velocities, accelerations, mass, type, density,
 // pressure, internal energy and smoothing length live in the SoA arrays;
@@ -40,6 +43,7 @@
 // (csgd::aos), their authoritative copy while the state is resident.
 #include <cooperative_groups.h>
 
+#include "dev_fpint.cuh"
 #include "dev_internal.cuh"
 
 namespace cg = cooperative_groups;
@@ -205,23 +209,23 @@ __device__ void fresh_body(const Bodies &b, int i, int type)
 __device__ void swallow(Hole &H, const Bodies &b, int v)
 {
     const double mv = b.m[v], mt = H.m + mv;
-    H.vx = (H.m * H.vx + mv * b.vx[v]) / mt;
-    H.vy = (H.m * H.vy + mv * b.vy[v]) / mt;
-    H.vz = (H.m * H.vz + mv * b.vz[v]) / mt;
+    H.vx = div_rn(H.m * H.vx + mv * b.vx[v], mt);
+    H.vy = div_rn(H.m * H.vy + mv * b.vy[v], mt);
+    H.vz = div_rn(H.m * H.vz + mv * b.vz[v], mt);
     const double px = b.x[v] - H.x, py = b.y[v] - H.y, pz = b.z[v] - H.z;
     const double qx = b.vx[v] - H.vx, qy = b.vy[v] - H.vy, qz = b.vz[v] - H.vz;
     const double jx = py * qz - pz * qy, jy = pz * qx - px * qz, jz = px * qy - py * qx;
-    const double j = sqrt(jx * jx + jy * jy + jz * jz);
+    const double j = sqrt_rn(jx * jx + jy * jy + jz * jz);
     if (j > 1e-15) {
-        const double f = mv / mt * 0.01;
-        H.sx += f * jx / j;
-        H.sy += f * jy / j;
-        H.sz += f * jz / j;
-        const double sn = sqrt(H.sx * H.sx + H.sy * H.sy + H.sz * H.sz);
+        const double f = div_rn(mv, mt) * 0.01;
+        H.sx += div_rn(f * jx, j);
+        H.sy += div_rn(f * jy, j);
+        H.sz += div_rn(f * jz, j);
+        const double sn = sqrt_rn(H.sx * H.sx + H.sy * H.sy + H.sz * H.sz);
         if (sn > 1e-15) {
-            H.sx /= sn;
-            H.sy /= sn;
-            H.sz /= sn;
+            H.sx = div_rn(H.sx, sn);
+            H.sy = div_rn(H.sy, sn);
+            H.sz = div_rn(H.sz, sn);
         }
     }
     H.m = mt;
@@ -238,7 +242,7 @@ __device__ bool settle(const Bodies &b, const QCfg &c, const Hole &H, int i, dou
 {
     const double qx = b.vx[i] - H.vx, qy = b.vy[i] - H.vy, qz = b.vz[i] - H.vz;
     const double jx = dy * qz - dz * qy, jy = dz * qx - dx * qz, jz = dx * qy - dy * qx;
-    const double r_circ = (jx * jx + jy * jy + jz * jz) / (H.m * r);
+    const double r_circ = div_rn(jx * jx + jy * jy + jz * jz, H.m * r);
     if (r_circ > c.isco_r && b.type[i] != BODY_GAS) {
         b.type[i] = BODY_GAS;
         if (b.h[i] < 1e-10)
@@ -251,14 +255,14 @@ __device__ bool settle(const Bodies &b, const QCfg &c, const Hole &H, int i, dou
     if (b.type[i] != BODY_GAS)
         return false;
     const double rx = b.x[i] - H.x, ry = b.y[i] - H.y, rz = b.z[i] - H.z;
-    const double rr = sqrt(rx * rx + ry * ry + rz * rz);
+    const double rr = sqrt_rn(rx * rx + ry * ry + rz * rz);
     if (rr < 1e-15)
         return true;
     const double wx = b.vx[i] - H.vx, wy = b.vy[i] - H.vy, wz = b.vz[i] - H.vz;
-    const double radial = (wx * rx + wy * ry + wz * rz) / rr;
-    b.ax[i] -= c.alpha * (radial * rx / rr);
-    b.ay[i] -= c.alpha * (radial * ry / rr);
-    b.az[i] -= c.alpha * (radial * rz / rr);
+    const double radial = div_rn(wx * rx + wy * ry + wz * rz, rr);
+    b.ax[i] -= c.alpha * div_rn(radial * rx, rr);
+    b.ay[i] -= c.alpha * div_rn(radial * ry, rr);
+    b.az[i] -= c.alpha * div_rn(radial * rz, rr);
     return true;
 }
 
@@ -352,45 +356,92 @@ __global__ void __launch_bounds__(QB) k_quasar_step(Bodies b, QCfg c, QuasarStat
         grid.sync();
         const int n_inner = grid_compact(grid, w.bits, nwords, w.list, w.blockcnt);
         grid.sync();
-        if (lead) { // the chain of possible accretions, in index order
+        if (blockIdx.x == 0) {
+            // The chain of possible accretions, in index order. The whole block
+            // stages a chunk of candidates in shared memory, one thread runs
+            // the chain over it (the same arithmetic on the staged copies),
+            // the block writes the candidates back.
+            __shared__ double cf[12][QB];
+            __shared__ int ct[QB];
+            const Bodies sb{cf[0], cf[1], cf[2], cf[3], cf[4], cf[5], cf[6], cf[7], cf[8], cf[9],
+                            nullptr, nullptr, cf[10], cf[11], ct, nullptr};
             Hole H{hx, hy, hz, b.vx[s], b.vy[s], b.vz[s], b.m[s], b.aos[s].spin_x,
                    b.aos[s].spin_y, b.aos[s].spin_z};
             double swallowed = q->swallowed;
             int e = 0;
-            w.ev_idx[0] = -1;
-            w.ev_m[0] = H.m;
-            w.ev_vx[0] = H.vx;
-            w.ev_vy[0] = H.vy;
-            w.ev_vz[0] = H.vz;
-            for (int t = 0; t < n_inner; t++) {
-                const int i = w.list[t];
-                const double dx = b.x[i] - hx, dy = b.y[i] - hy, dz = b.z[i] - hz;
-                const double d2 = dx * dx + dy * dy + dz * dz;
-                bool eaten = d2 < r_sw_sq;
-                if (!eaten) {
-                    const double r = sqrt(d2);
-                    eaten = settle(b, c, H, i, dx, dy, dz, r) && r < c.isco_r;
-                }
-                if (eaten) {
-                    swallowed += b.m[i];
-                    swallow(H, b, i);
-                    e++;
-                    w.ev_idx[e] = i;
-                    w.ev_m[e] = H.m;
-                    w.ev_vx[e] = H.vx;
-                    w.ev_vy[e] = H.vy;
-                    w.ev_vz[e] = H.vz;
-                }
+            if (tid == 0) {
+                w.ev_idx[0] = -1;
+                w.ev_m[0] = H.m;
+                w.ev_vx[0] = H.vx;
+                w.ev_vy[0] = H.vy;
+                w.ev_vz[0] = H.vz;
             }
-            q->n_events = e;
-            q->swallowed = swallowed;
-            b.m[s] = H.m;
-            b.vx[s] = H.vx;
-            b.vy[s] = H.vy;
-            b.vz[s] = H.vz;
-            b.aos[s].spin_x = H.sx;
-            b.aos[s].spin_y = H.sy;
-            b.aos[s].spin_z = H.sz;
+            for (int base = 0; base < n_inner; base += QB) {
+                const int cnt = min(QB, n_inner - base);
+                const int i = tid < cnt ? w.list[base + tid] : 0;
+                if (tid < cnt) {
+                    sb.x[tid] = b.x[i];
+                    sb.y[tid] = b.y[i];
+                    sb.z[tid] = b.z[i];
+                    sb.vx[tid] = b.vx[i];
+                    sb.vy[tid] = b.vy[i];
+                    sb.vz[tid] = b.vz[i];
+                    sb.ax[tid] = b.ax[i];
+                    sb.ay[tid] = b.ay[i];
+                    sb.az[tid] = b.az[i];
+                    sb.m[tid] = b.m[i];
+                    sb.u[tid] = b.u[i];
+                    sb.h[tid] = b.h[i];
+                    sb.type[tid] = b.type[i];
+                }
+                __syncthreads();
+                if (tid == 0) {
+                    for (int t = 0; t < cnt; t++) {
+                        const double dx = sb.x[t] - hx, dy = sb.y[t] - hy, dz = sb.z[t] - hz;
+                        const double d2 = dx * dx + dy * dy + dz * dz;
+                        bool eaten = d2 < r_sw_sq;
+                        if (!eaten) {
+                            const double r = sqrt_rn(d2);
+                            eaten = settle(sb, c, H, t, dx, dy, dz, r) && r < c.isco_r;
+                        }
+                        if (eaten) {
+                            swallowed += sb.m[t];
+                            swallow(H, sb, t);
+                            e++;
+                            w.ev_idx[e] = w.list[base + t];
+                            w.ev_m[e] = H.m;
+                            w.ev_vx[e] = H.vx;
+                            w.ev_vy[e] = H.vy;
+                            w.ev_vz[e] = H.vz;
+                        }
+                    }
+                }
+                __syncthreads();
+                if (tid < cnt) {
+                    b.vx[i] = sb.vx[tid];
+                    b.vy[i] = sb.vy[tid];
+                    b.vz[i] = sb.vz[tid];
+                    b.ax[i] = sb.ax[tid];
+                    b.ay[i] = sb.ay[tid];
+                    b.az[i] = sb.az[tid];
+                    b.m[i] = sb.m[tid];
+                    b.u[i] = sb.u[tid];
+                    b.h[i] = sb.h[tid];
+                    b.type[i] = sb.type[tid];
+                }
+                __syncthreads(); // the next chunk reuses the staging
+            }
+            if (tid == 0) {
+                q->n_events = e;
+                q->swallowed = swallowed;
+                b.m[s] = H.m;
+                b.vx[s] = H.vx;
+                b.vy[s] = H.vy;
+                b.vz[s] = H.vz;
+                b.aos[s].spin_x = H.sx;
+                b.aos[s].spin_y = H.sy;
+                b.aos[s].spin_z = H.sz;
+            }
         }
         grid.sync();
         // outer candidates, each with the SMBH state at its index

@@ -1,8 +1,9 @@
 // dev_sort.cu — exclusive scan and stable LSD radix sort used by the tree build.
 //
 // Radix sort: 8-bit digits; one kernel counts the digits of every pass, then
-// one single-pass kernel per digit (tiles of 1024 keys below 2M keys, 4096
-// above) finds each tile's offsets by decoupled look-back. Stability inside a
+// one single-pass kernel per digit (tiles of 1024 keys below 2M keys, 2048
+// above) finds each tile's offsets by decoupled look-back and writes the tile
+// out reordered by digit in shared memory (coalesced runs). Stability inside a
 // tile comes from giving each warp a contiguous slice of the tile and ranking
 // equal digits in input order (a lane's peers, the lanes holding the same
 // digit, from nine ballots on the digit's bits); across tiles from the
@@ -19,7 +20,7 @@ constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
 constexpr int SORT_THREADS = 256;
 constexpr int SORT_WARPS = SORT_THREADS / CSG_WARP;
-// Items per lane: 16 (tiles of 4096 keys) for large sorts, 4 (tiles of 1024)
+// Items per lane: 8 (tiles of 2048 keys) for large sorts, 4 (tiles of 1024)
 // below 2M keys, so that a 100k-key sort still spreads over ~100 blocks.
 constexpr int sort_tile(int ipl) { return SORT_WARPS * CSG_WARP * ipl; }
 constexpr int RADIX = 256;
@@ -243,6 +244,14 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_counts(const unsigned lo
 // One pass: keys/values of a tile to their places. counts: this pass's 256
 // digit counts; status / status_next: this pass's and the next pass's status
 // buffers (this pass clears its tile's entries of the next one).
+//
+// The tile's keys stay in registers after one coalesced read. Each key's rank
+// among the equal digits of its warp slice comes from the ballots; per-digit
+// counts give every key its place in the tile sorted by digit (stable: warp
+// slices in order, within a slice input order). The tile is reordered so in
+// shared memory, then written out in tile order, so consecutive threads write
+// consecutive slots of one digit's run: coalesced stores instead of up to 32
+// scattered ones per warp instruction.
 template <int IPL>
 __global__ void __launch_bounds__(SORT_THREADS) k_radix_onesweep(
     const unsigned long long *__restrict__ key_in, const int *__restrict__ val_in,
@@ -251,12 +260,17 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_onesweep(
     unsigned long long *status, unsigned long long *__restrict__ status_next, int nblocks,
     const int *__restrict__ n_dev, DevScalars *sc, int wait_polls)
 {
+    constexpr int TILE = sort_tile(IPL);
     if (n_dev) { // key count known on the device only: the grid covers the bound
         n = max(0, min(n, *n_dev));
-        nblocks = (n + sort_tile(IPL) - 1) / sort_tile(IPL);
+        nblocks = (n + TILE - 1) / TILE;
     }
     static_assert(SORT_THREADS == RADIX, "one digit per thread");
-    __shared__ int wcount[SORT_WARPS][RADIX];
+    __shared__ unsigned long long s_key[TILE];
+    __shared__ int s_val[TILE];
+    __shared__ int wcount[SORT_WARPS][RADIX]; // a warp's digit counts, then its offsets
+    __shared__ int s_tds[RADIX];              // where each digit's run starts in the tile
+    __shared__ long long s_glob[RADIX];       // ... and in the output
     __shared__ int warp_tot[SORT_WARPS];
     __shared__ int sh_tile;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -269,76 +283,96 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_onesweep(
     if (tile >= nblocks) // only when the live count is below the bound
         return;
     status_next[(size_t)tile * RADIX + threadIdx.x] = 0ull;
-    const long long w0 = (long long)tile * sort_tile(IPL) + (long long)warp * (CSG_WARP * IPL);
+    const long long t0 = (long long)tile * TILE;
+    const long long w0 = t0 + (long long)warp * (CSG_WARP * IPL);
     const unsigned lt = (1u << lane) - 1u;
-    // per-warp digit counts
+    unsigned long long k[IPL];
+    int v[IPL], rank[IPL];
+#pragma unroll
     for (int c = 0; c < IPL; c++) {
-        long long i = w0 + c * CSG_WARP + lane;
-        int dg = (i < n) ? (int)((key_in[i] >> shift) & (RADIX - 1)) : RADIX;
-        unsigned peers = same_digit_lanes((unsigned)dg);
+        const long long i = w0 + c * CSG_WARP + lane;
+        const bool ok = i < n;
+        k[c] = ok ? key_in[i] : 0ull;
+        v[c] = ok ? val_in[i] : 0;
+        const int dg = ok ? (int)((k[c] >> shift) & (RADIX - 1)) : RADIX;
+        const unsigned peers = same_digit_lanes((unsigned)dg);
+        rank[c] = (dg < RADIX ? wcount[warp][dg] : 0) + __popc(peers & lt);
+        __syncwarp();
         if (dg < RADIX && (peers & lt) == 0)
             wcount[warp][dg] += __popc(peers);
         __syncwarp();
     }
     __syncthreads();
+    // per digit (one thread each): the warps' offsets inside the digit's run
     const int dg = threadIdx.x;
     int tot = 0;
-    for (int w = 0; w < SORT_WARPS; w++)
-        tot += wcount[w][dg];
+    for (int w = 0; w < SORT_WARPS; w++) {
+        const int cw = wcount[w][dg];
+        wcount[w][dg] = tot;
+        tot += cw;
+    }
     unsigned long long *mine = status + (size_t)tile * RADIX + dg;
     lb_store(mine, (tile == 0 ? LB_PRE : LB_AGG) | (unsigned long long)tot);
-    // global exclusive offset of the digit: block scan of the pass's counts
+    // global exclusive offset of the digit (block scan of the pass's counts)
+    // and the digit's start inside the tile (block scan of the tile's counts)
     const int c = (int)counts[dg];
     const int incl = warp_incl_scan(c);
+    const int tincl = warp_incl_scan(tot);
     if (lane == 31)
         warp_tot[warp] = incl;
     __syncthreads();
     int gex = incl - c;
     for (int w = 0; w < warp; w++)
         gex += warp_tot[w];
+    __syncthreads();
+    if (lane == 31)
+        warp_tot[warp] = tincl;
+    __syncthreads();
+    int tds = tincl - tot;
+    for (int w = 0; w < warp; w++)
+        tds += warp_tot[w];
     // keys of this digit in earlier tiles
     long long excl = 0;
     if (tile > 0) {
         for (int j = tile - 1; j >= 0; j--) {
-            const unsigned long long v = lb_wait(status + (size_t)j * RADIX + dg, wait_polls, sc);
-            if (!v) // gave up (recorded): leave the wait
+            const unsigned long long vv = lb_wait(status + (size_t)j * RADIX + dg, wait_polls, sc);
+            if (!vv) // gave up (recorded): leave the wait
                 break;
-            excl += (long long)(v & LB_VAL);
-            if (v & LB_PRE)
+            excl += (long long)(vv & LB_VAL);
+            if (vv & LB_PRE)
                 break;
         }
         lb_store(mine, LB_PRE | (unsigned long long)(excl + tot));
     }
-    int run = gex + (int)excl;
-    for (int w = 0; w < SORT_WARPS; w++) {
-        const int cw = wcount[w][dg];
-        wcount[w][dg] = run;
-        run += cw;
+    s_tds[dg] = tds;
+    s_glob[dg] = (long long)gex + excl;
+    __syncthreads();
+    // the tile sorted by digit, in shared memory
+#pragma unroll
+    for (int cc = 0; cc < IPL; cc++) {
+        const long long i = w0 + cc * CSG_WARP + lane;
+        if (i < n) {
+            const int d = (int)((k[cc] >> shift) & (RADIX - 1));
+            const int lp = s_tds[d] + wcount[warp][d] + rank[cc];
+            s_key[lp] = k[cc];
+            s_val[lp] = v[cc];
+        }
     }
     __syncthreads();
-    // stable placement in input order
+    // written out in tile order: runs of one digit land on consecutive slots
+    const int count = (int)min((long long)TILE, (long long)n - t0);
+#pragma unroll
     for (int cc = 0; cc < IPL; cc++) {
-        long long i = w0 + cc * CSG_WARP + lane;
-        unsigned long long k = 0;
-        int v = 0;
-        int d = RADIX;
-        if (i < n) {
-            k = key_in[i];
-            v = val_in[i];
-            d = (int)((k >> shift) & (RADIX - 1));
-        }
-        unsigned peers = same_digit_lanes((unsigned)d);
-        if (d < RADIX) {
-            const int pos = wcount[warp][d] + __popc(peers & lt);
+        const int j = threadIdx.x + cc * SORT_THREADS;
+        if (j < count) {
+            const unsigned long long kk = s_key[j];
+            const int d = (int)((kk >> shift) & (RADIX - 1));
+            const long long pos = s_glob[d] + (j - s_tds[d]);
             if (pos >= 0 && pos < n) {
-                key_out[pos] = k;
-                val_out[pos] = v;
+                key_out[pos] = kk;
+                val_out[pos] = s_val[j];
             }
         }
-        __syncwarp();
-        if (d < RADIX && (peers & lt) == 0)
-            wcount[warp][d] += __popc(peers);
-        __syncwarp();
     }
 }
 
@@ -423,7 +457,7 @@ int csg_radix_sort(csgd_t *d, unsigned long long *key, int *val, unsigned long l
     if (n <= 1)
         return CSG_OK;
     const bool small = n < (2 << 20);
-    const int tile = small ? sort_tile(4) : sort_tile(16);
+    const int tile = small ? sort_tile(4) : sort_tile(8);
     const int nblocks = (n + tile - 1) / tile;
     const size_t status_words = (size_t)RADIX * nblocks; // 64-bit words per buffer
     const int passes = (bits + 7) / 8;
@@ -452,7 +486,7 @@ int csg_radix_sort(csgd_t *d, unsigned long long *key, int *val, unsigned long l
         if (small)
             { k_radix_onesweep<4><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, n_dev, d->sc, CSG_WAIT_POLLS_DEFAULT); d->launches++; }
         else
-            { k_radix_onesweep<16><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, n_dev, d->sc, CSG_WAIT_POLLS_DEFAULT); d->launches++; }
+            { k_radix_onesweep<8><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, n_dev, d->sc, CSG_WAIT_POLLS_DEFAULT); d->launches++; }
         unsigned long long *tk = ki;
         ki = ko;
         ko = tk;

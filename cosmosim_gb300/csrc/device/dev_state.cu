@@ -9,6 +9,7 @@
 
 #include <nvtx3/nvToolsExt.h>
 
+#include <stddef.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -67,7 +68,11 @@ __global__ void k_pack(Body *__restrict__ b, int n, const double *x, const doubl
     q.internal_energy = u[i];
     q.smoothing_h = h[i];
     q.mass = m[i];
-    q.type = (BodyType)type[i];
+    // type and the 4 padding bytes after it as one 8-byte word: the padding
+    // leaves the device as zeros instead of whatever a wider store would put
+    // there (offset 80 of a 168-byte record: 8-byte aligned)
+    static_assert(offsetof(Body, type) == 80 && sizeof(Body) % 8 == 0, "Body layout");
+    *reinterpret_cast<int2 *>(&q.type) = make_int2(type[i], 0);
 }
 
 // Half kick and drift, src/integrator.c:22-31.
@@ -489,10 +494,10 @@ extern "C" int csgd_reserve(csgd_t *d, int n)
     ok &= dalloc(&d->ext, 3 * cap) == cudaSuccess;
     // radix sort scratch: digit counts and tile counters (8 * 256 + 64 words),
     // then two status buffers of 256 64-bit words per tile; tiles of 1024 keys
-    // below 2M keys, else 4096 (sized for any key count up to ncap)
+    // below 2M keys, else 2048 (sized for any key count up to ncap)
     const size_t sort_items = ncap;
     const size_t small_items = sort_items < (2u << 20) ? sort_items : (2u << 20) - 1;
-    const size_t tiles_small = (small_items + 1023) / 1024, tiles_large = (sort_items + 4095) / 4096;
+    const size_t tiles_small = (small_items + 1023) / 1024, tiles_large = (sort_items + 2047) / 2048;
     const size_t hist = 256 * (tiles_small > tiles_large ? tiles_small : tiles_large);
     d->sort_hist_cap = (int)(4 * hist + 8 * 256 + 64);
     ok &= dalloc(&d->sort_hist, (size_t)d->sort_hist_cap) == cudaSuccess;

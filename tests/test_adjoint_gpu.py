@@ -84,3 +84,26 @@ def test_tree_adjoint_close_to_direct_sum_adjoint():
     t.close()
     d.close()
     assert np.linalg.norm(a - b) / np.linalg.norm(b) < 0.05
+
+
+def test_adjoint_at_the_benchmark_size():
+    """The differentiable-merger configuration itself: 10,000 stars, 200
+    substeps at dt 2e-3, checkpoints every 20. 32 random directions of the
+    initial state and the three orbital parameters against central
+    differences (h = 1e-6) of the frozen-list map, to 1e-4; the Barnes-Hut
+    adjoint against the FP64 direct-sum adjoint of the same run (they differ
+    by the tree's theta = 0.5 approximation, not by the adjoint: cosine)."""
+    pr = MergerProblem()  # n=10000, substeps=200, dt=2e-3, checkpoint_every=20
+    loss, gp, gx, gv = pr.gradients(record=True)
+    gnorm = np.sqrt((gx ** 2).sum() + (gv ** 2).sum())
+    err = floored_errors(pr.fd_directions(gx, gv, k=32, h=1e-6), gnorm)
+    perr = rel_errors(pr.fd_params(gp, h=1e-6))
+    pr.close()
+    assert max(err) <= 1e-4, err
+    assert max(perr) <= 1e-4, perr
+    d = MergerProblem(mode=lib.ADJ_DIRECT)
+    _, _, dx, dv = d.gradients(record=False)
+    d.close()
+    a = np.concatenate([gx.ravel(), gv.ravel()])
+    b = np.concatenate([dx.ravel(), dv.ravel()])
+    assert a @ b / (np.linalg.norm(a) * np.linalg.norm(b)) > 0.95
