@@ -237,6 +237,8 @@ struct csgd {
     DevScalars *sc_host; // pinned mirror
     int *h_int;          // pinned scratch for single values read back (4 ints)
     QuasarState *qs;     // device, allocated by the first quasar step
+    double *wpart;       // FP32 walk units' partial sums, 24 x wpart_cap doubles
+    int wpart_cap;
     void *q_scratch;     // device scratch of the quasar step (dev_quasar.cu)
     int q_scratch_cap;   // bodies it is sized for
     int geometry_valid;
@@ -282,6 +284,17 @@ int csg_scan_exclusive(csgd_t *d, const int *in, int *out, int n, const int *cou
 
 // Polls a bounded device wait makes before it gives up (csgd::wait_polls).
 constexpr int CSG_WAIT_POLLS_DEFAULT = 1 << 22;
+// The FP32 walk splits each task by the root's children when the system has
+// few tasks for the GPU: up to 12 per SM (about 58k bodies on 152 SMs).
+// Above that the whole-task walk already fills the SMs and the split only
+// adds root-level work.
+inline bool csgd_walk_split(const csgd_t *d)
+{
+    return (long long)d->n / 32 + d->n_gal + 1 <= 12LL * d->num_sms;
+}
+// Scratch of the split FP32 walk, allocated on first use outside any capture
+// when `precision` and the size call for it; CSG_OK or CSG_ERR_NOMEM.
+int csgd_prepare_walk(csgd_t *d, int precision);
 inline int csgd_wait_polls(const csgd_t *d)
 {
     return d->wait_polls > 0 ? d->wait_polls : CSG_WAIT_POLLS_DEFAULT;

@@ -391,6 +391,8 @@ extern "C" void csgd_destroy(csgd_t *d)
         cudaFreeHost(d->h_int);
     if (d->qs)
         cudaFree(d->qs);
+    if (d->wpart)
+        cudaFree(d->wpart);
     csgd_quasar_free(d);
     if (d->aux) {
         cudaStreamSynchronize(d->aux);
@@ -773,6 +775,8 @@ extern "C" int csgd_substep(csgd_t *d, double dt, const csgd_force_params *p, in
     int rc = sph ? csgd_prepare_sph(d) : CSG_OK;
     if (!rc && d->export_dst)
         rc = csgd_ensure_tree_extras(d, 1, 1);
+    if (!rc)
+        rc = csgd_prepare_walk(d, p->precision);
     if (rc)
         return rc;
     phase_mark(d, 0);
@@ -836,6 +840,28 @@ extern "C" int csgd_substep(csgd_t *d, double dt, const csgd_force_params *p, in
         cudaStreamWaitEvent(d->stream, d->ev_join2, 0); // always rejoin (a capture needs it)
     phase_mark(d, 6);
     return rc;
+}
+
+int csgd_prepare_walk(csgd_t *d, int precision)
+{
+    if (precision != CSG_PREC_FP32_MIXED || !csgd_walk_split(d) ||
+        (d->wpart && d->wpart_cap >= d->cap))
+        return CSG_OK;
+    csgd_drop_graph(d); // a captured walk holds the old pointer
+    if (d->wpart) {
+        cudaStreamSynchronize(d->stream);
+        cudaFree(d->wpart);
+    }
+    d->wpart = nullptr;
+    d->wpart_cap = 0;
+    const size_t cap = (size_t)(d->cap > 0 ? d->cap : 1);
+    if (csgd_malloc((void **)&d->wpart, sizeof(double) * 3 * 8 * cap) != cudaSuccess) {
+        cudaGetLastError();
+        d->wpart = nullptr;
+        return CSG_ERR_NOMEM;
+    }
+    d->wpart_cap = (int)cap;
+    return CSG_OK;
 }
 
 void csgd_build_mark(csgd_t *d, int k)
@@ -1026,6 +1052,8 @@ static int capture_substep(csgd_t *d, double dt, const csgd_force_params *p, int
     if (sph && csgd_prepare_sph(d))
         return CSG_ERR_NOMEM;
     if (d->export_dst && csgd_ensure_tree_extras(d, 1, 1))
+        return CSG_ERR_NOMEM;
+    if (csgd_prepare_walk(d, p->precision))
         return CSG_ERR_NOMEM;
     // host-side flags a substep resets anyway; start from the same state
     d->gas_valid = 0;

@@ -24,8 +24,11 @@
 //   tree; used by parity tests.
 // FP32-mixed walk: positions and centres as float hi/lo pairs (differences
 //   keep ~48 bits), rsqrt/products in FP32, Kahan-compensated FP32 sums per
-//   body. Openings within the FP32 error band of the threshold are decided in
-//   FP64, so the interaction set equals the FP64 walk's.
+//   body and per child subtree of the root, added in FP64. Openings within the
+//   FP32 error band of the threshold are decided in FP64, so the interaction
+//   set equals the FP64 walk's. Systems with few tasks for the GPU are walked
+//   by eight warps per task, one per root child (k_walk32_units), with the
+//   same bits as one warp per task (k_walk32).
 #include "dev_internal.cuh"
 
 namespace {
@@ -392,23 +395,53 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v)
 // (per-body compensated FP32 summation); G applied once. The step is
 // branch-light: every lane computes the pair term and lanes that do not take
 // the cell add zero, so the warp never splits on "take".
+//
+// Sums are kept per child subtree of the system's root ("segment" k < 8, in
+// the order a lane meets them): the compensated FP32 sum of a segment is
+// closed into a double partial, and the body's acceleration is G times the
+// sum of its partials in child order. A task can so be walked by one warp
+// (all segments in turn) or by eight warps (one segment each, the partials
+// added by k_walk32_sum) with the same bits; the launch picks by size.
+constexpr int WSEGS = 8;
 
+// A lane's body: its FP64 position and the FP32 high and low parts of it.
+struct Lane32 {
+    bool valid;
+    int me;
+    double px, py, pz;
+    float hx, hy, hz, lx, ly, lz;
+};
+
+__device__ __forceinline__ Lane32 lane32(const WalkArgs &a, const TaskRange &tr)
+{
+    Lane32 L;
+    const int lane = threadIdx.x & 31;
+    L.valid = lane < tr.count;
+    L.me = L.valid ? a.perm[tr.pos0 + lane] : -1;
+    L.px = L.valid ? a.x[L.me] : 0.0;
+    L.py = L.valid ? a.y[L.me] : 0.0;
+    L.pz = L.valid ? a.z[L.me] : 0.0;
+    L.hx = (float)L.px;
+    L.hy = (float)L.py;
+    L.hz = (float)L.pz;
+    L.lx = (float)(L.px - (double)L.hx);
+    L.ly = (float)(L.py - (double)L.hy);
+    L.lz = (float)(L.pz - (double)L.hz);
+    return L;
+}
+
+// Cells [cur, nn) in preorder from the lane state `skip` (a lane is active at
+// cells >= skip); adds into the compensated sums (sx, cx) ... in blocks of up
+// to 8 steps. `win` caches 32 consecutive cells from wbase (kept across
+// calls; cells below wend, the system's end). Returns with cur >= nn.
 template <bool STATS, bool EMPTY>
-__device__ __forceinline__ void walk32_task(const WalkArgs &a, NodeW32 *win, const TaskRange &tr,
+__device__ __forceinline__ void walk32_span(const WalkArgs &a, NodeW32 *win, int &cur, int nn,
+                                            int wend, int &skip, int &wbase, const Lane32 &L,
+                                            float &sx,
+                                            float &sy, float &sz, float &cx, float &cy, float &cz,
                                             WalkStats &st)
 {
     const int lane = threadIdx.x & 31;
-    const int nn = tr.end;
-    const bool valid = lane < tr.count;
-    const int me = valid ? a.perm[tr.pos0 + lane] : -1;
-    const double px = valid ? a.x[me] : 0.0, py = valid ? a.y[me] : 0.0,
-                 pz = valid ? a.z[me] : 0.0;
-    const float hx = (float)px, hy = (float)py, hz = (float)pz;
-    const float lx = (float)(px - (double)hx), ly = (float)(py - (double)hy),
-                lz = (float)(pz - (double)hz);
-    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-    int skip = valid ? 0 : INT_MAX;
-    int cur = tr.root, wbase = INT_MIN / 2;
     while (cur < nn) {
         // a block of up to 8 steps: at most one term per lane per step, then
         // one compensated add of the block (warp-uniform)
@@ -420,7 +453,7 @@ __device__ __forceinline__ void walk32_task(const WalkArgs &a, NodeW32 *win, con
             if (cur - wbase >= CSG_WARP) {
                 wbase = cur;
                 __syncwarp();
-                if (wbase + lane < nn)
+                if (wbase + lane < wend)
                     win[lane] = a.w32[wbase + lane];
                 __syncwarp();
             }
@@ -430,14 +463,14 @@ __device__ __forceinline__ void walk32_task(const WalkArgs &a, NodeW32 *win, con
                 st.steps++;
                 st.active += active;
             }
-            const float dx = (c.cx - hx) + (c.lx - lx);
-            const float dy = (c.cy - hy) + (c.ly - ly);
-            const float dz = (c.cz - hz) + (c.lz - lz);
+            const float dx = (c.cx - L.hx) + (c.lx - L.lx);
+            const float dy = (c.cy - L.hy) + (c.ly - L.ly);
+            const float dz = (c.cz - L.hz) + (c.lz - L.lz);
             const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             bool take;
             int nxt;
             if (c.body >= 0) { // leaf (warp-uniform): nothing to open, no vote
-                take = active && c.body != me;
+                take = active && c.body != L.me;
                 if (EMPTY && take && c.m == 0.0f && a.w64[cur].m == 0.0)
                     take = false;
                 nxt = c.next;
@@ -453,7 +486,7 @@ __device__ __forceinline__ void walk32_task(const WalkArgs &a, NodeW32 *win, con
                     acc = c.s2 * a.acc_k < d2; // implies d2 > 0
                     const bool amb = active && !acc && !(c.s2 * a.opn_k > d2);
                     if (amb) // rare
-                        acc = decide64(a, cur, px, py, pz);
+                        acc = decide64(a, cur, L.px, L.py, L.pz);
                     open = active && !acc;
                 }
                 take = active && acc;
@@ -475,17 +508,137 @@ __device__ __forceinline__ void walk32_task(const WalkArgs &a, NodeW32 *win, con
         kahan_add(sy, cy, by);
         kahan_add(sz, cz, bz);
     }
-    if (valid) {
-        a.ax[me] = a.G * ((double)sx - (double)cx);
-        a.ay[me] = a.G * ((double)sy - (double)cy);
-        a.az[me] = a.G * ((double)sz - (double)cz);
+}
+
+// End of the subtree starting at cell c (c < end), kept inside [c + 1, end].
+__device__ __forceinline__ int subtree_end(const WalkArgs &a, int c, int end)
+{
+    return min(end, max(a.w32[c].next, c + 1));
+}
+
+// The whole task by one warp: the root, then each child subtree of the root
+// as a segment, every one closed into the double sum g. Trees built here give
+// the root at most eight children; a caller's pool walked here (never split)
+// may give more, each a segment of its own.
+template <bool STATS, bool EMPTY>
+__device__ __forceinline__ void walk32_task(const WalkArgs &a, NodeW32 *win, const TaskRange &tr,
+                                            WalkStats &st)
+{
+    const int lane = threadIdx.x & 31;
+    // the double sums live in shared memory right after the window
+    // (g[d * 32 + lane]): registers stay with the traversal
+    double *g = reinterpret_cast<double *>(win + CSG_WARP);
+    const Lane32 L = lane32(a, tr);
+    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+    g[lane] = 0.0;
+    g[CSG_WARP + lane] = 0.0;
+    g[2 * CSG_WARP + lane] = 0.0;
+    int skip = L.valid ? 0 : INT_MAX, wbase = INT_MIN / 2, cur = tr.root, nn = tr.root + 1;
+    for (;;) {
+        walk32_span<STATS, EMPTY>(a, win, cur, nn, tr.end, skip, wbase, L, sx, sy, sz, cx, cy, cz,
+                                  st);
+        g[lane] += (double)sx - (double)cx;
+        g[CSG_WARP + lane] += (double)sy - (double)cy;
+        g[2 * CSG_WARP + lane] += (double)sz - (double)cz;
+        sx = sy = sz = cx = cy = cz = 0.f;
+        // after the root, cur < end says that some lane opened it
+        if (cur >= tr.end)
+            break;
+        nn = subtree_end(a, cur, tr.end);
     }
+    if (L.valid) {
+        a.ax[L.me] = a.G * g[lane];
+        a.ay[L.me] = a.G * g[CSG_WARP + lane];
+        a.az[L.me] = a.G * g[2 * CSG_WARP + lane];
+    }
+}
+
+// Segment k < 8 of a task by one warp (a tree built here); its partial into
+// part[k] (3 x pstride), segment 0's with the root's term added first (as the
+// whole walk adds them: 0 + root is the root exactly). The root step runs for
+// every k: it sets which lanes go on. The root's partial waits in shared
+// memory after the window, as in the whole walk.
+template <bool STATS, bool EMPTY>
+__device__ __forceinline__ void walk32_unit(const WalkArgs &a, NodeW32 *win, const TaskRange &tr,
+                                            int k, double *part, long long pstride, WalkStats &st)
+{
+    const int lane = threadIdx.x & 31;
+    double *q = reinterpret_cast<double *>(win + CSG_WARP);
+    const Lane32 L = lane32(a, tr);
+    float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
+    int skip = L.valid ? 0 : INT_MAX, wbase = INT_MIN / 2, cur = tr.root, nn = tr.root + 1;
+    for (bool root = true;; root = false) {
+        walk32_span<STATS, EMPTY>(a, win, cur, nn, tr.end, skip, wbase, L, sx, sy, sz, cx, cy, cz,
+                                  st);
+        if (!root)
+            break;
+        const bool keep = k == 0;
+        q[lane] = keep ? (double)sx - (double)cx : 0.0;
+        q[CSG_WARP + lane] = keep ? (double)sy - (double)cy : 0.0;
+        q[2 * CSG_WARP + lane] = keep ? (double)sz - (double)cz : 0.0;
+        sx = sy = sz = cx = cy = cz = 0.f;
+        for (int j = 0; j < k && cur < tr.end; j++)
+            cur = subtree_end(a, cur, tr.end);
+        if (cur >= tr.end)
+            break;
+        nn = subtree_end(a, cur, tr.end);
+    }
+    if (L.valid) {
+        part[(3 * k + 0) * pstride + L.me] = q[lane] + ((double)sx - (double)cx);
+        part[(3 * k + 1) * pstride + L.me] = q[CSG_WARP + lane] + ((double)sy - (double)cy);
+        part[(3 * k + 2) * pstride + L.me] = q[2 * CSG_WARP + lane] + ((double)sz - (double)cz);
+    }
+}
+
+// a = G (part[0] + ... + part[7]) for every live body, in child order: the
+// whole walk's own sum.
+__global__ void k_walk32_sum(const double *__restrict__ part, long long pstride,
+                             const double *__restrict__ m, int n, double G, double *ax,
+                             double *ay, double *az)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || m[i] <= 0.0)
+        return;
+    double s[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int k = 0; k < WSEGS; k++)
+#pragma unroll
+        for (int d = 0; d < 3; d++)
+            s[d] += part[(3 * k + d) * pstride + i];
+    ax[i] = G * s[0];
+    ay[i] = G * s[1];
+    az[i] = G * s[2];
+}
+
+// One warp per (task, segment): unit u walks segment u % 8 of task u / 8.
+__global__ void __launch_bounds__(4 * CSG_WARP, 8) k_walk32_units(WalkArgs a, double *part,
+                                                                   long long pstride)
+{
+    constexpr int GCELLS = (3 * CSG_WARP * sizeof(double) + sizeof(NodeW32) - 1) / sizeof(NodeW32);
+    __shared__ NodeW32 win_all[4][CSG_WARP + GCELLS];
+    NodeW32 *win = win_all[threadIdx.x >> 5];
+    WalkStats st;
+    const int nn = a.sc->n_nodes;
+    if (nn > a.node_cap || nn < 1)
+        return;
+    const int u = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (u >= a.sc->n_tasks * WSEGS)
+        return;
+    const WalkTask w = a.tasks[u / WSEGS];
+    const DevRoot &r = a.roots[w.gal];
+    const TaskRange tr{w.pos0, w.count, r.root, r.end};
+    if (tr.root < 0 || tr.end > nn || tr.root >= tr.end)
+        dev_fail(a.sc, CSG_ERR_WALK_LIMIT);
+    else
+        walk32_unit<false, false>(a, win, tr, u % WSEGS, part, pstride, st);
 }
 
 template <bool STATS, bool EMPTY, int WARPS, bool PERSIST>
 __global__ void __launch_bounds__(WARPS * CSG_WARP, persist_min_blocks(WARPS, PERSIST)) k_walk32(WalkArgs a)
 {
-    __shared__ NodeW32 win_all[WARPS][CSG_WARP];
+    // per warp: the cell window, then the double sums (3 x 32) right after it
+    constexpr int GCELLS = (3 * CSG_WARP * sizeof(double) + sizeof(NodeW32) - 1) / sizeof(NodeW32);
+    __shared__ NodeW32 win_all[WARPS][CSG_WARP + GCELLS];
     NodeW32 *win = win_all[threadIdx.x >> 5];
     WalkStats st;
     for_each_task<WARPS, PERSIST>(a, [&](const TaskRange &tr) { walk32_task<STATS, EMPTY>(a, win, tr, st); });
@@ -951,6 +1104,15 @@ void launch_walk(csgd_t *d, const WalkArgs &a, int precision, int exact)
             k_walk64_exact<true><<<grid, 8 * CSG_WARP, 0, s>>>(b);
         else
             k_walk64_exact<false><<<grid, 8 * CSG_WARP, 0, s>>>(b);
+    } else if (precision == CSG_PREC_FP32_MIXED && !stats && !empty && csgd_walk_split(d)) {
+        // few tasks for the GPU: eight warps per task, one per root child,
+        // then the partials added in child order (the same bits as below)
+        const long long units = ((long long)d->n / CSG_WARP + d->n_gal + 1) * WSEGS;
+        k_walk32_units<<<(int)((units + 3) / 4), 4 * CSG_WARP, 0, s>>>(b, d->wpart,
+                                                                       (long long)d->wpart_cap);
+        d->launches++;
+        k_walk32_sum<<<csgd_grid(d->n, 256), 256, 0, s>>>(d->wpart, (long long)d->wpart_cap, d->m,
+                                                          d->n, b.G, d->ax, d->ay, d->az);
     } else if (precision == CSG_PREC_FP32_MIXED) {
         if (W == 4)
             CSG_LAUNCH_WALK(k_walk32, 4, grid, s, b);
@@ -997,6 +1159,12 @@ extern "C" int csgd_gravity_ex(csgd_t *d, const csgd_force_params *p, int exact)
     if (exact) // the parity walk keeps one warp per task, 8 warps per block
         a.group = 0;
     cudaStream_t s = d->stream;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone) {
+        const int rc = csgd_prepare_walk(d, p->precision); // a capture prepared it before
+        if (rc)
+            return rc;
+    }
     { k_zero_acc<<<csgd_grid(n, 256), 256, 0, s>>>(d->m, d->ax, d->ay, d->az, n, d->sc); d->launches++; }
     if (exact) {
         const int saved = d->walk_warps;

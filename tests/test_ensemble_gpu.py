@@ -42,7 +42,10 @@ def _make(lib, sizes=SIZES, dead=5):
 @pytest.mark.parametrize("prec,sizes", [(0, SIZES), (1, SIZES),
                                         # 42.5k bodies: the FP64 walk of the ensemble takes the
                                         # two-pairs-per-block layout, each system alone one pair
-                                        (0, [30000, 517, 12000])])
+                                        (0, [30000, 517, 12000]),
+                                        # 74.5k bodies: the FP32 ensemble is walked one warp per
+                                        # task, the small systems alone eight warps per task
+                                        (1, [60000, 2000, 517, 12000])])
 def test_ensemble_equals_separate_handles(lib, prec, sizes):
     parts = _make(lib, sizes)
     allb = _concat(parts)
