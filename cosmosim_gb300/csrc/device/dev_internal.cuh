@@ -190,6 +190,10 @@ struct csgd {
     int gal_cap;
     int *gid, *sgid;
     DevRoot *roots;
+    // bodies per system of an ensemble (device, gal_cap ints) and their
+    // least and largest count; a single system has d->n bodies
+    int *sys_n;
+    int sys_min_n, sys_max_n;
     WalkTask *tasks;
     int task_cap;
     // walk launch shape: warps per block (4 or 8), task group (0 = one warp
@@ -284,15 +288,20 @@ int csg_scan_exclusive(csgd_t *d, const int *in, int *out, int n, const int *cou
 
 // Polls a bounded device wait makes before it gives up (csgd::wait_polls).
 constexpr int CSG_WAIT_POLLS_DEFAULT = 1 << 22;
-// The FP32 walk splits each task by the root's children when the system has
-// few tasks for the GPU: up to 12 per SM (about 58k bodies on 152 SMs).
-// Above that the whole-task walk already fills the SMs and the split only
-// adds root-level work.
+// The walks split each task by the root's children when there are few tasks
+// for the GPU: up to 12 per SM (about 58k bodies on 152 SMs). Above that the
+// whole-task walk already fills the SMs and the split only adds root-level
+// work. The FP32 walk decides per launch (both forms give the same bits); the
+// FP64 walk per system, by its body count (the forms sum differently, and a
+// system must come out the same alone and in an ensemble).
 inline bool csgd_walk_split(const csgd_t *d)
 {
     return (long long)d->n / 32 + d->n_gal + 1 <= 12LL * d->num_sms;
 }
-// Scratch of the split FP32 walk, allocated on first use outside any capture
+inline long long csgd_split_max_bodies(const csgd_t *d) { return 12LL * 32 * d->num_sms; }
+inline int csgd_sys_min_n(const csgd_t *d) { return d->n_gal > 1 ? d->sys_min_n : d->n; }
+inline int csgd_sys_max_n(const csgd_t *d) { return d->n_gal > 1 ? d->sys_max_n : d->n; }
+// Scratch of the split walks, allocated on first use outside any capture
 // when `precision` and the size call for it; CSG_OK or CSG_ERR_NOMEM.
 int csgd_prepare_walk(csgd_t *d, int precision);
 inline int csgd_wait_polls(const csgd_t *d)

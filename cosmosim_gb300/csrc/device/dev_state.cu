@@ -385,6 +385,8 @@ extern "C" void csgd_destroy(csgd_t *d)
         cudaFree(d->sc);
     if (d->roots)
         cudaFree(d->roots);
+    if (d->sys_n)
+        cudaFree(d->sys_n);
     if (d->sc_host)
         cudaFreeHost(d->sc_host);
     if (d->h_int)
@@ -588,25 +590,46 @@ extern "C" int csgd_set_systems(csgd_t *d, int n_sys, const int *host_counts)
         cudaStreamSynchronize(d->stream);
         DevRoot *r = nullptr;
         WalkTask *t = nullptr;
+        int *sn = nullptr;
         const size_t tcap = (size_t)(d->cap > 0 ? d->cap : 1) / CSG_WARP + (size_t)n_sys + 2;
-        if (dalloc(&r, (size_t)n_sys) != cudaSuccess || dalloc(&t, tcap) != cudaSuccess) {
+        if (dalloc(&r, (size_t)n_sys) != cudaSuccess || dalloc(&t, tcap) != cudaSuccess ||
+            dalloc(&sn, (size_t)n_sys) != cudaSuccess) {
             cudaGetLastError();
             if (r)
                 cudaFree(r);
+            if (t)
+                cudaFree(t);
             csgd_set_err(d, CSG_ERR_NOMEM);
             return CSG_ERR_NOMEM;
         }
         cudaFree(d->roots);
         if (d->tasks)
             cudaFree(d->tasks);
+        if (d->sys_n)
+            cudaFree(d->sys_n);
         d->roots = r;
         d->tasks = t;
+        d->sys_n = sn;
         d->gal_cap = n_sys;
         d->task_cap = (int)tcap;
     }
     d->n_gal = n_sys;
     d->geometry_valid = 0;
     d->gas_valid = 0;
+    if (n_sys > 1) {
+        d->sys_min_n = INT_MAX;
+        d->sys_max_n = 0;
+        for (int g = 0; g < n_sys; g++) {
+            d->sys_min_n = host_counts[g] < d->sys_min_n ? host_counts[g] : d->sys_min_n;
+            d->sys_max_n = host_counts[g] > d->sys_max_n ? host_counts[g] : d->sys_max_n;
+        }
+        cudaError_t e = cudaMemcpyAsync(d->sys_n, host_counts, sizeof(int) * (size_t)n_sys,
+                                        cudaMemcpyHostToDevice, d->stream);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(d->stream); // host_counts is the caller's
+        if (e != cudaSuccess)
+            return csgd_check(d, e);
+    }
     if (d->n == 0 || !d->gid)
         return csgd_check(d, cudaGetLastError());
     if (n_sys == 1) {
@@ -844,8 +867,10 @@ extern "C" int csgd_substep(csgd_t *d, double dt, const csgd_force_params *p, in
 
 int csgd_prepare_walk(csgd_t *d, int precision)
 {
-    if (precision != CSG_PREC_FP32_MIXED || !csgd_walk_split(d) ||
-        (d->wpart && d->wpart_cap >= d->cap))
+    const bool split = precision == CSG_PREC_FP32_MIXED ? csgd_walk_split(d)
+                       : precision == CSG_PREC_FP64     ? csgd_sys_min_n(d) <= csgd_split_max_bodies(d)
+                                                        : false;
+    if (!split || (d->wpart && d->wpart_cap >= d->cap))
         return CSG_OK;
     csgd_drop_graph(d); // a captured walk holds the old pointer
     if (d->wpart) {

@@ -14,11 +14,12 @@
 // The next 32 cells in preorder are staged per warp in shared memory with one
 // coalesced load, and re-staged only when the cursor leaves that window.
 //
-// FP64 walk: the drop-in precision (k_walk64ws; k_walk64q for persistent
-//   launch shapes). Openings decided as in the FP32 walk (equal to the
-//   reference's FP64 rounding); interactions queued and evaluated densely in
-//   FP64 — by a second warp per task in k_walk64ws — with 1/r^3 from an FP32
-//   rsqrt seed by integer arithmetic (one rounding). k_walk64_exact instead
+// FP64 walk: the drop-in precision (k_walk64ws). Openings decided as in the
+//   FP32 walk (equal to the reference's FP64 rounding); interactions queued
+//   and evaluated densely in FP64 by a second warp per task, with 1/r^3 from
+//   an FP32 rsqrt seed by integer arithmetic (one rounding), summed per child
+//   subtree of the root as the FP32 walk does; small systems split the same
+//   way (k_walk64ws_units), with the same bits. k_walk64_exact instead
 //   uses the reference's own operation sequence per step (1/(r2*sqrt(r2)),
 //   no fused multiply-add) — bit-identical results on the reference's own
 //   tree; used by parity tests.
@@ -51,6 +52,13 @@ struct WalkArgs {
     int node_cap;
     int group; // 0: one warp per task; g > 0: take g tasks at a time from a counter
     int wait_polls; // producer/consumer waits give up after this many polls
+    double *part;   // split walks: segment partials, part[(3 * k + d) * pstride + body]
+    long long pstride;
+    // FP64: systems of at most split_max bodies are walked split (sys_n[gal]
+    // bodies each in an ensemble, n_bodies for one system); the whole-task
+    // walk leaves them out when skip_small is set
+    const int *sys_n;
+    int n_bodies, split_max, skip_small;
 };
 
 // Work distribution shared by the walks. A task is up to 32 consecutive
@@ -71,15 +79,6 @@ __device__ __forceinline__ int take_tasks(const WalkArgs &a)
 // registers a thread) for one-warp-per-task launches, 24 (up to 85) for
 // persistent ones, whose task loop state would otherwise spill.
 constexpr int persist_min_blocks(int warps, bool persist) { return (persist ? 24 : 32) / warps; }
-// The queued FP64 walk is bound by the FP64 pipe, not by latency: it is sized
-// for fewer resident warps so that its queue state stays in registers.
-#ifndef CSG_W64Q_RESIDENT_WARPS
-#define CSG_W64Q_RESIDENT_WARPS 24
-#endif
-constexpr int w64q_min_blocks(int warps, bool persist)
-{
-    return (persist ? 24 : CSG_W64Q_RESIDENT_WARPS) / warps;
-}
 
 // Walk statistics: interactions, warp steps and lane-steps of lanes that
 // had not finished (lane utilisation = active / (32 steps)).
@@ -315,20 +314,22 @@ __device__ __forceinline__ Cell load_cell(const WalkArgs &a, NodeW32 *win, int &
     return c;
 }
 
-// Visits the preorder tree for the warp's 32 bodies; calls take(cell, dx, dy,
-// dz, d2, cur) (under a warp-uniform "some lane takes" branch) for every cell
-// the lane interacts with, in the reference's depth-first order; after(cur,
-// active) runs once per step for the whole warp. EMPTY: cells of zero mass may occur
-// (caller pools); the reference skips them with everything below.
+// Visits cells [cur, nn) of the preorder tree for the warp's 32 bodies, from
+// the lane state `skip` (a lane is active at cells >= skip); calls take(cell,
+// dx, dy, dz, d2, cur) (under a warp-uniform "some lane takes" branch) for
+// every cell the lane interacts with, in the reference's depth-first order;
+// after(cur, active) runs once per step for the whole warp. `win` caches 32
+// cells from wbase (below wend, the system's end). EMPTY: cells of zero mass
+// may occur (caller pools); the reference skips them with everything below.
+// Returns with cur >= nn (cur = INT_MAX after a malformed tree).
 template <bool EMPTY, typename Take, typename After>
-__device__ __forceinline__ void walk_cells(const WalkArgs &a, NodeW32 *win, int root, int nn,
-                                           int me, bool valid, const BodyPos &b, Take take_fn,
-                                           After after_fn)
+__device__ __forceinline__ void walk_cells_span(const WalkArgs &a, NodeW32 *win, int &cur, int nn,
+                                                int wend, int &skip, int &wbase, int me,
+                                                bool valid, const BodyPos &b, Take take_fn,
+                                                After after_fn)
 {
-    int skip = valid ? 0 : INT_MAX;
-    int cur = root, wbase = INT_MIN / 2;
     while (cur < nn) {
-        const Cell c = load_cell(a, win, wbase, cur, nn);
+        const Cell c = load_cell(a, win, wbase, cur, wend);
         const bool active = cur >= skip;
         bool take = false, open = false;
         if (EMPTY && c.A.w == 0.0f && __any_sync(0xffffffffu, active)) {
@@ -338,6 +339,7 @@ __device__ __forceinline__ void walk_cells(const WalkArgs &a, NodeW32 *win, int 
                 after_fn(cur, active);
                 if (c.next <= cur) {
                     dev_fail(a.sc, CSG_ERR_WALK_LIMIT);
+                    cur = INT_MAX;
                     break;
                 }
                 cur = c.next;
@@ -355,6 +357,7 @@ __device__ __forceinline__ void walk_cells(const WalkArgs &a, NodeW32 *win, int 
             after_fn(cur, active);
             if (c.next <= cur) {
                 dev_fail(a.sc, CSG_ERR_WALK_LIMIT);
+                cur = INT_MAX;
                 break;
             }
             cur = c.next;
@@ -375,9 +378,46 @@ __device__ __forceinline__ void walk_cells(const WalkArgs &a, NodeW32 *win, int 
         const int nxt = __any_sync(0xffffffffu, open) ? cur + 1 : c.next;
         if (nxt <= cur) { // a malformed tree must not loop
             dev_fail(a.sc, CSG_ERR_WALK_LIMIT);
+            cur = INT_MAX;
             break;
         }
         cur = nxt;
+    }
+}
+
+// The whole preorder range [root, nn) of a system.
+template <bool EMPTY, typename Take, typename After>
+__device__ __forceinline__ void walk_cells(const WalkArgs &a, NodeW32 *win, int root, int nn,
+                                           int me, bool valid, const BodyPos &b, Take take_fn,
+                                           After after_fn)
+{
+    int skip = valid ? 0 : INT_MAX, cur = root, wbase = INT_MIN / 2;
+    walk_cells_span<EMPTY>(a, win, cur, nn, nn, skip, wbase, me, valid, b, take_fn, after_fn);
+}
+
+// Segments [k0, k0 + g) of a system for the split walks (a tree built here;
+// segment k is the subtree of the root's child k, the last, k == 7, running
+// to the system's end): the root step (take reports root interactions only
+// for k0 == 0: every unit needs the step to know which lanes go on), then the
+// segments in order, between(k) before segment k > k0.
+template <bool EMPTY, typename Take, typename After, typename Between>
+__device__ __forceinline__ void walk_cells_segments(const WalkArgs &a, NodeW32 *win,
+                                                    const TaskRange &tr, int k0, int g, int me,
+                                                    bool valid, const BodyPos &b, Take take_fn,
+                                                    After after_fn, Between between)
+{
+    int skip = valid ? 0 : INT_MAX, cur = tr.root, wbase = INT_MIN / 2;
+    walk_cells_span<EMPTY>(a, win, cur, tr.root + 1, tr.end, skip, wbase, me, valid, b, take_fn,
+                           after_fn);
+    // cur < end: some lane opened the root
+    for (int j = 0; j < k0 && cur < tr.end; j++)
+        cur = min(tr.end, max(a.w32[cur].next, cur + 1));
+    for (int k = k0; k < k0 + g && cur < tr.end; k++) {
+        if (k > k0)
+            between(k);
+        const int nn = k == 7 ? tr.end : min(tr.end, max(a.w32[cur].next, cur + 1));
+        walk_cells_span<EMPTY>(a, win, cur, nn, tr.end, skip, wbase, me, valid, b, take_fn,
+                               after_fn);
     }
 }
 
@@ -401,7 +441,7 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v)
 // closed into a double partial, and the body's acceleration is G times the
 // sum of its partials in child order. A task can so be walked by one warp
 // (all segments in turn) or by eight warps (one segment each, the partials
-// added by k_walk32_sum) with the same bits; the launch picks by size.
+// added by k_walk_sum) with the same bits; the launch picks by size.
 constexpr int WSEGS = 8;
 
 // A lane's body: its FP64 position and the FP32 high and low parts of it.
@@ -592,7 +632,7 @@ __device__ __forceinline__ void walk32_unit(const WalkArgs &a, NodeW32 *win, con
 
 // a = G (part[0] + ... + part[7]) for every live body, in child order: the
 // whole walk's own sum.
-__global__ void k_walk32_sum(const double *__restrict__ part, long long pstride,
+__global__ void k_walk_sum(const double *__restrict__ part, long long pstride,
                              const double *__restrict__ m, int n, double G, double *ax,
                              double *ay, double *az)
 {
@@ -646,31 +686,30 @@ __global__ void __launch_bounds__(WARPS * CSG_WARP, persist_min_blocks(WARPS, PE
         add_hits(a, st);
 }
 
-// FP64 walk with dense evaluation. The traversal is walk_cells (decisions
-// equal the FP64 reference's); accepted cells are pushed into per-lane FIFO
-// queues in shared memory and evaluated in FP64 in batches where every lane
-// has work, in the order they were accepted (the reference's depth-first
-// order). The FP64 pipe then does useful work on (almost) every lane instead
-// of once per traversal step for the few lanes that interact at that step.
-// Queue slots per lane (a power of two): 64 for 4-warp blocks, 32 for 8-warp
-// blocks (static shared memory stays below 48 KB). Deeper queues make the
-// overflow drains, which leave lanes idle, rarer. The evaluation order (FIFO)
-// and so the results do not depend on the depth.
-constexpr int q64_slots(int warps) { return warps == 4 ? 64 : 32; }
-constexpr int F64 = 8; // entries per lane per dense batch
+// FP64 evaluation: accepted cells are queued per lane in shared memory and
+// evaluated in FP64 in batches where every lane has work, in the order they
+// were accepted (the reference's depth-first order). The FP64 pipe then does
+// useful work on (almost) every lane instead of once per traversal step for
+// the few lanes that interact at that step.
 
 // Loads queued entry s of the lane (its cell's centre of mass and mass), or
-// zeros when s >= count (no queue read, no cell read).
-template <int Q64>
+// zeros when s >= count (no queue read, no cell read). With MARK a negative
+// entry is a segment marker (mk; nothing loaded).
+template <int Q64, bool MARK>
 __device__ __forceinline__ void q64_load(const WalkArgs &a, const int *q, int lane, int head, int s,
-                                         int count, double2 &p01, double2 &p23)
+                                         int count, double2 &p01, double2 &p23, bool &mk)
 {
     p01 = make_double2(0.0, 0.0);
     p23 = p01;
+    mk = false;
     if (s < count) {
         const int c = q[((head + s) & (Q64 - 1)) * CSG_WARP + lane];
-        p01 = __ldg((const double2 *)&a.w64[c]);     // cx, cy
-        p23 = __ldg((const double2 *)&a.w64[c] + 1); // cz, m
+        if (MARK)
+            mk = c < 0;
+        if (!MARK || !mk) {
+            p01 = __ldg((const double2 *)&a.w64[c]);     // cx, cy
+            p23 = __ldg((const double2 *)&a.w64[c] + 1); // cz, m
+        }
     }
 }
 
@@ -686,114 +725,74 @@ __device__ __forceinline__ void q64_term(const WalkArgs &a, const double2 &p01, 
     sz = fma(f, dz, sz);
 }
 
-// Evaluates the lane's next `count` queued cells (count >= 0; lanes without a
-// body pass 0 and never read their queue), two at a time in queue order. With
-// PREFETCH the next two cells' loads are in flight while the current two are
-// evaluated (the producer/consumer walk: few consumer warps per SM at small
-// N, each waiting on its loads); without, each pair is loaded and then
-// evaluated (the queued walk, whose registers are tighter). The sums are the
-// same either way.
-template <int Q64, bool PREFETCH = false>
+// A unit's segment partials: part[(3 * k + d) * pstride + body].
+__device__ __forceinline__ void put_partial(const WalkArgs &a, int k, int me, double sx, double sy,
+                                            double sz)
+{
+    a.part[(3 * k + 0) * a.pstride + me] = sx;
+    a.part[(3 * k + 1) * a.pstride + me] = sy;
+    a.part[(3 * k + 2) * a.pstride + me] = sz;
+}
+
+// Evaluates the lane's next `count` queued entries (count >= 0; lanes without
+// a body pass 0 and never read their queue), two at a time in queue order.
+// The next two cells' loads are in flight while the current two are
+// evaluated (few consumer warps per SM at small N, each waiting on its
+// loads). MARK: a marker closes segment kc (its partial written, the sum
+// restarted).
+template <int Q64, bool MARK>
 __device__ __forceinline__ void q64_eval(const WalkArgs &a, const int *q, int lane, int &head,
                                          int count, double px, double py, double pz,
-                                         double &sx, double &sy, double &sz)
+                                         double &sx, double &sy, double &sz, int me, int &kc)
 {
     count = max(count, 0);
     const int kmax = (int)__reduce_max_sync(0xffffffffu, (unsigned)count);
     double2 a01, a23, b01, b23;
-    if (PREFETCH) {
-        q64_load<Q64>(a, q, lane, head, 0, count, a01, a23);
-        q64_load<Q64>(a, q, lane, head, 1, count, b01, b23);
-    }
+    bool ma, mb;
+    q64_load<Q64, MARK>(a, q, lane, head, 0, count, a01, a23, ma);
+    q64_load<Q64, MARK>(a, q, lane, head, 1, count, b01, b23, mb);
     for (int s = 0; s < kmax; s += 2) {
         double2 c01, c23, d01, d23;
-        if (PREFETCH) {
-            q64_load<Q64>(a, q, lane, head, s + 2, count, c01, c23);
-            q64_load<Q64>(a, q, lane, head, s + 3, count, d01, d23);
-        } else {
-            q64_load<Q64>(a, q, lane, head, s, count, a01, a23);
-            q64_load<Q64>(a, q, lane, head, s + 1, count, b01, b23);
+        bool mc, md;
+        q64_load<Q64, MARK>(a, q, lane, head, s + 2, count, c01, c23, mc);
+        q64_load<Q64, MARK>(a, q, lane, head, s + 3, count, d01, d23, md);
+        if (s < count) {
+            if (MARK && ma) { // rare
+                put_partial(a, kc++, me, sx, sy, sz);
+                sx = sy = sz = 0.0;
+            } else {
+                q64_term(a, a01, a23, px, py, pz, sx, sy, sz);
+            }
         }
-        if (s < count)
-            q64_term(a, a01, a23, px, py, pz, sx, sy, sz);
-        if (s + 1 < count)
-            q64_term(a, b01, b23, px, py, pz, sx, sy, sz);
-        if (PREFETCH) {
-            a01 = c01;
-            a23 = c23;
-            b01 = d01;
-            b23 = d23;
+        if (s + 1 < count) {
+            if (MARK && mb) {
+                put_partial(a, kc++, me, sx, sy, sz);
+                sx = sy = sz = 0.0;
+            } else {
+                q64_term(a, b01, b23, px, py, pz, sx, sy, sz);
+            }
         }
+        a01 = c01;
+        a23 = c23;
+        b01 = d01;
+        b23 = d23;
+        ma = mc;
+        mb = md;
     }
     head += count;
-}
-
-template <bool STATS, bool EMPTY, int Q64>
-__device__ __forceinline__ void walk64q_task(const WalkArgs &a, NodeW32 *win, int *q,
-                                             const TaskRange &tr, WalkStats &st)
-{
-    const int lane = threadIdx.x & 31;
-    const bool valid = lane < tr.count;
-    const int me = valid ? a.perm[tr.pos0 + lane] : -1;
-    const BodyPos b = body_pos(a, me, valid);
-    double sx = 0.0, sy = 0.0, sz = 0.0;
-    int head = 0, tail = 0;
-    walk_cells<EMPTY>(a, win, tr.root, tr.end, me, valid, b,
-        [&](bool take, const Cell &, float, float, float, float, int cur) {
-            if (take) {
-                q[(tail & (Q64 - 1)) * CSG_WARP + lane] = cur;
-                tail++;
-                if (STATS)
-                    st.hits++;
-            }
-        },
-        [&](int, bool active) {
-            if (STATS) {
-                st.steps++;
-                st.active += active;
-            }
-            const int cnt = tail - head; // 0..Q64-1; always 0 for a lane without a body
-            const int cmin = (int)__reduce_min_sync(0xffffffffu, (unsigned)(valid ? cnt : INT_MAX));
-            const int cmax = (int)__reduce_max_sync(0xffffffffu, (unsigned)cnt);
-            if (cmin >= F64)
-                q64_eval<Q64>(a, q, lane, head, valid ? F64 : 0, b.px, b.py, b.pz, sx, sy, sz);
-            else if (cmax >= Q64 - 1) // a lane is about to overflow: drain what is there
-                q64_eval<Q64>(a, q, lane, head, min(cnt, F64), b.px, b.py, b.pz, sx, sy, sz);
-        });
-    while (__any_sync(0xffffffffu, tail - head > 0))
-        q64_eval<Q64>(a, q, lane, head, min(tail - head, F64), b.px, b.py, b.pz, sx, sy, sz);
-    if (valid) {
-        a.ax[me] = a.G * sx;
-        a.ay[me] = a.G * sy;
-        a.az[me] = a.G * sz;
-    }
-}
-
-template <bool STATS, bool EMPTY, int WARPS, bool PERSIST>
-__global__ void __launch_bounds__(WARPS * CSG_WARP, w64q_min_blocks(WARPS, PERSIST)) k_walk64q(WalkArgs a)
-{
-    constexpr int Q64 = q64_slots(WARPS);
-    __shared__ int q_all[WARPS][Q64 * CSG_WARP];
-    __shared__ NodeW32 win_all[WARPS][CSG_WARP];
-    const int warp = threadIdx.x >> 5;
-    int *q = q_all[warp];
-    NodeW32 *win = win_all[warp];
-    WalkStats st;
-    for_each_task<WARPS, PERSIST>(a, [&](const TaskRange &tr) { walk64q_task<STATS, EMPTY, Q64>(a, win, q, tr, st); });
-    if (STATS)
-        add_hits(a, st);
 }
 
 // FP64 walk, producer/consumer form. Each task has two warps: the producer
 // walks the tree (walk_cells, the FP32 decisions) and appends each lane's
 // accepted cells to that lane's ring in shared memory; the consumer evaluates
-// the rings in FP64, in the order the cells were accepted, so its sums are
-// the queued walk's bit for bit. The traversal (FP32/ALU pipes) and the
-// evaluation (FP64 pipe) then overlap on every SM instead of alternating in
-// one warp. The warps hand over through per-lane head and tail counters in
-// shared memory; every wait polls with a sleep and gives up after
-// a.wait_polls polls (recording CSG_ERR_DEVICE_WAIT, then both warps leave
-// the task).
+// the rings in FP64, in the order the cells were accepted. The traversal
+// (FP32/ALU pipes) and the evaluation (FP64 pipe) then overlap on every SM
+// instead of alternating in one warp. The warps hand over through per-lane
+// head and tail counters in shared memory; every wait polls with a sleep and
+// gives up after a.wait_polls polls (recording CSG_ERR_DEVICE_WAIT, then both
+// warps leave the task). A pair of the split form (G > 0) walks G segments
+// of a task: the root step, then the subtrees of the root's children k0 ..
+// k0 + G - 1, with a marker (-1) queued on every lane between two segments.
 constexpr int WS_RING = 128;   // ring slots per lane (power of two)
 constexpr int WS_BATCH = 8;    // dense batch the consumer waits for
 constexpr int WS_PUBLISH = 4;  // the producer publishes its tails every few steps
@@ -808,9 +807,9 @@ struct WsShared {
 
 __device__ __forceinline__ int ws_load(const volatile int *p) { return *p; }
 
-template <bool STATS, bool EMPTY>
+template <bool STATS, bool EMPTY, int G>
 __device__ __forceinline__ void ws_produce(const WalkArgs &a, NodeW32 *win, WsShared &sh,
-                                           const TaskRange &tr, WalkStats &st)
+                                           const TaskRange &tr, int k0, WalkStats &st)
 {
     const int lane = threadIdx.x & 31;
     const bool valid = lane < tr.count;
@@ -822,52 +821,67 @@ __device__ __forceinline__ void ws_produce(const WalkArgs &a, NodeW32 *win, WsSh
         __threadfence_block(); // ring entries before the tail
         ((volatile int *)sh.tail)[lane] = tail;
     };
-    walk_cells<EMPTY>(a, win, tr.root, tr.end, me, valid, b,
-        [&](bool take, const Cell &, float, float, float, float, int cur) {
-            // room for one entry on every lane that takes (warp-uniform wait)
-            bool full = take && tail - head_seen >= WS_RING;
-            if (__any_sync(0xffffffffu, full)) {
-                publish();
-                for (int k = 0; k < a.wait_polls; k++) {
-                    head_seen = ws_load(&sh.head[lane]);
-                    full = take && tail - head_seen >= WS_RING;
-                    if (!__any_sync(0xffffffffu, full) || ws_load(&sh.broken))
-                        break;
-                    __nanosleep(64);
+    // one entry on every lane that wants to push: waits (warp-uniform) for room
+    // (a's fields copied out: a closure holding a reference to a would put
+    // the kernel's argument block on the stack)
+    const int wait_polls = a.wait_polls;
+    DevScalars *const sc = a.sc;
+    auto push = [&](bool want, int value) {
+        bool full = want && tail - head_seen >= WS_RING;
+        if (__any_sync(0xffffffffu, full)) {
+            publish();
+            for (int i = 0; i < wait_polls; i++) {
+                head_seen = ws_load(&sh.head[lane]);
+                full = want && tail - head_seen >= WS_RING;
+                if (!__any_sync(0xffffffffu, full) || ws_load(&sh.broken))
+                    break;
+                __nanosleep(64);
+            }
+            __threadfence_block(); // heads read before slots are overwritten
+            if (__any_sync(0xffffffffu, full)) { // gave up (or the consumer did)
+                if (lane == 0) {
+                    dev_fail(sc, CSG_ERR_DEVICE_WAIT);
+                    ((volatile int *)&sh.broken)[0] = 1;
                 }
-                __threadfence_block(); // heads read before slots are overwritten
-                if (__any_sync(0xffffffffu, full)) { // gave up (or the consumer did)
-                    if (lane == 0) {
-                        dev_fail(a.sc, CSG_ERR_DEVICE_WAIT);
-                        ((volatile int *)&sh.broken)[0] = 1;
-                    }
-                    broken = true;
-                }
+                broken = true;
             }
-            if (take && !broken) {
-                sh.ring[(tail & (WS_RING - 1)) * CSG_WARP + lane] = cur;
-                tail++;
-                if (STATS)
-                    st.hits++;
-            }
-        },
-        [&](int, bool active) {
-            if (STATS) {
-                st.steps++;
-                st.active += active;
-            }
-            if (++steps == WS_PUBLISH) {
-                steps = 0;
-                publish();
-            }
-        });
+        }
+        if (want && !broken) {
+            sh.ring[(tail & (WS_RING - 1)) * CSG_WARP + lane] = value;
+            tail++;
+        }
+    };
+    auto take_fn = [&](bool take, const Cell &, float, float, float, float, int cur) {
+        if (G > 0 && k0 != 0 && cur == tr.root) // the root's terms are segment 0's
+            take = false;
+        push(take, cur);
+        if (STATS && take && !broken)
+            st.hits++;
+    };
+    auto after_fn = [&](int, bool active) {
+        if (STATS) {
+            st.steps++;
+            st.active += active;
+        }
+        if (++steps == WS_PUBLISH) {
+            steps = 0;
+            publish();
+        }
+    };
+    if (G > 0)
+        walk_cells_segments<EMPTY>(a, win, tr, k0, G, me, valid, b, take_fn, after_fn,
+                                   [&](int) { push(valid, -1); });
+    else
+        walk_cells<EMPTY>(a, win, tr.root, tr.end, me, valid, b, take_fn, after_fn);
     publish();
     __syncwarp();
     if (lane == 0)
         ((volatile int *)&sh.done)[0] = 1; // after every lane's final tail (fenced above)
 }
 
-__device__ __forceinline__ void ws_consume(const WalkArgs &a, WsShared &sh, const TaskRange &tr)
+template <int G>
+__device__ __forceinline__ void ws_consume(const WalkArgs &a, WsShared &sh, const TaskRange &tr,
+                                           int k0)
 {
     const int lane = threadIdx.x & 31;
     const bool valid = lane < tr.count;
@@ -875,7 +889,7 @@ __device__ __forceinline__ void ws_consume(const WalkArgs &a, WsShared &sh, cons
     const double px = valid ? a.x[me] : 0.0, py = valid ? a.y[me] : 0.0,
                  pz = valid ? a.z[me] : 0.0;
     double sx = 0.0, sy = 0.0, sz = 0.0;
-    int head = 0, polls = 0;
+    int head = 0, polls = 0, kc = k0; // kc: the segment being summed (split form)
     while (true) {
         const bool done = ws_load(&sh.done) != 0; // read before the tails: they are final then
         __threadfence_block();
@@ -890,8 +904,8 @@ __device__ __forceinline__ void ws_consume(const WalkArgs &a, WsShared &sh, cons
         else if (done || amax >= WS_RING - WS_BATCH)
             take = -1; // the rest (done) or relief for a lane whose ring is nearly full
         if (take != 0) {
-            const int k = take > 0 ? (valid ? take : 0) : min(avail, done ? avail : WS_BATCH);
-            q64_eval<WS_RING, true>(a, sh.ring, lane, head, k, px, py, pz, sx, sy, sz);
+            const int n = take > 0 ? (valid ? take : 0) : min(avail, done ? avail : WS_BATCH);
+            q64_eval<WS_RING, (G > 1)>(a, sh.ring, lane, head, n, px, py, pz, sx, sy, sz, me, kc);
             __threadfence_block(); // entries read before the head is published
             ((volatile int *)sh.head)[lane] = head;
             polls = 0;
@@ -910,7 +924,11 @@ __device__ __forceinline__ void ws_consume(const WalkArgs &a, WsShared &sh, cons
         }
         __nanosleep(64);
     }
-    if (valid) {
+    if (valid && G > 0) { // the last segment's partial (segment 0's with the root's term),
+        put_partial(a, kc, me, sx, sy, sz); // zeros for segments the walk did not reach
+        for (int kk = kc + 1; kk < k0 + G; kk++)
+            put_partial(a, kk, me, 0.0, 0.0, 0.0);
+    } else if (valid) {
         a.ax[me] = a.G * sx;
         a.ay[me] = a.G * sy;
         a.az[me] = a.G * sz;
@@ -921,8 +939,10 @@ __device__ __forceinline__ void ws_consume(const WalkArgs &a, WsShared &sh, cons
 // t % PAIRS of block t / PAIRS), 12 pairs per SM either way: one pair for
 // launches of few tasks (finer blocks balance better over the SMs), two
 // otherwise (measured faster from ~100k bodies on).
-template <bool STATS, bool EMPTY, int PAIRS>
-__global__ void __launch_bounds__(2 * PAIRS * CSG_WARP, 24 / (2 * PAIRS)) k_walk64ws(WalkArgs a)
+// One producer/consumer pair per task (G == 0) or per unit of G segments,
+// u = (8 / G) * task + k0 / G (partials into a.part).
+template <bool STATS, bool EMPTY, int PAIRS, int G>
+__device__ __forceinline__ void walk64ws_body(const WalkArgs &a)
 {
     __shared__ WsShared sh_all[PAIRS];
     __shared__ NodeW32 win_all[PAIRS][CSG_WARP];
@@ -931,14 +951,18 @@ __global__ void __launch_bounds__(2 * PAIRS * CSG_WARP, 24 / (2 * PAIRS)) k_walk
     const int nn = a.sc->n_nodes;
     if (nn > a.node_cap || nn < 1)
         return;
-    const int t = blockIdx.x * PAIRS + pair;
+    const int u = blockIdx.x * PAIRS + pair;
+    const int t = G > 0 ? u / (8 / G) : u, k0 = G > 0 ? (u % (8 / G)) * G : 0;
     TaskRange tr{0, 0, 0, 0};
     bool ok = t < a.sc->n_tasks;
     if (ok) {
         const WalkTask w = a.tasks[t];
         const DevRoot &r = a.roots[w.gal];
         tr = TaskRange{w.pos0, w.count, r.root, r.end};
-        if (tr.root < 0 || tr.end > nn || tr.root >= tr.end) {
+        const bool small = (a.sys_n ? a.sys_n[w.gal] : a.n_bodies) <= a.split_max;
+        if (G > 0 ? !small : (small && a.skip_small)) {
+            ok = false; // the other form walks this system
+        } else if (tr.root < 0 || tr.end > nn || tr.root >= tr.end) {
             if ((warp & 1) == 0 && lane == 0)
                 dev_fail(a.sc, CSG_ERR_WALK_LIMIT);
             ok = false;
@@ -957,11 +981,26 @@ __global__ void __launch_bounds__(2 * PAIRS * CSG_WARP, 24 / (2 * PAIRS)) k_walk
         return; // both warps of the pair
     WalkStats st;
     if ((warp & 1) == 0)
-        ws_produce<STATS, EMPTY>(a, win_all[pair], sh, tr, st);
+        ws_produce<STATS, EMPTY, G>(a, win_all[pair], sh, tr, k0, st);
     else
-        ws_consume(a, sh, tr);
+        ws_consume<G>(a, sh, tr, k0);
     if (STATS && (warp & 1) == 0)
         add_hits(a, st);
+}
+
+template <bool STATS, bool EMPTY, int PAIRS>
+__global__ void __launch_bounds__(2 * PAIRS * CSG_WARP, 24 / (2 * PAIRS)) k_walk64ws(WalkArgs a)
+{
+    walk64ws_body<STATS, EMPTY, PAIRS, 0>(a);
+}
+
+// The FP64 walk split by the root's children (trees built here, few tasks
+// for the GPU): partials into a.part, summed by k_walk_sum; the same bits as
+// k_walk64ws.
+template <bool STATS, int PAIRS, int G>
+__global__ void __launch_bounds__(2 * PAIRS * CSG_WARP, 24 / (2 * PAIRS)) k_walk64ws_units(WalkArgs a)
+{
+    walk64ws_body<STATS, false, PAIRS, G>(a);
 }
 
 // Dead bodies get a = 0 (src/octree.c:226-230); alive ones are overwritten by
@@ -1073,9 +1112,6 @@ WalkArgs walk_args(csgd_t *d, const csgd_force_params *p)
             K<false, false, W, false><<<grid, W * CSG_WARP, 0, s>>>(a);                     \
     } while (0)
 
-#ifndef CSG_WALK64_WS
-#define CSG_WALK64_WS 1
-#endif
 
 // One walk launch with the state's launch shape.
 void launch_walk(csgd_t *d, const WalkArgs &a, int precision, int exact)
@@ -1104,21 +1140,71 @@ void launch_walk(csgd_t *d, const WalkArgs &a, int precision, int exact)
             k_walk64_exact<true><<<grid, 8 * CSG_WARP, 0, s>>>(b);
         else
             k_walk64_exact<false><<<grid, 8 * CSG_WARP, 0, s>>>(b);
-    } else if (precision == CSG_PREC_FP32_MIXED && !stats && !empty && csgd_walk_split(d)) {
+    } else if (precision == CSG_PREC_FP32_MIXED && !stats && !empty && csgd_walk_split(d) &&
+               d->wpart && d->wpart_cap >= d->n) {
         // few tasks for the GPU: eight warps per task, one per root child,
         // then the partials added in child order (the same bits as below)
         const long long units = ((long long)d->n / CSG_WARP + d->n_gal + 1) * WSEGS;
         k_walk32_units<<<(int)((units + 3) / 4), 4 * CSG_WARP, 0, s>>>(b, d->wpart,
                                                                        (long long)d->wpart_cap);
         d->launches++;
-        k_walk32_sum<<<csgd_grid(d->n, 256), 256, 0, s>>>(d->wpart, (long long)d->wpart_cap, d->m,
+        k_walk_sum<<<csgd_grid(d->n, 256), 256, 0, s>>>(d->wpart, (long long)d->wpart_cap, d->m,
                                                           d->n, b.G, d->ax, d->ay, d->az);
     } else if (precision == CSG_PREC_FP32_MIXED) {
         if (W == 4)
             CSG_LAUNCH_WALK(k_walk32, 4, grid, s, b);
         else
             CSG_LAUNCH_WALK(k_walk32, 8, grid, s, b);
-    } else if (CSG_WALK64_WS && !persist) {
+    } else { // FP64: producer/consumer pairs (the task group applies to FP32 only)
+        // small systems (split_max bodies or fewer): a pair per (task, root
+        // child), partials added by k_walk_sum; the rest a pair per task
+        // afterwards (it also overwrites what the sum wrote for their bodies)
+        b.sys_n = d->n_gal > 1 ? d->sys_n : nullptr;
+        b.n_bodies = d->n;
+        b.split_max = (int)csgd_split_max_bodies(d);
+        const bool units = !empty && d->wpart && d->wpart_cap >= d->n &&
+                           csgd_sys_min_n(d) <= b.split_max;
+        b.skip_small = units;
+        if (units) {
+            // G segments per pair: one while the units fit about four waves of
+            // pairs (12 per SM), more (with markers between them) for larger launches
+            const long long tasks = (long long)d->n / CSG_WARP + d->n_gal + 1;
+            int g = 1;
+            while (g < WSEGS && tasks * (WSEGS / g) > 4LL * 12 * d->num_sms)
+                g *= 2;
+            const long long nu = tasks * (WSEGS / g);
+            const int pairs = nu > 8LL * d->num_sms ? 2 : 1;
+            const int gw = (int)((nu + pairs - 1) / pairs);
+            b.part = d->wpart;
+            b.pstride = d->wpart_cap;
+#define CSG_U(ST, P, GG) k_walk64ws_units<ST, P, GG><<<gw, 2 * P * CSG_WARP, 0, s>>>(b)
+#define CSG_UG(ST, P)                                                                              \
+    do {                                                                                          \
+        if (g == 1)                                                                               \
+            CSG_U(ST, P, 1);                                                                      \
+        else if (g == 2)                                                                          \
+            CSG_U(ST, P, 2);                                                                      \
+        else if (g == 4)                                                                          \
+            CSG_U(ST, P, 4);                                                                      \
+        else                                                                                      \
+            CSG_U(ST, P, 8);                                                                      \
+    } while (0)
+            if (pairs == 2 && stats)
+                CSG_UG(true, 2);
+            else if (pairs == 2)
+                CSG_UG(false, 2);
+            else if (stats)
+                CSG_UG(true, 1);
+            else
+                CSG_UG(false, 1);
+#undef CSG_UG
+#undef CSG_U
+            k_walk_sum<<<csgd_grid(d->n, 256), 256, 0, s>>>(d->wpart, (long long)d->wpart_cap,
+                                                              d->m, d->n, b.G, d->ax, d->ay, d->az);
+            d->launches += 2;
+            if (csgd_sys_max_n(d) <= b.split_max)
+                return; // every system is small
+        }
         const long long tasks = (long long)d->n / CSG_WARP + d->n_gal + 1; // >= n_tasks
         const int pairs = tasks > 8LL * d->num_sms ? 2 : 1;
         const int gw = (int)((tasks + pairs - 1) / pairs);
@@ -1139,11 +1225,6 @@ void launch_walk(csgd_t *d, const WalkArgs &a, int precision, int exact)
         else
             CSG_WS(false, false);
 #undef CSG_WS
-    } else {
-        if (W == 4)
-            CSG_LAUNCH_WALK(k_walk64q, 4, grid, s, b);
-        else
-            CSG_LAUNCH_WALK(k_walk64q, 8, grid, s, b);
     }
     d->launches++;
 }

@@ -43,6 +43,13 @@ def _make(lib, sizes=SIZES, dead=5):
                                         # 42.5k bodies: the FP64 walk of the ensemble takes the
                                         # two-pairs-per-block layout, each system alone one pair
                                         (0, [30000, 517, 12000]),
+                                        # FP64 with one system above the split size (about 58k
+                                        # bodies on 152 SMs): one launch of each form
+                                        (0, [70000, 2000, 517]),
+                                        # FP64, 121k bodies of small systems: the ensemble's
+                                        # pairs walk eight root children each, the systems alone
+                                        # two or one
+                                        (0, [30000, 29000, 31000, 30500, 700]),
                                         # 74.5k bodies: the FP32 ensemble is walked one warp per
                                         # task, the small systems alone eight warps per task
                                         (1, [60000, 2000, 517, 12000])])
