@@ -79,12 +79,16 @@ WALK32_NOTE = ("20 flop per reference interaction / the walk's time inside the s
 # SM) runs eight warps per task, one per child subtree of the root
 # (k_walk32_units, then k_walk32_sum adds the eight partials): the same bits.
 WALK32_SPLIT_TASKS_PER_SM = 12
+# the same two figures for k_walk32_units from its capture on the 20k disk
+# (profiles/walk_units_disk20k.md: 2.05 MB read, 0 written; issue 48.6% busy)
+WALK32U_DRAM_BYTES_PER_BODY = 2.04672e6 / 20_000
+WALK32U_ISSUE_BUSY = 0.486
 
 
 def walk32_kernel(torch, n_bodies, n_systems=1):
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     if n_bodies // 32 + n_systems + 1 <= WALK32_SPLIT_TASKS_PER_SM * sms:
-        return "k_walk32_units + k_walk32_sum (gravity walk, a warp per root child)", True
+        return "k_walk32_units + k_walk_sum (gravity walk, a warp per root child)", True
     return "k_walk32 (gravity walk)", False
 
 
@@ -919,10 +923,12 @@ def main():
         "roofline": {"bound": "fp32-pipe", "kernel": walk_name,
                      "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak,
-                     "traffic": None if walk_split else WALK32_DRAM_BYTES_PER_BODY * cfg["n"],
-                     "issue_slots_busy_ncu": None if walk_split else WALK32_ISSUE_BUSY,
-                     "note": WALK32_NOTE + ("; this workload takes the split walk, which that "
-                                            "capture does not cover: traffic and issue null"
+                     "traffic": (WALK32U_DRAM_BYTES_PER_BODY if walk_split
+                                 else WALK32_DRAM_BYTES_PER_BODY) * cfg["n"],
+                     "issue_slots_busy_ncu": WALK32U_ISSUE_BUSY if walk_split else WALK32_ISSUE_BUSY,
+                     "note": WALK32_NOTE + ("; this workload takes the split walk: traffic and "
+                                            "issue from the capture of k_walk32_units on the 20k "
+                                            "disk (profiles/walk_units_disk20k.md)"
                                             if walk_split else "")},
         "errors": r["errors"],
         "e2e": {"value": e2e_value, "unit": UNIT, "api": "integrator_step (pinned host Body[])",
