@@ -62,12 +62,12 @@ ENSEMBLE = dict(n_gal=64, n_min=2000, n_max=50000, size_seed=12, theta=0.5, eps=
                 desc="64 independent exp.-disk galaxies, N log-uniform [2000, 50000], one handle")
 FLOP_PER_INTERACTION = 20  # monopole body-cell interaction: 3 sub, 3 fma d2, rsqrt, 3 mul, 3 fma acc
 # DRAM bytes per body of one k_walk32 launch, from the ncu capture of the
-# 100k merger (profiles/k_walk32_merger100k_fp32.md: 10.06 MB read, 0 written
+# 100k merger (profiles/k_walk32_merger100k_fp32.md: 10.07 MB read, 0 written
 # for 100,000 bodies): the first touch of the tree and the bodies; the tree
 # stays in L2 during the walk. Other workloads scale it by the body count.
-WALK32_DRAM_BYTES_PER_BODY = 10.06e6 / 100_000
-# issue slots busy in the same capture (k_walk32, 100k merger): 57.8%
-WALK32_ISSUE_BUSY = 0.578
+WALK32_DRAM_BYTES_PER_BODY = 10.07e6 / 100_000
+# issue slots busy in the same capture (k_walk32, 100k merger): 55.2%
+WALK32_ISSUE_BUSY = 0.552
 WALK32_NOTE = ("20 flop per reference interaction / the walk's time inside the substep (CUDA "
                "events around it, SPH running beside it); peak = FP32 FMA throughput "
                "measured live by csg_measure_fp_peaks (the walk is CUDA-core bound: no dense "
