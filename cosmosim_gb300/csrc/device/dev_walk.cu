@@ -436,12 +436,13 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float v)
 // branch-light: every lane computes the pair term and lanes that do not take
 // the cell add zero, so the warp never splits on "take".
 //
-// Sums are kept per child subtree of the system's root ("segment" k < 8, in
-// the order a lane meets them): the compensated FP32 sum of a segment is
-// closed into a double partial, and the body's acceleration is G times the
-// sum of its partials in child order. A task can so be walked by one warp
-// (all segments in turn) or by eight warps (one segment each, the partials
-// added by k_walk_sum) with the same bits; the launch picks by size.
+// Sums are closed into double partials: first the root's own term, then one
+// per child subtree of the system's root ("segment" k < 8, in child order);
+// the body's acceleration is G times the sum of the partials in that order.
+// A task can so be walked by one warp (all segments in turn) or by eight
+// warps (one segment each; unit 0 also takes the root's term, and 0 + root
+// is the root exactly; the partials added by k_walk_sum) with the same bits.
+// The launch picks by size.
 constexpr int WSEGS = 8;
 
 // A lane's body: its FP64 position and the FP32 high and low parts of it.
