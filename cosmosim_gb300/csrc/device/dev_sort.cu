@@ -170,6 +170,7 @@ __global__ void k_scan_total(int *__restrict__ out, int n, const int *__restrict
 constexpr unsigned long long LB_AGG = 1ull << 62; // tile count published
 constexpr unsigned long long LB_PRE = 1ull << 63; // inclusive prefix published
 constexpr unsigned long long LB_VAL = LB_AGG - 1;
+constexpr int LB_WINDOW = 8; // tiles whose status words a look-back step reads at once
 
 // layout of the sort scratch (32-bit words): digit counts [8][256], tile
 // counters [8], padding to an 8-byte boundary, then two status buffers of
@@ -331,16 +332,32 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_onesweep(
     int tds = tincl - tot;
     for (int w = 0; w < warp; w++)
         tds += warp_tot[w];
-    // keys of this digit in earlier tiles
+    // keys of this digit in earlier tiles: the words of LB_WINDOW tiles back
+    // are read at once (their loads in flight together), then summed nearest
+    // first until a tile with its inclusive prefix; a word not yet published
+    // is waited for alone
     long long excl = 0;
     if (tile > 0) {
-        for (int j = tile - 1; j >= 0; j--) {
-            const unsigned long long vv = lb_wait(status + (size_t)j * RADIX + dg, wait_polls, sc);
-            if (!vv) // gave up (recorded): leave the wait
-                break;
-            excl += (long long)(vv & LB_VAL);
-            if (vv & LB_PRE)
-                break;
+        bool fin = false;
+        for (int j = tile - 1; j >= 0 && !fin; j -= LB_WINDOW) {
+            unsigned long long w[LB_WINDOW];
+#pragma unroll
+            for (int q = 0; q < LB_WINDOW; q++)
+                w[q] = j - q >= 0 ? lb_load(status + (size_t)(j - q) * RADIX + dg) : LB_PRE;
+#pragma unroll
+            for (int q = 0; q < LB_WINDOW; q++) {
+                if (fin)
+                    break;
+                unsigned long long vv = w[q];
+                if (!(vv & (LB_AGG | LB_PRE)))
+                    vv = lb_wait(status + (size_t)(j - q) * RADIX + dg, wait_polls, sc);
+                if (!vv) { // gave up (recorded): leave the wait
+                    fin = true;
+                    break;
+                }
+                excl += (long long)(vv & LB_VAL);
+                fin = (vv & LB_PRE) != 0; // tile 0 always has it: j - q < 0 is never read
+            }
         }
         lb_store(mine, LB_PRE | (unsigned long long)(excl + tot));
     }
