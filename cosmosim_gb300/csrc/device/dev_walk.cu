@@ -633,13 +633,18 @@ __device__ __forceinline__ void walk32_unit(const WalkArgs &a, NodeW32 *win, con
 
 // a = G (part[0] + ... + part[7]) for every live body, in child order: the
 // whole walk's own sum.
+// With sys_n (an ensemble's FP64 walk): only bodies of systems of at most
+// split_max bodies, the ones the split walk covered.
 __global__ void k_walk_sum(const double *__restrict__ part, long long pstride,
                              const double *__restrict__ m, int n, double G, double *ax,
-                             double *ay, double *az)
+                             double *ay, double *az, const int *__restrict__ gid,
+                             const int *__restrict__ sys_n, int split_max)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || m[i] <= 0.0)
         return;
+    if (sys_n && sys_n[gid[i]] > split_max)
+        return; // walked whole, written by that walk
     double s[3] = {0.0, 0.0, 0.0};
 #pragma unroll
     for (int k = 0; k < WSEGS; k++)
@@ -1150,16 +1155,16 @@ void launch_walk(csgd_t *d, const WalkArgs &a, int precision, int exact)
                                                                        (long long)d->wpart_cap);
         d->launches++;
         k_walk_sum<<<csgd_grid(d->n, 256), 256, 0, s>>>(d->wpart, (long long)d->wpart_cap, d->m,
-                                                          d->n, b.G, d->ax, d->ay, d->az);
+                                                          d->n, b.G, d->ax, d->ay, d->az, nullptr,
+                                                          nullptr, 0);
     } else if (precision == CSG_PREC_FP32_MIXED) {
         if (W == 4)
             CSG_LAUNCH_WALK(k_walk32, 4, grid, s, b);
         else
             CSG_LAUNCH_WALK(k_walk32, 8, grid, s, b);
     } else { // FP64: producer/consumer pairs (the task group applies to FP32 only)
-        // small systems (split_max bodies or fewer): a pair per (task, root
-        // child), partials added by k_walk_sum; the rest a pair per task
-        // afterwards (it also overwrites what the sum wrote for their bodies)
+        // small systems (split_max bodies or fewer): pairs per (task, root
+        // children), partials added by k_walk_sum; the rest a pair per task
         b.sys_n = d->n_gal > 1 ? d->sys_n : nullptr;
         b.n_bodies = d->n;
         b.split_max = (int)csgd_split_max_bodies(d);
@@ -1201,7 +1206,8 @@ void launch_walk(csgd_t *d, const WalkArgs &a, int precision, int exact)
 #undef CSG_UG
 #undef CSG_U
             k_walk_sum<<<csgd_grid(d->n, 256), 256, 0, s>>>(d->wpart, (long long)d->wpart_cap,
-                                                              d->m, d->n, b.G, d->ax, d->ay, d->az);
+                                                              d->m, d->n, b.G, d->ax, d->ay, d->az,
+                                                              d->gid, b.sys_n, b.split_max);
             d->launches += 2;
             if (csgd_sys_max_n(d) <= b.split_max)
                 return; // every system is small
