@@ -219,20 +219,13 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_counts(const unsigned lo
     for (int i = threadIdx.x; i < 8 * RADIX; i += blockDim.x)
         (&h[0][0])[i] = 0;
     __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1u;
+    // plain shared-memory atomics: measured faster than aggregating equal
+    // digits of a warp first (the ballots cost more than the collisions)
     const long long stride = (long long)gridDim.x * blockDim.x;
-    // warp-uniform trip count: every lane takes part in the match below
-    for (long long base = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31); base < n;
-         base += stride) {
-        const long long i = base + lane;
-        const unsigned long long k = (i < n) ? key[i] : 0ull;
-        for (int p = 0; p < passes; p++) {
-            const int dg = (i < n) ? (int)((k >> (8 * p)) & (RADIX - 1)) : RADIX;
-            const unsigned peers = same_digit_lanes((unsigned)dg);
-            if (dg < RADIX && (peers & lt) == 0)
-                atomicAdd(&h[p][dg], (unsigned)__popc(peers));
-        }
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const unsigned long long k = key[i];
+        for (int p = 0; p < passes; p++)
+            atomicAdd(&h[p][(int)((k >> (8 * p)) & (RADIX - 1))], 1u);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < passes * RADIX; i += blockDim.x) {
