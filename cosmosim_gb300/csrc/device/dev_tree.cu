@@ -569,9 +569,12 @@ __global__ void k_nodes(csgd_t dd, DevScalars *sc, const DevRoot *__restrict__ r
                         const signed char *__restrict__ lcp, const int *__restrict__ base,
                         const int *__restrict__ perm, int *__restrict__ leaf_of)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    // one thread per cell (and, for positions without a leaf, per position;
+    // grid-stride beyond the grid): the cells of a position are written by as
+    // many threads, so no thread walks the searches of a whole column of levels
+    const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
     const int na = sc->n_alive;
-    if (p == 0) {
+    if (t0 == 0) {
         int total = (na == 0) ? 1 : base[na];
         sc->n_nodes = total;
         if (total > dd.node_cap)
@@ -587,26 +590,43 @@ __global__ void k_nodes(csgd_t dd, DevScalars *sc, const DevRoot *__restrict__ r
             return;
         }
     }
-    if (p >= na)
+    if (na == 0)
         return;
-    const double hs0 = roots[sgid[p]].hs0;
-    const int P = (p > 0) ? (int)lcp[p - 1] : -1;
-    const int Q = (int)lcp[p];
-    int id = base[p];
-    const int Lhi = min(Q, CSG_MAX_LEVEL - 1);
-    for (int L = P + 1; L <= Lhi; L++, id++) {
-        int hi = search_hi(key, ext, sgid, na, p, L);
-        int parent = parent_id(key, ext, sgid, lcp, base, p, P, L, id);
-        write_cell(dd, sc, hs0, id, parent, L, p, hi - p + 1, base[hi + 1], -1);
-    }
-    if (P < CSG_MAX_LEVEL) {
-        int L = min(max(P, Q) + 1, CSG_MAX_LEVEL); // bodies equal to depth 64 share a leaf
-        int hi = (Q == CSG_MAX_LEVEL) ? search_hi(key, ext, sgid, na, p, CSG_MAX_LEVEL) : p;
-        int parent = parent_id(key, ext, sgid, lcp, base, p, P, L, id);
-        write_cell(dd, sc, hs0, id, parent, L, p, hi - p + 1, id + 1, perm[p]);
-        leaf_of[p] = id;
-    } else {
-        leaf_of[p] = -1;
+    const int total = base[na];
+    const int limit = max(total, na);
+    for (int c = t0; c < limit; c += gridDim.x * blockDim.x) {
+        if (c < na && c > 0 && (int)lcp[c - 1] >= CSG_MAX_LEVEL)
+            leaf_of[c] = -1; // bodies equal to depth 64 after the first share its leaf
+        if (c >= total)
+            continue;
+        // the position whose cells include id c: the last p with base[p] <= c
+        int lo = 0, hi = na - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (base[mid] <= c)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const int p = lo;
+        const double hs0 = roots[sgid[p]].hs0;
+        const int P = (p > 0) ? (int)lcp[p - 1] : -1;
+        const int Q = (int)lcp[p];
+        const int j = c - base[p];
+        const int internal = min(Q, CSG_MAX_LEVEL - 1) - P; // levels P+1 .. before the leaf
+        if (j < internal) {
+            const int L = P + 1 + j;
+            const int hi_p = search_hi(key, ext, sgid, na, p, L);
+            const int parent = parent_id(key, ext, sgid, lcp, base, p, P, L, c);
+            write_cell(dd, sc, hs0, c, parent, L, p, hi_p - p + 1, base[hi_p + 1], -1);
+        } else { // the leaf (a position without one has no cell to land here)
+            const int L = min(max(P, Q) + 1, CSG_MAX_LEVEL); // equal to depth 64: one leaf
+            const int hi_p =
+                (Q == CSG_MAX_LEVEL) ? search_hi(key, ext, sgid, na, p, CSG_MAX_LEVEL) : p;
+            const int parent = parent_id(key, ext, sgid, lcp, base, p, P, L, c);
+            write_cell(dd, sc, hs0, c, parent, L, p, hi_p - p + 1, c + 1, perm[p]);
+            leaf_of[p] = c;
+        }
     }
 }
 
@@ -1209,8 +1229,8 @@ extern "C" int csgd_build_tree(csgd_t *d, int geometry)
     if (rc)
         return rc;
     // d->cnt (the counts, consumed by the scan) now holds each position's leaf
-    { k_nodes<<<g, B, 0, s>>>(*d, sc, d->roots, d->key, d->ext, d->sgid, d->lcp, d->base, d->perm, d->cnt); d->launches++; }
-    const int gn = csgd_grid(cell_threads(d), B);
+    const int gn = csgd_grid(cell_threads(d), B); // >= cells and >= positions
+    { k_nodes<<<gn, B, 0, s>>>(*d, sc, d->roots, d->key, d->ext, d->sgid, d->lcp, d->base, d->perm, d->cnt); d->launches++; }
     { k_link<<<gn, B, 0, s>>>(*d, sc, d->key, d->ext); d->launches++; }
     csgd_build_mark(d, 3);
     if (d->export_order)
