@@ -701,9 +701,21 @@ __global__ void k_link(csgd_t dd, DevScalars *sc, const unsigned long long *__re
 
 // Bottom-up moments: one thread per leaf (sorted positions that start one);
 // the last child to finish computes its parent, summing the children in
-// octant order so the result does not depend on scheduling. Only the centre
-// of mass and mass fields are written (write_cell set the rest). EXPORT also
-// keeps the two lowest body indices below each cell (the pool export order).
+// octant order so the result does not depend on scheduling. The climb
+// carries and stores raw sums (sum of m x, sum of m) in the FP64 record, so
+// no division sits on its chain of dependent levels; k_moments_norm then
+// turns every cell's sums into its centre of mass and writes the FP32 record.
+// Only the centre of mass and mass fields are written (write_cell set the
+// rest). EXPORT also keeps the two lowest body indices below each cell (the
+// pool export order).
+__device__ __forceinline__ void put_raw(const csgd_t &dd, int node, double ax, double ay,
+                                        double az, double M)
+{
+    double2 *w = (double2 *)&dd.w64[node];
+    w[0] = make_double2(ax, ay);
+    w[1] = make_double2(az, M);
+}
+
 __device__ __forceinline__ void put_moments(const csgd_t &dd, int node, double sx, double sy,
                                             double sz, double M)
 {
@@ -728,11 +740,11 @@ __device__ __forceinline__ void put_moments(const csgd_t &dd, int node, double s
 constexpr int MOM_DIRECT = 16;
 
 template <bool EXPORT>
-__device__ __forceinline__ void moments_climb(const csgd_t &dd, int node, double sx, double sy,
-                                              double sz, double M, int2 mi)
+__device__ __forceinline__ void moments_climb(const csgd_t &dd, int node, double ax, double ay,
+                                              double az, double M, int2 mi)
 {
     while (true) {
-        put_moments(dd, node, sx, sy, sz, M);
+        put_raw(dd, node, ax, ay, az, M);
         if (EXPORT)
             dd.minidx[node] = mi;
         int parent = dd.link[node].parent;
@@ -744,7 +756,7 @@ __device__ __forceinline__ void moments_climb(const csgd_t &dd, int node, double
             break;
         __threadfence();
         M = 0.0;
-        double ax = 0.0, ay = 0.0, az = 0.0;
+        ax = ay = az = 0.0;
         int m1 = INT_MAX, m2 = INT_MAX;
         const int4 *cp = (const int4 *)(dd.child + 8 * (size_t)parent);
         const int4 c03 = __ldcg(cp), c47 = __ldcg(cp + 1);
@@ -756,9 +768,9 @@ __device__ __forceinline__ void moments_climb(const csgd_t &dd, int node, double
             const double2 *cw = (const double2 *)&dd.w64[c];
             const double2 xy = __ldcg(cw), zm = __ldcg(cw + 1);
             M += zm.y;
-            ax += zm.y * xy.x;
-            ay += zm.y * xy.y;
-            az += zm.y * zm.x;
+            ax += xy.x;
+            ay += xy.y;
+            az += zm.x;
             if (EXPORT) {
                 int2 cmi = __ldcg(&dd.minidx[c]);
                 int cand[2] = {cmi.x, cmi.y};
@@ -773,10 +785,6 @@ __device__ __forceinline__ void moments_climb(const csgd_t &dd, int node, double
                 }
             }
         }
-        const double inv = div_rn(1.0, M); // correctly rounded, off the FP64 pipe
-        sx = ax * inv;
-        sy = ay * inv;
-        sz = az * inv;
         mi = make_int2(m1, m2);
         node = parent;
     }
@@ -793,46 +801,56 @@ __device__ __forceinline__ void moments_cell(const csgd_t &dd, int id, const dou
     const bool leaf = dd.nchild[id] == 0;
     if ((!leaf && l.count > MOM_DIRECT) || l.count < 1)
         return; // formed by the climb (or a cell without bodies)
-    double M, sx, sy, sz;
+    double M = 0.0, ax = 0.0, ay = 0.0, az = 0.0;
     int2 mi = make_int2(INT_MAX, INT_MAX);
-    if (l.count == 1) {
-        const int b = perm[l.first];
-        M = m[b];
-        sx = x[b];
-        sy = y[b];
-        sz = z[b];
-        mi.x = b;
-    } else {
-        M = 0.0;
-        double ax = 0.0, ay = 0.0, az = 0.0;
-        for (int k = 0; k < l.count; k++) {
-            const int b = perm[l.first + k];
-            const double mb = m[b];
-            M += mb;
-            ax += mb * x[b];
-            ay += mb * y[b];
-            az += mb * z[b];
-            if (EXPORT) {
-                if (b < mi.x) {
-                    mi.y = mi.x;
-                    mi.x = b;
-                } else if (b < mi.y) {
-                    mi.y = b;
-                }
+    for (int k = 0; k < l.count; k++) {
+        const int b = perm[l.first + k];
+        const double mb = m[b];
+        M += mb;
+        ax += mb * x[b];
+        ay += mb * y[b];
+        az += mb * z[b];
+        if (EXPORT) {
+            if (b < mi.x) {
+                mi.y = mi.x;
+                mi.x = b;
+            } else if (b < mi.y) {
+                mi.y = b;
             }
         }
-        const double inv = div_rn(1.0, M); // correctly rounded, off the FP64 pipe
-        sx = ax * inv;
-        sy = ay * inv;
-        sz = az * inv;
     }
     if (l.parent >= 0 && dd.link[l.parent].count <= MOM_DIRECT) {
-        put_moments(dd, id, sx, sy, sz, M); // the parent sums its own bodies
+        put_raw(dd, id, ax, ay, az, M); // the parent sums its own bodies
         if (EXPORT)
             dd.minidx[id] = mi;
         return;
     }
-    moments_climb<EXPORT>(dd, id, sx, sy, sz, M, mi);
+    moments_climb<EXPORT>(dd, id, ax, ay, az, M, mi);
+}
+
+// Raw sums to centre of mass, every cell: a single-body leaf keeps the body's
+// position exactly (the reference's leaf centre), any other cell takes
+// (sum m x) / (sum m), the reciprocal correctly rounded off the FP64 pipe.
+__global__ void k_moments_norm(csgd_t dd, DevScalars *sc, const double *__restrict__ x,
+                               const double *__restrict__ y, const double *__restrict__ z)
+{
+    const int nn = sc->n_nodes;
+    if (nn > dd.node_cap || sc->n_alive == 0)
+        return;
+    for (int id = blockIdx.x * blockDim.x + threadIdx.x; id < nn; id += gridDim.x * blockDim.x) {
+        const NodeLink l = dd.link[id];
+        if (l.count < 1)
+            continue;
+        const double2 *w = (const double2 *)&dd.w64[id];
+        const double2 xy = w[0], zm = w[1];
+        const int body = dd.w64[id].body;
+        if (l.count == 1 && body >= 0) {
+            put_moments(dd, id, x[body], y[body], z[body], zm.y);
+        } else {
+            const double inv = div_rn(1.0, zm.y);
+            put_moments(dd, id, xy.x * inv, xy.y * inv, zm.x * inv, zm.y);
+        }
+    }
 }
 
 template <bool EXPORT>
@@ -1237,6 +1255,7 @@ extern "C" int csgd_build_tree(csgd_t *d, int geometry)
         { k_moments<true><<<gn, B, 0, s>>>(*d, sc, d->x, d->y, d->z, d->m, d->perm); d->launches++; }
     else
         { k_moments<false><<<gn, B, 0, s>>>(*d, sc, d->x, d->y, d->z, d->m, d->perm); d->launches++; }
+    { k_moments_norm<<<gn, B, 0, s>>>(*d, sc, d->x, d->y, d->z); d->launches++; }
     d->minidx_valid = d->export_order;
     csgd_build_mark(d, 4);
     { k_tasks<<<min(d->n_gal, 152), 256, 0, s>>>(sc, d->roots, d->n_gal, d->base, d->tasks, d->task_cap, 0); d->launches++; }
