@@ -1,8 +1,8 @@
 // dev_sort.cu — exclusive scan and stable LSD radix sort used by the tree build.
 //
 // Radix sort: 8-bit digits; one kernel counts the digits of every pass, then
-// one single-pass kernel per digit (tiles of 1024 keys below 2M keys, 2048
-// above) finds each tile's offsets by decoupled look-back and writes the tile
+// one single-pass kernel per digit (tiles of 512 keys below 64k keys, 1024
+// below 2M, 2048 above) finds each tile's offsets by decoupled look-back and writes the tile
 // out reordered by digit in shared memory (coalesced runs). Stability inside a
 // tile comes from giving each warp a contiguous slice of the tile and ranking
 // equal digits in input order (a lane's peers, the lanes holding the same
@@ -21,7 +21,8 @@ constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 constexpr int SORT_THREADS = 256;
 constexpr int SORT_WARPS = SORT_THREADS / CSG_WARP;
 // Items per lane: 8 (tiles of 2048 keys) for large sorts, 4 (tiles of 1024)
-// below 2M keys, so that a 100k-key sort still spreads over ~100 blocks.
+// below 2M keys, so that a 100k-key sort still spreads over ~100 blocks, and 2
+// (tiles of 512) below 64k keys.
 constexpr int sort_tile(int ipl) { return SORT_WARPS * CSG_WARP * ipl; }
 constexpr int RADIX = 256;
 
@@ -466,8 +467,8 @@ int csg_radix_sort(csgd_t *d, unsigned long long *key, int *val, unsigned long l
 {
     if (n <= 1)
         return CSG_OK;
-    const bool small = n < (2 << 20);
-    const int tile = small ? sort_tile(4) : sort_tile(8);
+    const bool small = n < (2 << 20), tiny = n < (1 << 16);
+    const int tile = tiny ? sort_tile(2) : small ? sort_tile(4) : sort_tile(8);
     const int nblocks = (n + tile - 1) / tile;
     const size_t status_words = (size_t)RADIX * nblocks; // 64-bit words per buffer
     const int passes = (bits + 7) / 8;
@@ -493,7 +494,9 @@ int csg_radix_sort(csgd_t *d, unsigned long long *key, int *val, unsigned long l
         const int shift = 8 * p;
         unsigned long long *st = status + (size_t)(p & 1) * status_words;
         unsigned long long *st_next = status + (size_t)((p + 1) & 1) * status_words;
-        if (small)
+        if (tiny)
+            { k_radix_onesweep<2><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, n_dev, d->sc, CSG_WAIT_POLLS_DEFAULT); d->launches++; }
+        else if (small)
             { k_radix_onesweep<4><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, n_dev, d->sc, CSG_WAIT_POLLS_DEFAULT); d->launches++; }
         else
             { k_radix_onesweep<8><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, n_dev, d->sc, CSG_WAIT_POLLS_DEFAULT); d->launches++; }

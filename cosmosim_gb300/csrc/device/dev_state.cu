@@ -497,12 +497,17 @@ extern "C" int csgd_reserve(csgd_t *d, int n)
     ok &= dalloc(&d->perm_alt, cap) == cudaSuccess;
     ok &= dalloc(&d->ext, 3 * cap) == cudaSuccess;
     // radix sort scratch: digit counts and tile counters (8 * 256 + 64 words),
-    // then two status buffers of 256 64-bit words per tile; tiles of 1024 keys
-    // below 2M keys, else 2048 (sized for any key count up to ncap)
+    // then two status buffers of 256 64-bit words per tile; tiles of 512 keys
+    // below 64k keys, 1024 below 2M, else 2048 (sized for any key count up to
+    // ncap)
     const size_t sort_items = ncap;
+    const size_t tiny_items = sort_items < (1u << 16) ? sort_items : (1u << 16) - 1;
     const size_t small_items = sort_items < (2u << 20) ? sort_items : (2u << 20) - 1;
+    const size_t tiles_tiny = (tiny_items + 511) / 512;
     const size_t tiles_small = (small_items + 1023) / 1024, tiles_large = (sort_items + 2047) / 2048;
-    const size_t hist = 256 * (tiles_small > tiles_large ? tiles_small : tiles_large);
+    size_t tiles = tiles_small > tiles_large ? tiles_small : tiles_large;
+    tiles = tiles_tiny > tiles ? tiles_tiny : tiles;
+    const size_t hist = 256 * tiles;
     d->sort_hist_cap = (int)(4 * hist + 8 * 256 + 64);
     ok &= dalloc(&d->sort_hist, (size_t)d->sort_hist_cap) == cudaSuccess;
     ok &= dalloc(&d->lcp, cap) == cudaSuccess;
