@@ -245,8 +245,62 @@ __global__ void k_bbox(const double *__restrict__ x, const double *__restrict__ 
             }
         }
     }
-    if (cur_g >= 0)
-        bbox_flush(roots, cur_g, lo, hi, cnt);
+    // the warps' last running boxes: combined in the block first, one set of
+    // atomics per system the block ends on (one per block for a single system)
+    __shared__ unsigned long long s_lo[32][3], s_hi[32][3];
+    __shared__ int s_cnt[32], s_g[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        lo[a] = warp_min_u64(lo[a]);
+        hi[a] = warp_max_u64(hi[a]);
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if (lane == 0) {
+        s_g[warp] = cur_g;
+        s_cnt[warp] = cnt;
+        for (int a = 0; a < 3; a++) {
+            s_lo[warp][a] = lo[a];
+            s_hi[warp][a] = hi[a];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int g = -1, c = 0;
+        unsigned long long l[3] = {~0ull, ~0ull, ~0ull}, h[3] = {0ull, 0ull, 0ull};
+        const int nw = (int)(blockDim.x >> 5);
+        for (int w = 0; w <= nw; w++) {
+            const int gw = w < nw ? s_g[w] : -1;
+            if (w == nw || (gw >= 0 && gw != g)) {
+                if (g >= 0) { // flush the system collected so far
+                    for (int a = 0; a < 3; a++) {
+                        if (l[a] != ~0ull)
+                            atomicMin(&roots[g].omin[a], l[a]);
+                        if (h[a] != 0ull)
+                            atomicMax(&roots[g].omax[a], h[a]);
+                    }
+                    if (c)
+                        atomicAdd(&roots[g].n_alive, c);
+                }
+                if (w == nw)
+                    break;
+                g = gw;
+                c = 0;
+                for (int a = 0; a < 3; a++) {
+                    l[a] = ~0ull;
+                    h[a] = 0ull;
+                }
+            }
+            if (gw < 0)
+                continue;
+            c += s_cnt[w];
+            for (int a = 0; a < 3; a++) {
+                l[a] = s_lo[w][a] < l[a] ? s_lo[w][a] : l[a];
+                h[a] = s_hi[w][a] > h[a] ? s_hi[w][a] : h[a];
+            }
+        }
+    }
     if (bad)
         dev_fail(gsc, CSG_ERR_BAD_ARG);
 }
