@@ -77,7 +77,7 @@ WALK32_NOTE = ("20 flop per reference interaction / the walk's time inside the s
                "(profiles/), traffic scaled by the body count")
 # The FP32 walk of a system with few 32-body tasks for the GPU (at most 12 per
 # SM) runs eight warps per task, one per child subtree of the root
-# (k_walk32_units, then k_walk32_sum adds the eight partials): the same bits.
+# (k_walk32_units, then k_walk_sum adds the eight partials): the same bits.
 WALK32_SPLIT_TASKS_PER_SM = 12
 # the same two figures for k_walk32_units from its capture on the 20k disk
 # (profiles/walk_units_disk20k.md: 2.05 MB read, 0 written; issue 48.6% busy)

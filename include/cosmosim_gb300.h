@@ -50,8 +50,10 @@ extern "C" {
                       time from a device counter until none are left
      blocks_per_sm    persistent launch only: blocks per SM (1..32)
      ms               filled by the autotuner: median walk time, ms
-   Results do not depend on the shape (each body's sum is formed by one lane
-   in the reference's order); only the time does. */
+   The shape applies to the FP32-mixed walk; the FP64 walk always runs one
+   producer/consumer warp pair per task (or, for systems of up to 12 x 32
+   bodies per SM, pairs per child subtree of the root). Results do not depend
+   on the shape; only the time does. */
 typedef struct {
     int warps_per_block;
     int task_group;
