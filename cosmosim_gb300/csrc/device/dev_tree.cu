@@ -753,8 +753,8 @@ __global__ void k_link(csgd_t dd, DevScalars *sc, const unsigned long long *__re
     }
 }
 
-// Bottom-up moments: one thread per leaf (sorted positions that start one);
-// the last child to finish computes its parent, summing the children in
+// Bottom-up moments: one thread per cell of at most MOM_DIRECT bodies (and
+// per leaf); above those, the last child to finish computes its parent, summing the children in
 // octant order so the result does not depend on scheduling. The climb
 // carries and stores raw sums (sum of m x, sum of m) in the FP64 record, so
 // no division sits on its chain of dependent levels; k_moments_norm then
@@ -793,27 +793,38 @@ __device__ __forceinline__ void put_moments(const csgd_t &dd, int node, double s
 // order, so the two smallest caller indices of a cell are its first two.
 constexpr int MOM_DIRECT = 16;
 
+// The ticket of a cell: one gpu-scope acquire-release add. Release: this
+// thread's sums (stored above) are visible to whichever child takes the last
+// ticket; acquire: the last child sees every sibling's sums (the adds on one
+// ticket form a release sequence).
+__device__ __forceinline__ int ticket_take(int *p)
+{
+    int old;
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+    return old;
+}
+
 template <bool EXPORT>
-__device__ __forceinline__ void moments_climb(const csgd_t &dd, int node, double ax, double ay,
-                                              double az, double M, int2 mi)
+__device__ __forceinline__ void moments_climb(const csgd_t &dd, int node, int parent, double ax,
+                                              double ay, double az, double M, int2 mi)
 {
     while (true) {
         put_raw(dd, node, ax, ay, az, M);
         if (EXPORT)
             dd.minidx[node] = mi;
-        int parent = dd.link[node].parent;
         if (parent < 0 || parent >= node)
             break; // preorder: a parent always precedes its children
-        __threadfence();
-        int t = atomicAdd(&dd.ticket[parent], 1);
-        if (t != __ldcg(&dd.nchild[parent]) - 1)
+        // the parent's children, their count and its own parent are fixed
+        // since k_link: their loads run while the sums above drain
+        const int4 *cp = (const int4 *)(dd.child + 8 * (size_t)parent);
+        const int4 c03 = __ldg(cp), c47 = __ldg(cp + 1);
+        const int nc = __ldg(&dd.nchild[parent]);
+        const int up = __ldg(&dd.link[parent].parent);
+        if (ticket_take(&dd.ticket[parent]) != nc - 1)
             break;
-        __threadfence();
         M = 0.0;
         ax = ay = az = 0.0;
         int m1 = INT_MAX, m2 = INT_MAX;
-        const int4 *cp = (const int4 *)(dd.child + 8 * (size_t)parent);
-        const int4 c03 = __ldcg(cp), c47 = __ldcg(cp + 1);
         const int ch[8] = {c03.x, c03.y, c03.z, c03.w, c47.x, c47.y, c47.z, c47.w};
         for (int q = 0; q < 8; q++) {
             const int c = ch[q];
@@ -841,8 +852,13 @@ __device__ __forceinline__ void moments_climb(const csgd_t &dd, int node, double
         }
         mi = make_int2(m1, m2);
         node = parent;
+        parent = up;
     }
 }
+
+// Bodies summed directly, four bodies' loads in flight at a time; the additions
+// keep the sorted order (M += m, then sum += m x as one fused multiply-add).
+constexpr int MOM_LOADS = 4;
 
 template <bool EXPORT>
 __device__ __forceinline__ void moments_cell(const csgd_t &dd, int id, const double *__restrict__ x,
@@ -855,31 +871,52 @@ __device__ __forceinline__ void moments_cell(const csgd_t &dd, int id, const dou
     const bool leaf = dd.nchild[id] == 0;
     if ((!leaf && l.count > MOM_DIRECT) || l.count < 1)
         return; // formed by the climb (or a cell without bodies)
+    // a parent of at most MOM_DIRECT bodies sums its own bodies
+    const int pcount = (l.parent >= 0) ? __ldg(&dd.link[l.parent].count) : INT_MAX;
     double M = 0.0, ax = 0.0, ay = 0.0, az = 0.0;
     int2 mi = make_int2(INT_MAX, INT_MAX);
-    for (int k = 0; k < l.count; k++) {
-        const int b = perm[l.first + k];
-        const double mb = m[b];
-        M += mb;
-        ax += mb * x[b];
-        ay += mb * y[b];
-        az += mb * z[b];
-        if (EXPORT) {
-            if (b < mi.x) {
-                mi.y = mi.x;
-                mi.x = b;
-            } else if (b < mi.y) {
-                mi.y = b;
+    for (int k0 = 0; k0 < l.count; k0 += MOM_LOADS) {
+        int bb[MOM_LOADS];
+        double mv[MOM_LOADS], xv[MOM_LOADS], yv[MOM_LOADS], zv[MOM_LOADS];
+#pragma unroll
+        for (int j = 0; j < MOM_LOADS; j++)
+            bb[j] = (k0 + j < l.count) ? perm[l.first + k0 + j] : -1;
+#pragma unroll
+        for (int j = 0; j < MOM_LOADS; j++) {
+            if (bb[j] >= 0) {
+                mv[j] = m[bb[j]];
+                xv[j] = x[bb[j]];
+                yv[j] = y[bb[j]];
+                zv[j] = z[bb[j]];
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < MOM_LOADS; j++) {
+            if (bb[j] < 0)
+                break;
+            const int b = bb[j];
+            const double mb = mv[j];
+            M += mb;
+            ax += mb * xv[j];
+            ay += mb * yv[j];
+            az += mb * zv[j];
+            if (EXPORT) {
+                if (b < mi.x) {
+                    mi.y = mi.x;
+                    mi.x = b;
+                } else if (b < mi.y) {
+                    mi.y = b;
+                }
             }
         }
     }
-    if (l.parent >= 0 && dd.link[l.parent].count <= MOM_DIRECT) {
+    if (pcount <= MOM_DIRECT) {
         put_raw(dd, id, ax, ay, az, M); // the parent sums its own bodies
         if (EXPORT)
             dd.minidx[id] = mi;
         return;
     }
-    moments_climb<EXPORT>(dd, id, ax, ay, az, M, mi);
+    moments_climb<EXPORT>(dd, id, l.parent, ax, ay, az, M, mi);
 }
 
 // Raw sums to centre of mass, every cell: a single-body leaf keeps the body's
@@ -908,7 +945,7 @@ __global__ void k_moments_norm(csgd_t dd, DevScalars *sc, const double *__restri
 }
 
 template <bool EXPORT>
-__global__ void k_moments(csgd_t dd, DevScalars *sc, const double *__restrict__ x,
+__global__ void __launch_bounds__(256, 4) k_moments(csgd_t dd, DevScalars *sc, const double *__restrict__ x,
                           const double *__restrict__ y, const double *__restrict__ z,
                           const double *__restrict__ m, const int *__restrict__ perm)
 {
