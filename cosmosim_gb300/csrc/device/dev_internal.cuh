@@ -275,6 +275,49 @@ extern "C" int csgd_ensure_tree_extras(csgd_t *d, int geometry, int pool);
 void csgd_set_err(csgd_t *d, int code);
 int csgd_grid(long long n, int block);
 
+// ---- programmatic dependent launch ----
+// csgd_launch queues a kernel whose blocks may be scheduled while the kernel
+// before it in the stream still runs, so a chain of short kernels does not
+// pay each launch after the previous kernel's end. Every kernel queued this
+// way begins with pdl_wait(), which returns once the previous kernel has
+// completed and its writes are visible, before any global memory access;
+// pdl_release() then lets the next kernel's blocks be scheduled. Both are
+// no-ops in a kernel launched without the attribute. The tree build and its
+// sort and scans launch this way; the walks, kicks and SPH passes do not: with
+// SPH on its own stream beside the walk, blocks scheduled early and waiting
+// take SM slots from the other stream's kernels (100k merger substep 1.11 ->
+// 1.14 ms when they did).
+__device__ __forceinline__ void pdl_wait()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_release()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_enter()
+{
+    pdl_wait();
+    pdl_release();
+}
+template <typename... P, typename... A>
+inline void csgd_launch(csgd_t *d, void (*k)(P...), int grid, int block, cudaStream_t s,
+                        A &&...args)
+{
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, static_cast<A &&>(args)...);
+    d->launches++;
+}
+
 // ---- sort / scan utilities (dev_sort.cu) ----
 // Stable LSD radix sort of (key, value) over n items, on key bits [0, bits).
 // Result in (key, val); alt buffers are scratch of the same size. With n_dev

@@ -56,6 +56,7 @@ __device__ __forceinline__ int warp_incl_scan(int v)
 __global__ void k_scan_tile(const int *__restrict__ in, int *__restrict__ out, int n,
                             const int *__restrict__ limit, int *__restrict__ sums)
 {
+    pdl_enter();
     __shared__ int warp_tot[SCAN_THREADS / 32];
     const int lim = limit ? min(n, *limit) : n;
     const long long base = (long long)blockIdx.x * SCAN_TILE + (long long)threadIdx.x * SCAN_ITEMS;
@@ -101,6 +102,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_small(const int *__restri
                                                              int *__restrict__ out, int n,
                                                              const int *__restrict__ limit)
 {
+    pdl_enter();
     __shared__ int warp_tot[SCAN_THREADS / 32];
     __shared__ int tile_tot;
     const int lim = limit ? min(n, *limit) : n;
@@ -145,6 +147,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_small(const int *__restri
 
 __global__ void k_scan_add(int *__restrict__ out, int n, const int *__restrict__ offs)
 {
+    pdl_enter();
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n)
         out[i] += offs[i / SCAN_TILE];
@@ -152,6 +155,7 @@ __global__ void k_scan_add(int *__restrict__ out, int n, const int *__restrict__
 
 __global__ void k_scan_total(int *__restrict__ out, int n, const int *__restrict__ total)
 {
+    pdl_enter();
     out[n] = *total;
 }
 
@@ -214,6 +218,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_counts(const unsigned lo
                                                                int passes,
                                                                unsigned int *__restrict__ counts)
 {
+    pdl_enter();
     if (n_dev)
         n = max(0, min(n, *n_dev));
     __shared__ unsigned int h[8][RADIX];
@@ -255,6 +260,7 @@ __global__ void __launch_bounds__(SORT_THREADS) k_radix_onesweep(
     unsigned long long *status, unsigned long long *__restrict__ status_next, int nblocks,
     const int *__restrict__ n_dev, DevScalars *sc, int wait_polls)
 {
+    pdl_enter();
     constexpr int TILE = sort_tile(IPL);
     if (n_dev) { // key count known on the device only: the grid covers the bound
         n = max(0, min(n, *n_dev));
@@ -426,7 +432,7 @@ int csg_scan_exclusive(csgd_t *d, const int *in, int *out, int n, const int *cou
         return csgd_check(d, cudaGetLastError());
     }
     if (n <= SCAN_SMALL) {
-        { k_scan_small<<<1, SCAN_THREADS, 0, d->stream>>>(in, out, n, count_limit); d->launches++; }
+        csgd_launch(d, k_scan_small, 1, SCAN_THREADS, d->stream, in, out, n, count_limit);
         return csgd_check(d, cudaGetLastError());
     }
     // level sizes: n -> ceil(n/T) -> ... -> 1
@@ -440,7 +446,7 @@ int csg_scan_exclusive(csgd_t *d, const int *in, int *out, int n, const int *cou
         csgd_set_err(d, CSG_ERR_NOMEM);
         return CSG_ERR_NOMEM;
     }
-    { k_scan_tile<<<nb, SCAN_THREADS, 0, d->stream>>>(in, out, n, count_limit, sums); d->launches++; }
+    csgd_launch(d, k_scan_tile, nb, SCAN_THREADS, d->stream, in, out, n, count_limit, sums);
     if (nb > 1) {
         // scan the block sums (exclusive, total at sums_out[nb]) and add back
         int *sums_out = sums + nb + 1;
@@ -454,10 +460,10 @@ int csg_scan_exclusive(csgd_t *d, const int *in, int *out, int n, const int *cou
         d->scan_tmp_cap = saved_cap;
         if (rc)
             return rc;
-        { k_scan_add<<<csgd_grid(n, 256), 256, 0, d->stream>>>(out, n, sums_out); d->launches++; }
-        { k_scan_total<<<1, 1, 0, d->stream>>>(out, n, sums_out + nb); d->launches++; }
+        csgd_launch(d, k_scan_add, csgd_grid(n, 256), 256, d->stream, out, n, sums_out);
+        csgd_launch(d, k_scan_total, 1, 1, d->stream, out, n, sums_out + nb);
     } else {
-        { k_scan_total<<<1, 1, 0, d->stream>>>(out, n, sums); d->launches++; }
+        csgd_launch(d, k_scan_total, 1, 1, d->stream, out, n, sums);
     }
     return csgd_check(d, cudaGetLastError());
 }
@@ -487,7 +493,7 @@ int csg_radix_sort(csgd_t *d, unsigned long long *key, int *val, unsigned long l
     int gc = d->num_sms * 4;
     if (gc > nblocks)
         gc = nblocks;
-    { k_radix_counts<<<gc, SORT_THREADS, 0, d->stream>>>(key, n, n_dev, passes, counts); d->launches++; }
+    csgd_launch(d, k_radix_counts, gc, SORT_THREADS, d->stream, key, n, n_dev, passes, counts);
     unsigned long long *ki = key, *ko = key_alt;
     int *vi = val, *vo = val_alt;
     for (int p = 0; p < passes; p++) {
@@ -495,11 +501,11 @@ int csg_radix_sort(csgd_t *d, unsigned long long *key, int *val, unsigned long l
         unsigned long long *st = status + (size_t)(p & 1) * status_words;
         unsigned long long *st_next = status + (size_t)((p + 1) & 1) * status_words;
         if (tiny)
-            { k_radix_onesweep<2><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, n_dev, d->sc, CSG_WAIT_POLLS_DEFAULT); d->launches++; }
+            csgd_launch(d, k_radix_onesweep<2>, nblocks, SORT_THREADS, d->stream, ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, n_dev, d->sc, CSG_WAIT_POLLS_DEFAULT);
         else if (small)
-            { k_radix_onesweep<4><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, n_dev, d->sc, CSG_WAIT_POLLS_DEFAULT); d->launches++; }
+            csgd_launch(d, k_radix_onesweep<4>, nblocks, SORT_THREADS, d->stream, ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, n_dev, d->sc, CSG_WAIT_POLLS_DEFAULT);
         else
-            { k_radix_onesweep<8><<<nblocks, SORT_THREADS, 0, d->stream>>>(ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, n_dev, d->sc, CSG_WAIT_POLLS_DEFAULT); d->launches++; }
+            csgd_launch(d, k_radix_onesweep<8>, nblocks, SORT_THREADS, d->stream, ki, vi, ko, vo, n, shift, counts + RADIX * p, tile_ctr + p, st, st_next, nblocks, n_dev, d->sc, CSG_WAIT_POLLS_DEFAULT);
         unsigned long long *tk = ki;
         ki = ko;
         ko = tk;

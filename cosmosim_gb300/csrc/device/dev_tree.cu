@@ -128,6 +128,7 @@ __device__ __forceinline__ int digit_at(const unsigned long long *__restrict__ k
 
 __global__ void k_reset(DevScalars *sc, DevRoot *roots, int n_gal)
 {
+    pdl_enter();
     for (int g = threadIdx.x; g < n_gal; g += blockDim.x) {
         for (int a = 0; a < 3; a++) {
             roots[g].omin[a] = ~0ull;
@@ -200,6 +201,7 @@ __global__ void k_bbox(const double *__restrict__ x, const double *__restrict__ 
                        const double *__restrict__ z, const double *__restrict__ m,
                        const int *__restrict__ gid, int n, DevRoot *roots, DevScalars *gsc)
 {
+    pdl_enter();
     unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0ull, 0ull, 0ull};
     int cnt = 0;
     int cur_g = -1; // warp-uniform: the system the running box belongs to
@@ -355,6 +357,7 @@ __device__ void root_cube(DevRoot *sc)
 // the sorted order (systems sort in id order) and the total alive count.
 __global__ void k_root(DevScalars *sc, DevRoot *roots, int n_gal)
 {
+    pdl_enter();
     // After an error (non-finite input found by k_bbox, or an earlier failure
     // not yet collected) the tree is built empty: no key is formed from the
     // bodies and nothing downstream walks them.
@@ -401,6 +404,7 @@ __global__ void k_keys(const double *__restrict__ x, const double *__restrict__ 
                        const DevRoot *__restrict__ roots, unsigned long long *__restrict__ key,
                        int *__restrict__ perm)
 {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n)
         return;
@@ -432,6 +436,7 @@ __global__ void k_keys(const double *__restrict__ x, const double *__restrict__ 
 __global__ void k_sgid(const DevScalars *sc, const int *__restrict__ perm,
                        const int *__restrict__ gid, int *__restrict__ sgid, int n)
 {
+    pdl_enter();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p < n)
         sgid[p] = (p < sc->n_alive) ? gid[perm[p]] : -1;
@@ -450,6 +455,7 @@ __global__ void k_deep_mark(const double *__restrict__ x, const double *__restri
                             const int *__restrict__ sgid, const int *__restrict__ perm,
                             unsigned long long *__restrict__ ext)
 {
+    pdl_enter();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const int na = sc->n_alive;
     if (p >= na)
@@ -482,6 +488,7 @@ __global__ void k_deep_sort(DevScalars *sc, const unsigned long long *__restrict
                             const int *__restrict__ sgid, int *__restrict__ perm,
                             unsigned long long *__restrict__ ext)
 {
+    pdl_enter();
     if (sc->deep == 0)
         return;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -523,6 +530,7 @@ __global__ void k_count(DevScalars *sc, const unsigned long long *__restrict__ k
                         const unsigned long long *__restrict__ ext, const int *__restrict__ sgid,
                         signed char *__restrict__ lcp, int *__restrict__ cnt)
 {
+    pdl_enter();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     const int na = sc->n_alive;
     if (p >= na)
@@ -623,6 +631,7 @@ __global__ void k_nodes(csgd_t dd, DevScalars *sc, const DevRoot *__restrict__ r
                         const signed char *__restrict__ lcp, const int *__restrict__ base,
                         const int *__restrict__ perm, int *__restrict__ leaf_of)
 {
+    pdl_enter();
     // one thread per cell (and, for positions without a leaf, per position;
     // grid-stride beyond the grid): the cells of a position are written by as
     // many threads, so no thread walks the searches of a whole column of levels
@@ -690,6 +699,7 @@ __global__ void k_nodes(csgd_t dd, DevScalars *sc, const DevRoot *__restrict__ r
 __global__ void k_tasks(DevScalars *sc, DevRoot *roots, int n_gal, const int *__restrict__ base,
                         WalkTask *tasks, int task_cap, int imported)
 {
+    pdl_enter();
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         int t = 0;
         for (int g = 0; g < n_gal; g++) {
@@ -740,6 +750,7 @@ __global__ void k_tasks(DevScalars *sc, DevRoot *roots, int n_gal, const int *__
 __global__ void k_link(csgd_t dd, DevScalars *sc, const unsigned long long *__restrict__ key,
                        const unsigned long long *__restrict__ ext)
 {
+    pdl_enter();
     const int nn = sc->n_nodes;
     if (nn > dd.node_cap)
         return;
@@ -925,6 +936,7 @@ __device__ __forceinline__ void moments_cell(const csgd_t &dd, int id, const dou
 __global__ void k_moments_norm(csgd_t dd, DevScalars *sc, const double *__restrict__ x,
                                const double *__restrict__ y, const double *__restrict__ z)
 {
+    pdl_enter();
     const int nn = sc->n_nodes;
     if (nn > dd.node_cap || sc->n_alive == 0)
         return;
@@ -949,6 +961,7 @@ __global__ void __launch_bounds__(256, 4) k_moments(csgd_t dd, DevScalars *sc, c
                           const double *__restrict__ y, const double *__restrict__ z,
                           const double *__restrict__ m, const int *__restrict__ perm)
 {
+    pdl_enter();
     const int nn = sc->n_nodes;
     if (nn > dd.node_cap || sc->n_alive == 0)
         return;
@@ -990,6 +1003,7 @@ __global__ void k_geometry(csgd_t dd, DevScalars *sc, const DevRoot *__restrict_
                            const unsigned long long *__restrict__ ext,
                            const int *__restrict__ sgid)
 {
+    pdl_enter();
     const int nn = sc->n_nodes;
     if (nn > dd.node_cap)
         return;
@@ -1248,6 +1262,7 @@ __global__ void k_gal_keys(const DevScalars *sc, const int *__restrict__ perm,
                            const int *__restrict__ gid, unsigned long long *__restrict__ gk,
                            int *__restrict__ idx, int n, int n_gal)
 {
+    pdl_enter();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= n)
         return;
@@ -1260,6 +1275,7 @@ __global__ void k_gather_sorted(const int *__restrict__ idx,
                                 const int *__restrict__ perm, unsigned long long *__restrict__ key2,
                                 int *__restrict__ perm2, int n)
 {
+    pdl_enter();
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n)
         return;
@@ -1278,14 +1294,14 @@ static int order_bodies(csgd_t *d)
     const int B = 256;
     const int G = d->n_gal;
     csgd_build_mark(d, 0);
-    { k_reset<<<1, 256, 0, s>>>(sc, d->roots, G); d->launches++; }
+    csgd_launch(d, k_reset, 1, 256, s, sc, d->roots, G);
     // few blocks: each warp flushes its running box with atomics on the same
     // words, so fewer warps contend less (4 blocks per SM keep HBM busy)
     int gb = min(csgd_grid(n, B), 4 * d->num_sms);
-    { k_bbox<<<gb > 0 ? gb : 1, B, 0, s>>>(d->x, d->y, d->z, d->m, d->gid, n, d->roots, sc); d->launches++; }
-    { k_root<<<1, 256, 0, s>>>(sc, d->roots, G); d->launches++; }
+    csgd_launch(d, k_bbox, gb > 0 ? gb : 1, B, s, d->x, d->y, d->z, d->m, d->gid, n, d->roots, sc);
+    csgd_launch(d, k_root, 1, 256, s, sc, d->roots, G);
     if (n > 0)
-        { k_keys<<<csgd_grid(n, B), B, 0, s>>>(d->x, d->y, d->z, d->m, d->gid, n, sc, d->roots, d->key, d->perm); d->launches++; }
+        csgd_launch(d, k_keys, csgd_grid(n, B), B, s, d->x, d->y, d->z, d->m, d->gid, n, sc, d->roots, d->key, d->perm);
     csgd_build_mark(d, 1);
     int rc = csg_radix_sort(d, d->key, d->perm, d->key_alt, d->perm_alt, n, 64);
     if (rc)
@@ -1293,21 +1309,21 @@ static int order_bodies(csgd_t *d)
     if (G > 1 && n > 1) {
         // stable pass on the system id: order (system, key)
         const int g = csgd_grid(n, B);
-        { k_gal_keys<<<g, B, 0, s>>>(sc, d->perm, d->gid, d->ord_key, d->ord_id, n, G); d->launches++; }
+        csgd_launch(d, k_gal_keys, g, B, s, sc, d->perm, d->gid, d->ord_key, d->ord_id, n, G);
         int bits = 1; // system ids 0..G (G marks dead bodies)
         while (bits < 31 && (1 << bits) <= G)
             bits++;
         rc = csg_radix_sort(d, d->ord_key, d->ord_id, d->ord_key_alt, d->ord_id_alt, n, bits);
         if (rc)
             return rc;
-        { k_gather_sorted<<<g, B, 0, s>>>(d->ord_id, d->key, d->perm, d->key_alt, d->perm_alt, n); d->launches++; }
+        csgd_launch(d, k_gather_sorted, g, B, s, d->ord_id, d->key, d->perm, d->key_alt, d->perm_alt, n);
         // back into (key, perm): the buffers keep their roles, so a captured
         // substep and direct launches always agree on where the order is
         cudaMemcpyAsync(d->key, d->key_alt, sizeof(unsigned long long) * (size_t)n,
                         cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(d->perm, d->perm_alt, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, s);
     }
-    { k_sgid<<<csgd_grid(n > 0 ? n : 1, B), B, 0, s>>>(sc, d->perm, d->gid, d->sgid, n); d->launches++; }
+    csgd_launch(d, k_sgid, csgd_grid(n > 0 ? n : 1, B), B, s, sc, d->perm, d->gid, d->sgid, n);
     return csgd_check(d, cudaGetLastError());
 }
 
@@ -1331,30 +1347,30 @@ extern "C" int csgd_build_tree(csgd_t *d, int geometry)
         return rc;
     const int g = csgd_grid(n > 0 ? n : 1, B);
     csgd_build_mark(d, 2);
-    { k_deep_mark<<<g, B, 0, s>>>(d->x, d->y, d->z, sc, d->roots, d->key, d->sgid, d->perm, d->ext); d->launches++; }
-    { k_deep_sort<<<g, B, 0, s>>>(sc, d->key, d->sgid, d->perm, d->ext); d->launches++; }
-    { k_count<<<g, B, 0, s>>>(sc, d->key, d->ext, d->sgid, d->lcp, d->cnt); d->launches++; }
+    csgd_launch(d, k_deep_mark, g, B, s, d->x, d->y, d->z, sc, d->roots, d->key, d->sgid, d->perm, d->ext);
+    csgd_launch(d, k_deep_sort, g, B, s, sc, d->key, d->sgid, d->perm, d->ext);
+    csgd_launch(d, k_count, g, B, s, sc, d->key, d->ext, d->sgid, d->lcp, d->cnt);
     rc = csg_scan_exclusive(d, d->cnt, d->base, n, &sc->n_alive);
     if (rc)
         return rc;
     // d->cnt (the counts, consumed by the scan) now holds each position's leaf
     const int gn = csgd_grid(cell_threads(d), B); // >= cells and >= positions
-    { k_nodes<<<gn, B, 0, s>>>(*d, sc, d->roots, d->key, d->ext, d->sgid, d->lcp, d->base, d->perm, d->cnt); d->launches++; }
-    { k_link<<<gn, B, 0, s>>>(*d, sc, d->key, d->ext); d->launches++; }
+    csgd_launch(d, k_nodes, gn, B, s, *d, sc, d->roots, d->key, d->ext, d->sgid, d->lcp, d->base, d->perm, d->cnt);
+    csgd_launch(d, k_link, gn, B, s, *d, sc, d->key, d->ext);
     csgd_build_mark(d, 3);
     if (d->export_order)
-        { k_moments<true><<<gn, B, 0, s>>>(*d, sc, d->x, d->y, d->z, d->m, d->perm); d->launches++; }
+        csgd_launch(d, k_moments<true>, gn, B, s, *d, sc, d->x, d->y, d->z, d->m, d->perm);
     else
-        { k_moments<false><<<gn, B, 0, s>>>(*d, sc, d->x, d->y, d->z, d->m, d->perm); d->launches++; }
-    { k_moments_norm<<<gn, B, 0, s>>>(*d, sc, d->x, d->y, d->z); d->launches++; }
+        csgd_launch(d, k_moments<false>, gn, B, s, *d, sc, d->x, d->y, d->z, d->m, d->perm);
+    csgd_launch(d, k_moments_norm, gn, B, s, *d, sc, d->x, d->y, d->z);
     d->minidx_valid = d->export_order;
     csgd_build_mark(d, 4);
-    { k_tasks<<<min(d->n_gal, 152), 256, 0, s>>>(sc, d->roots, d->n_gal, d->base, d->tasks, d->task_cap, 0); d->launches++; }
+    csgd_launch(d, k_tasks, min(d->n_gal, 152), 256, s, sc, d->roots, d->n_gal, d->base, d->tasks, d->task_cap, 0);
     d->geometry_valid = 0;
     d->imported = 0;
     d->gas_valid = 0;
     if (geometry) {
-        { k_geometry<<<gn, B, 0, s>>>(*d, sc, d->roots, d->key, d->ext, d->sgid); d->launches++; }
+        csgd_launch(d, k_geometry, gn, B, s, *d, sc, d->roots, d->key, d->ext, d->sgid);
         d->geometry_valid = 1;
     }
     csgd_build_mark(d, 5);
