@@ -6,11 +6,13 @@ import json
 import subprocess
 import sys
 
+import pytest
+
 from conftest import ROOT
 
 SCRIPT = r"""
 import contextlib, io, json, sys
-sys.argv = ["bench.py", "--impl", "reference", "--config", "disk20k", "--steps", "1",
+sys.argv = ["bench.py", "--impl", "reference", "--config", CONFIG, "--steps", "1",
             "--warmup", "3"]
 import bench
 buf = io.StringIO()
@@ -22,8 +24,10 @@ print(json.dumps({"line": buf.getvalue().strip().splitlines()[-1],
 """
 
 
-def test_reference_arm_line_and_no_product_library():
-    r = subprocess.run([sys.executable, "-c", SCRIPT], cwd=ROOT, capture_output=True, text=True,
+@pytest.mark.parametrize("config,n_bodies", [("disk20k", 20000), ("ensemble64", 1102884)])
+def test_reference_arm_line_and_no_product_library(config, n_bodies):
+    script = SCRIPT.replace("CONFIG", repr(config))
+    r = subprocess.run([sys.executable, "-c", script], cwd=ROOT, capture_output=True, text=True,
                        timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     out = json.loads(r.stdout.strip().splitlines()[-1])
@@ -36,7 +40,7 @@ def test_reference_arm_line_and_no_product_library():
     assert line["impl"] == "reference"
     assert line["value"] > 0 and line["steps"] == 1 and line["warmup"] == 3
     assert line["higher_is_better"] is True
-    assert line["config"]["n_bodies"] == 20000
+    assert line["config"]["n_bodies"] == n_bodies
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["cpu_baseline"]["value"] == line["value"]
     e2e = line["e2e"]
