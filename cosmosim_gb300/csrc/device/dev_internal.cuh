@@ -283,10 +283,10 @@ int csgd_grid(long long n, int block);
 // completed and its writes are visible, before any global memory access;
 // pdl_release() then lets the next kernel's blocks be scheduled. Both are
 // no-ops in a kernel launched without the attribute. The tree build and its
-// sort and scans launch this way; the walks, kicks and SPH passes do not: with
-// SPH on its own stream beside the walk, blocks scheduled early and waiting
-// take SM slots from the other stream's kernels (100k merger substep 1.11 ->
-// 1.14 ms when they did).
+// sort and scans launch this way; the walks, kicks and SPH passes do not (the
+// 100k merger substep, SPH on its own stream beside the walk, went from 1.11
+// to 1.14 ms when they did, likely because blocks scheduled early and waiting
+// hold SM slots the other stream's kernels could use).
 __device__ __forceinline__ void pdl_wait()
 {
     asm volatile("griddepcontrol.wait;" ::: "memory");
